@@ -1,0 +1,104 @@
+"""Builds the GB300 kernel set in-tree with nvcc (sm_103a only).
+
+Outputs (git-ignored):
+  flow_gb300/libflow_gb300.so   the kernel set + C ABI of include/flow_gb300.h
+  flow_gb300/flow.gb300         the C host driver (host/flow_main.c)
+
+Usage: ``python -m flow_gb300.build`` or ``flow_gb300.build.build()``.
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+import sys
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(PKG)
+CSRC = os.path.join(PKG, "csrc")
+OBJ = os.path.join(PKG, "_build")
+LIB = os.path.join(PKG, "libflow_gb300.so")
+DRIVER = os.path.join(PKG, "flow.gb300")
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
+              "-Xcompiler", "-O2", "-I" + os.path.join(ROOT, "include")]
+
+# Per-translation-unit flags.  stages.cu reproduces the reference's IEEE
+# evaluation order, so it must not contract a*b+c into fused multiply-adds.
+UNIT_FLAGS = {
+    "stages.cu": ["--fmad=false"],
+}
+
+SOURCES = ["stages.cu", "interface.cu", "fused.cu"]
+
+
+def _nvcc() -> str:
+    for cand in (shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and os.path.exists(cand):
+            return cand
+    raise RuntimeError("nvcc not found: the GB300 kernel set needs the CUDA toolkit")
+
+
+def _stale(target: str, deps: list[str]) -> bool:
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def _headers() -> list[str]:
+    hs = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
+    inc = os.path.join(ROOT, "include")
+    hs += [os.path.join(inc, f) for f in os.listdir(inc) if f.endswith(".h")]
+    return hs
+
+
+def _compile(src: str, verbose: bool) -> str:
+    obj = os.path.join(OBJ, os.path.splitext(src)[0] + ".o")
+    deps = [os.path.join(CSRC, src), __file__] + _headers()
+    if _stale(obj, deps):
+        cmd = [_nvcc(), *ARCH, *NVCC_FLAGS, *UNIT_FLAGS.get(src, []), "-c",
+               os.path.join(CSRC, src), "-o", obj]
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        subprocess.run(cmd, check=True)
+    return obj
+
+
+def build(verbose: bool = False, jobs: int | None = None) -> str:
+    """Compiles every CUDA unit (in parallel) and links the shared library."""
+    os.makedirs(OBJ, exist_ok=True)
+    srcs = [s for s in SOURCES if os.path.exists(os.path.join(CSRC, s))]
+    with cf.ThreadPoolExecutor(max_workers=jobs or min(8, os.cpu_count() or 2)) as ex:
+        objs = list(ex.map(lambda s: _compile(s, verbose), srcs))
+    if _stale(LIB, objs):
+        cuda_lib = os.path.join(os.path.dirname(os.path.dirname(_nvcc())), "lib64")
+        cmd = [_nvcc(), *ARCH, "-shared", "-cudart", "shared", "-Xlinker", "-rpath," + cuda_lib,
+               "-o", LIB, *objs]
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        subprocess.run(cmd, check=True)
+    _build_driver(verbose)
+    return LIB
+
+
+def _build_driver(verbose: bool) -> None:
+    src = os.path.join(PKG, "host", "flow_main.c")
+    if not os.path.exists(src):
+        return
+    if not _stale(DRIVER, [src, LIB] + _headers()):
+        return
+    cuda_lib = os.path.join(os.path.dirname(os.path.dirname(_nvcc())), "lib64")
+    cmd = ["gcc", "-O2", "-std=gnu99", "-I" + os.path.join(ROOT, "include"), src,
+           "-o", DRIVER, "-L" + PKG, "-lflow_gb300", "-Wl,-rpath,$ORIGIN",
+           "-L" + cuda_lib, "-Wl,-rpath," + cuda_lib, "-lcudart", "-lm"]
+    if verbose:
+        print(" ".join(cmd), flush=True)
+    subprocess.run(cmd, check=True)
+
+
+if __name__ == "__main__":
+    build(verbose="-v" in sys.argv)
+    print(LIB)

@@ -1,0 +1,25 @@
+// fused.h -- the fused FP64 timestep (fused.cu) and helpers shared by the
+// C ABI in interface.cu.
+#pragma once
+
+#include "../../include/flow_mesh.h"
+#include "stages.h"
+
+namespace flow {
+
+int record_error(int code, const char* fmt, ...);
+int check_launch(const char* where);
+int check_mesh(const Mesh* m, int nx, int ny, const char* where);
+int check_sizes(int nx, int ny, int pad, const char* where);
+cudaStream_t current_stream();
+int verbose();
+
+// One full timestep with the fused kernels; dt/dt_h stay on the device inside
+// the step and are copied to mesh->dt/dt_h before returning.
+int fused_solve(Mesh* mesh, int tt, double* P, double* rho, double* rho_old,
+                double* e, double* u, double* v, double* rho_u, double* rho_v,
+                double* Qxx, double* Qyy, double* F_x, double* F_y,
+                double* uF_x, double* uF_y, double* vF_x, double* vF_y,
+                double* reduce_array);
+
+}  // namespace flow

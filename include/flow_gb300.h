@@ -1,0 +1,189 @@
+/*
+ * flow_gb300.h -- C ABI of the GB300 (sm_103a) kernel set for the flow
+ * mini-app.
+ *
+ * Part 1 is the reference's own kernel-set interface, with identical names,
+ * argument order and meaning, so that an unmodified host driver (main.c) can
+ * select this set the way it selects omp3 or cuda (`KERNELS=gb300`).  Part 2
+ * adds status-returning control functions.  Part 3 is the mixed-precision and
+ * batched forms.
+ *
+ * Memory: every array argument is a DEVICE pointer (as for the reference cuda
+ * set).  The Mesh struct is host memory; its edgedx/edgedy/celldx/celldy
+ * arrays are device pointers; mesh->dt and mesh->dt_h are host doubles that
+ * set_timestep and solve_hydro_2d update before returning.  The kernel set
+ * never allocates: its only device scratch is the caller's reduce_array,
+ * which must hold at least local_nx*local_ny doubles (the arch default).
+ *
+ * Errors: the reference entry points return void and abort on a CUDA error
+ * (cuda/flow.cu:24 gpu_check).  Here they record the error instead; read it
+ * with gb300_last_error()/gb300_last_error_message().  A failed call leaves
+ * the mesh scalars unchanged.
+ *
+ * Scope: one rank (all Mesh::neighbours must be FLOW_EDGE); pad >= 2 and at
+ * least 2 interior cells per axis.
+ */
+#ifndef FLOW_GB300_H
+#define FLOW_GB300_H
+
+#include "flow_mesh.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ===== Part 1: the reference kernel-set interface ======================== */
+
+/* One timestep (replaces flow_interface.h:16-20; omp3/flow.c:10-52). */
+void solve_hydro_2d(Mesh* mesh, int tt, double* P, double* rho,
+                    double* rho_old, double* e, double* u, double* v,
+                    double* rho_u, double* rho_v, double* Qxx, double* Qyy,
+                    double* F_x, double* F_y, double* uF_x, double* uF_y,
+                    double* vF_x, double* vF_y, double* reduce_array);
+
+/* CFL timestep and leapfrog dt/dt_h update (flow_interface.h:23-26;
+ * omp3/flow.c:73-106).  Blocks until mesh->dt/dt_h are updated. */
+void set_timestep(const int nx, const int ny, double* Qxx, double* Qyy,
+                  const double* rho, const double* e, Mesh* mesh,
+                  double* reduce_array, const int first_step,
+                  const double* celldx, const double* celldy);
+
+/* Interior totals of rho and rho*e, printed on rank 0 when verbose
+ * (flow_interface.h:29-30; omp3/flow.c:973-995). */
+void print_conservation(const int nx, const int ny, double* rho, double* e,
+                        double* reduce_array, Mesh* mesh);
+
+/* Stage entry points (omp3/flow.h:4-88), each with its ghost fills. */
+void equation_of_state(const int nx, const int ny, double* P, const double* rho,
+                       const double* e); /* omp3/flow.h:4 */
+void pressure_acceleration(const int nx, const int ny, Mesh* mesh,
+                           const double dt, double* rho_u, double* rho_v,
+                           double* u, double* v, const double* P,
+                           const double* rho, const double* edgedx,
+                           const double* edgedy, const double* celldx,
+                           const double* celldy); /* omp3/flow.h:9 */
+void artificial_viscosity(const int nx, const int ny, Mesh* mesh,
+                          const double dt, double* Qxx, double* Qyy, double* u,
+                          double* v, double* rho_u, double* rho_v,
+                          const double* rho, const double* edgedx,
+                          const double* edgedy, const double* celldx,
+                          const double* celldy); /* omp3/flow.h:16 */
+void shock_heating_and_work(const int nx, const int ny, Mesh* mesh,
+                            const double dt_h, double* e, const double* P,
+                            const double* u, const double* v, const double* rho,
+                            const double* Qxx, const double* Qyy,
+                            const double* celldx,
+                            const double* celldy); /* omp3/flow.h:24 */
+void advect_mass_and_energy(const int nx, const int ny, Mesh* mesh,
+                            const int tt, const double dt, const double dt_h,
+                            double* rho, double* e, double* rho_old,
+                            double* F_x, double* F_y, double* eF_x,
+                            double* eF_y, const double* u, const double* v,
+                            const double* edgedx, const double* edgedy,
+                            const double* celldx,
+                            const double* celldy); /* omp3/flow.h:31 */
+void momentum_x_flux_in_x(const int nx, const int ny, Mesh* mesh,
+                          const double dt_h, double* velocity_x, double* uF_x,
+                          const double* mass_flux_x, const double* edgedx,
+                          const double* edgedy,
+                          const double* celldx); /* omp3/flow.h:40 */
+void momentum_x_flux_in_y(const int nx, const int ny, Mesh* mesh,
+                          const double dt_h, double* velocity_x,
+                          double* velocity_y, double* uF_y,
+                          const double* mass_flux_y, const double* edgedx,
+                          const double* edgedy,
+                          const double* celldy); /* omp3/flow.h:46 */
+void momentum_y_flux_in_x(const int nx, const int ny, Mesh* mesh,
+                          const double dt_h, const double* velocity_x,
+                          double* velocity_y, double* vF_x,
+                          const double* mass_flux_x, const double* edgedx,
+                          const double* celldy,
+                          const double* celldx); /* omp3/flow.h:53 */
+void momentum_y_flux_in_y(const int nx, const int ny, Mesh* mesh,
+                          const double dt_h, double* velocity_y, double* vF_y,
+                          const double* mass_flux_y, const double* edgedy,
+                          const double* celldx,
+                          const double* celldy); /* omp3/flow.h:60 */
+void advect_momentum(const int nx, const int ny, const int tt, Mesh* mesh,
+                     const double dt_h, const double dt, double* u, double* v,
+                     double* uF_x, double* uF_y, double* vF_x, double* vF_y,
+                     double* rho_u, double* rho_v, const double* rho,
+                     const double* F_x, const double* F_y,
+                     const double* edgedx, const double* edgedy,
+                     const double* celldx,
+                     const double* celldy); /* omp3/flow.h:66 */
+void x_mass_and_energy_flux(const int nx, const int ny, const int first,
+                            Mesh* mesh, const double dt, const double dt_h,
+                            double* rho, double* rho_old, double* e,
+                            const double* u, double* F_x, double* eF_x,
+                            const double* celldx, const double* edgedx,
+                            const double* celldy,
+                            const double* edgedy); /* omp3/flow.h:75 */
+void y_mass_and_energy_flux(const int nx, const int ny, const int first,
+                            Mesh* mesh, const double dt, const double dt_h,
+                            double* rho, double* rho_old, double* e,
+                            const double* v, double* F_y, double* eF_y,
+                            const double* celldx, const double* edgedx,
+                            const double* celldy,
+                            const double* edgedy); /* omp3/flow.h:83 */
+
+/* Reflective ghost fill of one nx x ny device array (the single-rank part of
+ * the arch handle_boundary_2d the reference calls 19 times per step, e.g.
+ * omp3/flow.c:156).  invert: 0 none, 1 negate across x walls, 2 across y. */
+void handle_boundary_2d(const int nx, const int ny, Mesh* mesh, double* arr,
+                        const int invert, const int pack);
+
+/* ===== Part 2: control and status ======================================== */
+
+enum {
+  GB300_OK = 0,
+  GB300_ERR_CUDA = 1,    /* a CUDA call or launch failed */
+  GB300_ERR_ARG = 2,     /* unsupported sizes, null pointers, multi-rank */
+  GB300_ERR_TIMEOUT = 3, /* a bounded device wait ran out */
+  GB300_ERR_STATE = 4    /* device-side status word reported a fault */
+};
+
+/* Timestep implementations selectable for solve_hydro_2d. */
+enum {
+  GB300_MODE_EXACT = 0, /* the stage entry points in sequence; bit-exact
+                           with the reference omp3 set */
+  GB300_MODE_FUSED = 1  /* fused kernels, FP64, within 1e-12 of the
+                           reference; the default */
+};
+
+int gb300_last_error(void);
+const char* gb300_last_error_message(void);
+void gb300_clear_error(void);
+
+/* Stream every launch of this thread goes to (default: the legacy stream). */
+int gb300_set_stream(void* stream);
+void* gb300_get_stream(void);
+
+int gb300_set_mode(int mode);
+int gb300_get_mode(void);
+
+/* 1 (default): print dt and conservation totals as the reference does
+ * (omp3/flow.c:18-20, 991-994); 0: silent. */
+int gb300_set_verbose(int verbose);
+
+int gb300_synchronize(void);
+
+/* Status-returning forms of the Part 1 calls. */
+int gb300_solve_hydro_2d(Mesh* mesh, int tt, double* P, double* rho,
+                         double* rho_old, double* e, double* u, double* v,
+                         double* rho_u, double* rho_v, double* Qxx,
+                         double* Qyy, double* F_x, double* F_y, double* uF_x,
+                         double* uF_y, double* vF_x, double* vF_y,
+                         double* reduce_array);
+
+/* Interior totals: out[0] = sum rho, out[1] = sum rho*e (host array).  With
+ * sync = 0 the totals stay in reduce_array[3..4] and out is not written. */
+int gb300_conservation(int nx, int ny, int pad, const double* rho,
+                       const double* e, double* reduce_array, double* out,
+                       int sync);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FLOW_GB300_H */

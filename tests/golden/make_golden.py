@@ -1,0 +1,97 @@
+"""Generates the golden fixtures of tests/golden/ from the REFERENCE itself.
+
+Run in a container that has the reference sources (it builds
+oracle/_ref/libflow_ref.so from omp3/flow.c with the arch shim):
+
+    python tests/golden/make_golden.py
+
+Each case stores its initial interior density/energy, the params dt, the
+step count, and every array of the reference host state after the run
+(main.c:52-62 layout), plus the dt/dt_h history.  The reference's own
+known-answer vector (flow.tests:1) is checked separately by
+tests/test_oracle.py.
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from oracle import oracle as O  # noqa: E402
+
+
+def _smooth(n_x, n_y, rng, modes=16, kmax=8, amp=0.1):
+    x = (np.arange(n_x) + 0.5) / n_x
+    y = (np.arange(n_y) + 0.5) / n_y
+    f = np.zeros((n_y, n_x))
+    a = rng.uniform(0, 1, modes)
+    a *= amp / a.sum()
+    for k in range(modes):
+        kx, ky = rng.integers(1, kmax + 1, 2)
+        ph = rng.uniform(0, 2 * np.pi)
+        f += a[k] * np.cos(2 * np.pi * (kx * x[None, :] + ky * y[:, None]) + ph)
+    return f
+
+
+def _boxes_state(gnx, gny, boxes):
+    hm = O.HostMesh(gnx, gny)
+    st = O.HostState(hm)
+    O.fill_boxes(hm, st, boxes)
+    return O.PAD, st.interior("rho").copy(), st.interior("e").copy()
+
+
+def _cfl(gnx, gny, e):
+    cs = np.sqrt(O.GAM * (O.GAM - 1.0) * e.max())
+    return min(1.0 / gnx, 1.0 / gny) / cs
+
+
+def cases():
+    rng = np.random.default_rng(20261203)
+    out = {}
+    _, r, e = _boxes_state(24, 20, O.sod_boxes())
+    out["sod_24x20"] = dict(rho=r, e=e, dt=_cfl(24, 20, e), steps=30)
+    _, r, e = _boxes_state(32, 32, O.sedov_boxes(32))
+    out["blast_32"] = dict(rho=r, e=e, dt=_cfl(32, 32, e), steps=40)
+    _, r, e = _boxes_state(40, 40, O.flow_params_boxes())
+    out["refproblem_40"] = dict(rho=r, e=e, dt=1e-3, steps=25)
+    r = 1.0 + _smooth(20, 28, rng)
+    e = 1.0 + _smooth(20, 28, rng)
+    out["smooth_20x28"] = dict(rho=r, e=e, dt=_cfl(20, 28, e), steps=21)
+    r = np.array([[1.0, 0.5], [0.25, 0.75], [0.6, 0.9]])
+    e = np.array([[2.0, 1.0], [1.5, 3.0], [2.5, 0.8]])
+    out["tiny_2x3"] = dict(rho=r, e=e, dt=_cfl(2, 3, e), steps=9)
+    return out
+
+
+def run_case(kind, c):
+    gny, gnx = c["rho"].shape
+    hm = O.HostMesh(gnx, gny, dt=c["dt"])
+    st = O.HostState(hm)
+    O.fill_fields(hm, st, c["rho"], c["e"])
+    O.initial_timestep(hm, st, kind)
+    hist = [(hm.mesh.dt, hm.mesh.dt_h)]
+    for tt in range(c["steps"]):
+        O.step(hm, st, tt, kind)
+        hist.append((hm.mesh.dt, hm.mesh.dt_h))
+    return hm, st, np.array(hist)
+
+
+def main():
+    if not O.have_reference():
+        O.build()
+    assert O.have_reference(), "needs the reference sources to build oracle/_ref"
+    for name, c in cases().items():
+        hm, st, hist = run_case("reference", c)
+        arrays = {f"out_{k}": v for k, v in st.a.items() if k != "reduce"}
+        np.savez_compressed(os.path.join(HERE, f"{name}.npz"), rho0=c["rho"], e0=c["e"],
+                            dt_param=c["dt"], steps=c["steps"], dt_hist=hist, **arrays)
+        print(name, hm.gnx, hm.gny, c["steps"], "dt", hist[-1])
+
+
+if __name__ == "__main__":
+    main()
