@@ -1,0 +1,367 @@
+#!/usr/bin/env python3
+"""Benchmark of the flow timestep on GB300: cell-steps/s of the FP64 solver.
+
+Workload (one "step" = one timestep, solve_hydro_2d + the conservation totals
+the reference driver computes every iteration, main.c:82-91): a Sedov-type
+blast on a 4096^2 uniform mesh, FP64, gamma 1.4, density 1, specific energy
+1e-5 with a central 4x4-cell square at 1e4, zero velocity, reflective walls,
+the params dt set to the CFL estimate of the initial state.  Synthetic data.
+The state (17 arrays of 4100^2 doubles, 2.3 GB) is larger than L2, so no L2
+flush is needed between steps.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Prints one JSON line on rank 0.  With --impl reference the same workload runs
+on the host cores through the CPU oracle (a C restatement of the reference
+omp3 kernel set, bit-exact with it), since the reference has no GPU path that
+builds here.  Under torchrun (N > 1) every rank advances its own independent
+replica (the single-mesh timestep does not shard without a halo exchange).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "cell-steps/s, % HBM peak: FP64 vs mixed/batched at stated L1 err"
+UNIT = "cell-steps/s"
+N_CELLS_SIDE = 4096
+B_ALG_FP64 = 64  # bytes/cell-step: rho, e, rho_u, rho_v read + written once
+
+# Algorithmic bytes per interior cell of each fused kernel: the arrays it must
+# read and write once (8 bytes each).  Used for the per-kernel HBM roofline.
+KERNEL_BYTES_PER_CELL = {
+    "lag_pressure": 8 * 12,      # rho, e, rho_u, rho_v in; P, rho_old, rho_u, rho_v, u, v, 1/rho_x, 1/rho_y out
+    "lag_viscosity": 8 * 5,      # u, v, rho in; Qxx, Qyy out
+    "lag_viscous_accel": 8 * 12,  # Qxx, Qyy, rho_u, rho_v, 1/rho_x, 1/rho_y in; rho_u, rho_v, u, v out (+2 rereads)
+    "lag_energy_dt": 8 * 8,      # rho, P, e, Qxx, Qyy, u, v in; e out
+    "mass_sweep_x": 8 * 7,       # rho, e, rho_old, u in; rho, e, F_x out
+    "mass_sweep_y": 8 * 7,
+    "flux_uFx": 8 * 3,           # u, F_x in; uF_x out
+    "flux_uFy": 8 * 4,           # u, v, F_y in; uF_y out
+    "flux_vFx": 8 * 4,
+    "flux_vFy": 8 * 3,
+    "update_rho_u": 8 * 3,       # flux, rho_u in; rho_u out (+ rho, u when the velocity is recomputed)
+    "update_rho_v": 8 * 3,
+}
+
+
+def parse_args():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=500)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--size", type=int, default=N_CELLS_SIDE)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def dist_env():
+    return (int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)),
+            int(os.environ.get("LOCAL_RANK", 0)))
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.QUERY}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.out = ""
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                self.out, _ = self.proc.communicate()
+
+    def summary(self):
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in (self.out or "").splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# CPU side: the oracle (C restatement of the reference omp3 set).
+
+def _omp_env():
+    ncpu = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(ncpu))
+    os.environ.setdefault("OMP_PROC_BIND", "close")
+    os.environ.setdefault("OMP_PLACES", "cores")
+    return int(os.environ["OMP_NUM_THREADS"])
+
+
+def cpu_run(n: int, steps: int, warmup: int, budget_s: float):
+    """Times the oracle on the same workload; returns (cell-steps/s, steps
+    timed, threads).  Times at most ~budget_s seconds of steps."""
+    threads = _omp_env()
+    from flow_gb300 import problems
+    from oracle import oracle as O
+    prob = problems.sedov(n)
+    hm = O.HostMesh(n, n, dt=prob.dt_param)
+    st = O.HostState(hm)
+    O.fill_fields(hm, st, prob.interior(prob.rho), prob.interior(prob.e))
+    O.initial_timestep(hm, st, "fast")
+    L = O.lib("fast")
+    out = (O.ctypes.c_double * 2)()
+
+    def one(tt):
+        O.step(hm, st, tt, "fast")
+        L.flow_oracle_conservation(hm.nx, hm.ny, O.PAD, O.ptr(st["rho"]), O.ptr(st["e"]),
+                                   O.ctypes.cast(out, O.ctypes.POINTER(O.ctypes.c_double)))
+
+    tt = 0
+    for _ in range(max(1, warmup)):
+        t0 = time.perf_counter()
+        one(tt)
+        tt += 1
+        t_step = time.perf_counter() - t0
+    timed = max(1, min(steps, int(budget_s / max(t_step, 1e-6))))
+    t0 = time.perf_counter()
+    for _ in range(timed):
+        one(tt)
+        tt += 1
+    el = time.perf_counter() - t0
+    return n * n * timed / el, timed, threads
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    value, timed, threads = cpu_run(args.size, args.steps, args.warmup, budget_s=150.0)
+    sample = (f"Sedov {args.size}^2 FP64 timesteps on {threads} host threads: "
+              f"{timed} of {args.steps} requested steps timed after {args.warmup} warm-up")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": args.size * args.size / value * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"sedov_{args.size}_fp64", "nx": args.size, "ny": args.size,
+                   "form": "fp64", "parallelism": "host OpenMP"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# GPU side.
+
+def run_gpu(args):
+    rank, world, local = dist_env()
+    import torch
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    device = f"cuda:{local}"
+    torch.cuda.set_device(device)
+    import flow_gb300 as fg
+    from flow_gb300 import build, problems
+    if not os.path.exists(fg.LIB_PATH):
+        build.build()
+    L = fg.lib()
+    fg.set_stream(torch.cuda.current_stream())
+    fg.set_mode(fg.MODE_FUSED)
+    n = args.size
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    prob = problems.sedov(n)
+    sim = fg.DeviceSim(prob, device)
+    sim.initial_timestep()
+    out2 = (fg.ctypes.c_double * 2)()
+    out2p = fg.ctypes.cast(out2, fg.ctypes.POINTER(fg.ctypes.c_double))
+    nx, ny = sim.nx, sim.ny
+
+    def step():
+        sim.step()
+        if L.gb300_conservation(nx, ny, 2, fg.dptr(sim.a["rho"]), fg.dptr(sim.a["e"]),
+                                fg.dptr(sim.a["reduce"]), out2p, 1) != 0:
+            fg.check()
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+
+    # ---- device-resident timed region ----
+    L.gb300_profile_reset()
+    L.gb300_profile_enable(1)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        barrier()
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(args.steps):
+            step()
+        e1.record()
+        torch.cuda.synchronize()
+        barrier()
+    L.gb300_profile_enable(0)
+    ms = e0.elapsed_time(e1)
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_per_step = ms / args.steps
+    value = world * n * n * args.steps / (ms * 1e-3)
+    mass, energy = out2[0], out2[1]
+
+    kernels = []
+    buf = fg.ctypes.create_string_buffer(64)
+    launches = fg.ctypes.c_longlong()
+    tot = fg.ctypes.c_double()
+    for i in range(L.gb300_profile_count()):
+        L.gb300_profile_entry(i, buf, 64, fg.ctypes.byref(launches), fg.ctypes.byref(tot))
+        kernels.append((buf.value.decode(), launches.value, tot.value))
+    kernels.sort(key=lambda k: -k[2])
+
+    # ---- end to end through the C ABI with host buffers ----
+    fields = ("rho", "e", "rho_u", "rho_v", "u", "v")
+    prob2 = problems.sedov(n)
+    sim2 = fg.DeviceSim(prob2, device)
+    host_in = {f: sim2.a[f].cpu().pin_memory() for f in fields}
+    host_out = {f: torch.empty_like(host_in[f]).pin_memory() for f in fields}
+    torch.cuda.synchronize()
+    barrier()
+    t0 = time.perf_counter()
+    for f in fields:
+        sim2.a[f].copy_(host_in[f], non_blocking=True)
+    sim2.initial_timestep()
+    for _ in range(args.steps):
+        sim2.step()
+        if L.gb300_conservation(nx, ny, 2, fg.dptr(sim2.a["rho"]), fg.dptr(sim2.a["e"]),
+                                fg.dptr(sim2.a["reduce"]), out2p, 1) != 0:
+            fg.check()
+    for f in fields:
+        host_out[f].copy_(sim2.a[f], non_blocking=True)
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    barrier()
+    h2d = sum(host_in[f].numel() * 8 for f in fields)
+    d2h = sum(host_out[f].numel() * 8 for f in fields)
+    e2e_value = world * n * n * args.steps / e2e_s
+    del sim2, host_in, host_out
+
+    if rank != 0:
+        return
+
+    # ---- roofline of the dominant kernel and of the FP64 pipe ----
+    peak, peak_kind = measured_peaks()
+    name, nl, total = kernels[0] if kernels else ("none", 1, float("nan"))
+    cells = (nx - 4) * (ny - 4)
+    bytes_launch = KERNEL_BYTES_PER_CELL.get(name, B_ALG_FP64) * cells
+    achieved = bytes_launch / (total / nl * 1e-3) / 1e9
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic_per_cell.json")
+    if os.path.exists(tpath):
+        with open(tpath) as f:
+            tb = json.load(f).get("fp64", {}).get(name)
+        if tb is not None:
+            traffic = tb * cells
+    fma_rate = fg.ctypes.c_double()
+    L.gb300_measure_fp64_fma_rate(fg.ctypes.byref(fma_rate))
+
+    cpu = None
+    if not args.no_cpu_baseline:
+        cv, timed, threads = cpu_run(n, 64, 1, budget_s=20.0)
+        cpu = {"value": cv, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"Sedov {n}^2 FP64, {timed} timesteps on {threads} host threads "
+                         "(C restatement of the reference omp3 set, OpenMP)"}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"sedov_{n}_fp64", "nx": n, "ny": n, "form": "fp64",
+                   "iterations_timed": args.steps, "l2": "inputs larger than L2 (2.3 GB state)",
+                   "parallelism": "replicas" if world > 1 else "single GPU",
+                   "hbm_fraction_of_step": value / world * B_ALG_FP64 / (peak * 1e9)},
+        "e2e": {"value": e2e_value, "unit": UNIT,
+                "h2d_bytes_per_step": h2d / args.steps, "d2h_bytes_per_step": d2h / args.steps + 32,
+                "what": "initial state H2D from pinned host, K timesteps + conservation readback "
+                        "through the C ABI, final state D2H"},
+        "roofline": {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+                     "peak_kind": peak_kind},
+        "fp64_pipe": {"fma_per_s_peak": fma_rate.value,
+                      "note": "FP64 issue rate measured on this GPU; the FP64 timestep is bound here"},
+        "kernels": [{"name": k, "launches": c, "ms": t, "share": t / sum(x[2] for x in kernels)}
+                    for k, c, t in kernels],
+        "cpu_baseline": cpu,
+        "clocks": clk.summary(),
+        "gpu_launches": 15 * args.steps,
+        "mass": mass, "energy": energy,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -103,6 +103,11 @@ def _declare(L: ctypes.CDLL) -> None:
         "gb300_synchronize": [],
         "gb300_solve_hydro_2d": [M, I] + [P] * 17,
         "gb300_conservation": [I, I, I, P, P, P, P, I],
+        "gb300_profile_enable": [I],
+        "gb300_profile_reset": [],
+        "gb300_profile_count": [],
+        "gb300_profile_entry": [I, ctypes.c_char_p, I, ctypes.POINTER(ctypes.c_longlong), P],
+        "gb300_measure_fp64_fma_rate": [P],
     }
     for name, args in status.items():
         fn = getattr(L, name)

@@ -19,6 +19,7 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 OBJ = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libflow_gb300.so")
+ARCH_LIB = os.path.join(PKG, "libflow_gb300_arch.so")
 DRIVER = os.path.join(PKG, "flow.gb300")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -31,7 +32,7 @@ UNIT_FLAGS = {
     "stages.cu": ["--fmad=false"],
 }
 
-SOURCES = ["stages.cu", "interface.cu", "fused.cu"]
+SOURCES = ["stages.cu", "interface.cu", "fused.cu", "profile.cu", "peaks.cu"]
 
 
 def _nvcc() -> str:
@@ -84,16 +85,27 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
     return LIB
 
 
+def _cuda_home() -> str:
+    return os.path.dirname(os.path.dirname(_nvcc()))
+
+
 def _build_driver(verbose: bool) -> None:
+    """The GPU arch layer (C, cudart) and the C host driver."""
+    inc = ["-I" + os.path.join(ROOT, "include"), "-I" + os.path.join(_cuda_home(), "include")]
+    cuda_lib = os.path.join(_cuda_home(), "lib64")
+    link_cuda = ["-L" + cuda_lib, "-Wl,-rpath," + cuda_lib, "-lcudart"]
+    arch_src = os.path.join(PKG, "host", "arch_gb300.c")
+    if _stale(ARCH_LIB, [arch_src] + _headers()):
+        cmd = ["gcc", "-O2", "-std=gnu99", "-fPIC", "-shared", *inc, arch_src, "-o", ARCH_LIB,
+               *link_cuda]
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        subprocess.run(cmd, check=True)
     src = os.path.join(PKG, "host", "flow_main.c")
-    if not os.path.exists(src):
+    if not _stale(DRIVER, [src, LIB, ARCH_LIB] + _headers()):
         return
-    if not _stale(DRIVER, [src, LIB] + _headers()):
-        return
-    cuda_lib = os.path.join(os.path.dirname(os.path.dirname(_nvcc())), "lib64")
-    cmd = ["gcc", "-O2", "-std=gnu99", "-I" + os.path.join(ROOT, "include"), src,
-           "-o", DRIVER, "-L" + PKG, "-lflow_gb300", "-Wl,-rpath,$ORIGIN",
-           "-L" + cuda_lib, "-Wl,-rpath," + cuda_lib, "-lcudart", "-lm"]
+    cmd = ["gcc", "-O2", "-std=gnu99", *inc, src, "-o", DRIVER, "-L" + PKG,
+           "-lflow_gb300", "-lflow_gb300_arch", "-Wl,-rpath,$ORIGIN", *link_cuda, "-lm"]
     if verbose:
         print(" ".join(cmd), flush=True)
     subprocess.run(cmd, check=True)

@@ -15,7 +15,7 @@ namespace {
 thread_local int t_err = GB300_OK;
 thread_local char t_msg[512] = "";
 thread_local cudaStream_t t_stream = nullptr;
-thread_local int t_mode = GB300_MODE_EXACT;
+thread_local int t_mode = GB300_MODE_FUSED;
 int g_verbose = 1;
 
 }  // namespace

@@ -182,6 +182,19 @@ int gb300_conservation(int nx, int ny, int pad, const double* rho,
                        const double* e, double* reduce_array, double* out,
                        int sync);
 
+/* Per-kernel CUDA-event timing of the fused timestep: enable, run steps,
+ * then read one (name, launches, total milliseconds) entry per kernel. */
+int gb300_profile_enable(int on);
+int gb300_profile_reset(void);
+int gb300_profile_count(void);
+int gb300_profile_entry(int i, char* name, int name_len, long long* launches,
+                        double* total_ms);
+
+/* Measured FP64 FMA issue rate of the current GPU (FMA instructions per
+ * second per GPU), the compute roofline of the FP64 timestep.  Allocates a
+ * small scratch buffer; not for use inside stream capture. */
+int gb300_measure_fp64_fma_rate(double* fma_per_s);
+
 #ifdef __cplusplus
 }
 #endif

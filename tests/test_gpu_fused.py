@@ -1,0 +1,113 @@
+"""GPU parity of the fused FP64 timestep (the default solve_hydro_2d mode)
+against the oracle: every state field per cell within 1e-12 relative (see
+tests/tolerance.py), dt within 1e-12, mass conserved to round-off."""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from tolerance import FP64_TOL, cell_rel_err
+
+pytestmark = pytest.mark.gpu
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLDEN = sorted(glob.glob(os.path.join(HERE, "golden", "*.npz")))
+STATE = ("rho", "e", "u", "v", "rho_u", "rho_v")
+
+
+@pytest.fixture(scope="module")
+def fg():
+    import flow_gb300
+    flow_gb300.lib()
+    flow_gb300.set_mode(flow_gb300.MODE_FUSED)
+    return flow_gb300
+
+
+def pair(fg, prob):
+    sim = fg.DeviceSim(prob)
+    hm = O.HostMesh(prob.gnx, prob.gny, dt=prob.dt_param)
+    st = O.HostState(hm)
+    O.fill_fields(hm, st, prob.interior(prob.rho), prob.interior(prob.e))
+    return sim, hm, st
+
+
+def compare(sim, st, tol=FP64_TOL, fields=STATE):
+    errs = {k: cell_rel_err(sim.interior(k), st.interior(k)) for k in fields}
+    bad = {k: v for k, v in errs.items() if not v <= tol}
+    assert not bad, errs
+    return errs
+
+
+def run_both(fg, prob, steps, check_every=None):
+    sim, hm, st = pair(fg, prob)
+    sim.initial_timestep()
+    O.initial_timestep(hm, st)
+    for tt in range(steps):
+        sim.step()
+        O.step(hm, st, tt)
+        assert abs(sim.mesh.dt - hm.mesh.dt) <= FP64_TOL * hm.mesh.dt, tt
+        assert abs(sim.mesh.dt_h - hm.mesh.dt_h) <= FP64_TOL * hm.mesh.dt_h, tt
+        if check_every and (tt + 1) % check_every == 0:
+            compare(sim, st)
+    return sim, hm, st
+
+
+@pytest.mark.parametrize("path", GOLDEN, ids=lambda p: os.path.basename(p))
+def test_fused_matches_reference_fixture(fg, path):
+    from flow_gb300.problems import Problem
+    z = np.load(path)
+    gny, gnx = z["rho0"].shape
+    prob = Problem(gnx, gny, dt_param=float(z["dt_param"])).fields(z["rho0"], z["e0"])
+    sim = fg.DeviceSim(prob)
+    sim.initial_timestep()
+    for _ in range(int(z["steps"])):
+        sim.step()
+    np.testing.assert_allclose(sim.mesh.dt, z["dt_hist"][-1][0], rtol=FP64_TOL)
+    hm = O.HostMesh(gnx, gny)
+    ref = O.HostState(hm)
+    for k in STATE:
+        ref.a[k][:] = z[f"out_{k}"]
+    compare(sim, ref)
+
+
+def test_fused_sod_512_100_steps(fg):
+    """Config 0: 512^2 Sod tube, 100 iterations, per-cell within 1e-12."""
+    from flow_gb300 import problems
+    sim, hm, st = run_both(fg, problems.sod(512), 100, check_every=25)
+    errs = compare(sim, st)
+    m_gpu, _ = sim.conservation()
+    m0 = 0.125 * 512 * 256 + 1.0 * 512 * 256
+    assert abs(m_gpu - m0) <= 1e-13 * m0, (m_gpu, m0)
+    print("sod512 max per-cell rel err", errs)
+
+
+def test_fused_blast_128_200_steps(fg):
+    """Sedov-type blast (config 1 at reduced size), 200 iterations."""
+    from flow_gb300 import problems
+    sim, hm, st = run_both(fg, problems.sedov(128), 200, check_every=50)
+    compare(sim, st)
+
+
+def test_fused_reference_problem_ragged(fg):
+    """The reference's own problem on a ragged mesh, odd and even steps."""
+    from flow_gb300.problems import Problem
+    prob = Problem(301, 187, dt_param=1e-3).boxes(O.flow_params_boxes())
+    sim, hm, st = run_both(fg, prob, 41)
+    compare(sim, st)
+
+
+def test_fused_and_exact_modes_agree(fg):
+    from flow_gb300 import problems
+    prob = problems.sod(200, 136)
+    sims = []
+    for mode in (fg.MODE_EXACT, fg.MODE_FUSED):
+        fg.set_mode(mode)
+        s = fg.DeviceSim(prob)
+        s.initial_timestep()
+        s.run(30)
+        sims.append(s)
+    fg.set_mode(fg.MODE_FUSED)
+    for k in STATE:
+        assert cell_rel_err(sims[1].interior(k), sims[0].interior(k)) <= FP64_TOL, k
