@@ -61,6 +61,9 @@ def parse_args():
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--size", type=int, default=N_CELLS_SIDE)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--fp64-only", action="store_true", help="skip the mixed/batched forms")
+    p.add_argument("--batch-steps", type=int, default=20,
+                   help="timed steps of each batched form (a sample of its 200/1000)")
     return p.parse_args()
 
 
@@ -200,6 +203,99 @@ def run_reference(args):
 # ---------------------------------------------------------------------------
 # GPU side.
 
+B_ALG_MIXED = 48  # rho, e (FP64) and rho_u, rho_v (FP32), each read + written
+
+
+def field_errors(fg, got, want, names=("rho", "e")):
+    """L1 (sum|d| / sum|want|) and L-infinity (max|d| / max|want|) per field."""
+    out = {}
+    for k in names:
+        a = got.interior(k)
+        b = want.interior(k)
+        out[k] = {"l1": float(abs(a - b).sum() / abs(b).sum()),
+                  "linf": float(abs(a - b).max() / abs(b).max())}
+    return out
+
+
+def batch_problems(problems, kind: str):
+    """Config 3 (kind "two_region"): 256 two-region instances with sides drawn
+    from {128, 192, ..., 1024}; config 4 (kind "smooth"): 64 instances of
+    2048^2 smooth random fields.  Seeded."""
+    import numpy as np
+    if kind == "two_region":
+        rng = np.random.default_rng(20261203)
+        sides = rng.choice(np.arange(128, 1025, 64), size=256)
+        return [problems.two_region(int(n), rng) for n in sides]
+    rng = np.random.default_rng(20261204)
+    return [problems.smooth_random(2048, rng) for _ in range(64)]
+
+
+def run_batched_form(fg, problems, torch, device, kind, precision, steps, warmup):
+    """Times one batched ensemble (autotuned, graph-replayed) and measures its
+    error on two sampled instances against the single-problem FP64 step."""
+    import numpy as np
+    probs = batch_problems(problems, kind)
+    b = fg.Batch(probs, precision=precision, device=device)
+    tune = b.autotune(steps=2)
+    b.step(warmup)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    b.step(steps, use_graph=True)
+    e1.record()
+    torch.cuda.synchronize()
+    b.status()
+    ms = e0.elapsed_time(e1)
+    cells = b.cells
+    value = cells * steps / (ms * 1e-3)
+    total_steps = b.steps_done
+    samples = [0, len(probs) // 2]
+    errs = {}
+    for i in samples:
+        rho, e, dt, _ = b.state(i)
+        ref = fg.DeviceSim(probs[i], device)
+        ref.initial_timestep()
+        ref.run(total_steps)
+        rr, er = ref.interior("rho"), ref.interior("e")
+        errs[f"instance_{i}_{probs[i].gnx}x{probs[i].gny}"] = {
+            "rho_l1": float(np.abs(rho - rr).sum() / np.abs(rr).sum()),
+            "e_l1": float(np.abs(e - er).sum() / np.abs(er).sum()),
+            "rho_linf": float(np.abs(rho - rr).max() / np.abs(rr).max()),
+            "max_abs_diff": float(max(np.abs(rho - rr).max(), np.abs(e - er).max()))}
+        del ref
+    del b
+    torch.cuda.empty_cache()
+    b_alg = B_ALG_FP64 if precision == 0 else B_ALG_MIXED
+    return {"workload": f"batch_{kind}_{'fp64' if precision == 0 else 'mixed'}",
+            "instances": len(probs), "cells": cells, "value": value, "unit": UNIT,
+            "ms_per_step": ms / steps, "steps_timed": steps, "steps_total": total_steps,
+            "graph": True, "tuning": tune,
+            "hbm_fraction_of_step": value * b_alg / (measured_peaks()[0] * 1e9),
+            "errors_vs_fp64_single_problem": errs}
+
+
+def run_mixed_form(fg, problems, torch, device, n, steps, warmup, ref_state=None, workload="sedov"):
+    """Times the mixed form on the same workload; returns its result dict and
+    the final simulation object."""
+    prob = problems.sedov(n) if workload == "sedov" else problems.sod(n)
+    sim = fg.MixedSim(prob, device)
+    for _ in range(warmup):
+        sim.step()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        sim.step()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    value = n * n * steps / (ms * 1e-3)
+    return {"workload": f"{workload}_{n}_mixed", "value": value, "unit": UNIT,
+            "ms_per_step": ms / steps, "steps": steps, "warmup": warmup,
+            "hbm_fraction_of_step_48B": value * B_ALG_MIXED / (measured_peaks()[0] * 1e9)}, sim
+
 def run_gpu(args):
     rank, world, local = dist_env()
     import torch
@@ -299,7 +395,29 @@ def run_gpu(args):
     h2d = sum(host_in[f].numel() * 8 for f in fields)
     d2h = sum(host_out[f].numel() * 8 for f in fields)
     e2e_value = world * n * n * args.steps / e2e_s
-    del sim2, host_in, host_out
+    del host_in, host_out
+
+    # ---- the mixed-precision form on the same workload ----
+    forms = {}
+    if not args.fp64_only:
+        mixed, msim = run_mixed_form(fg, problems, torch, device, n, args.steps, args.warmup)
+        # Error against the FP64 path after the same number of steps from the
+        # same initial state (the FP64 path itself matches the CPU oracle to
+        # ~1e-13 per cell).
+        ref = fg.DeviceSim(problems.sedov(n), device)
+        ref.initial_timestep()
+        ref.run(args.steps + args.warmup)
+        mixed["errors_vs_fp64"] = field_errors(fg, msim, ref)
+        mixed["mass_drift"] = abs(msim.conservation()[0] - ref.conservation()[0]) / ref.conservation()[0]
+        mixed["speedup_vs_fp64"] = mixed["value"] / (value / world)
+        forms["mixed"] = mixed
+        del msim, ref, sim, sim2
+        torch.cuda.empty_cache()
+        bsteps = min(args.steps, args.batch_steps)
+        forms["batched_fp64"] = run_batched_form(fg, problems, torch, device, "two_region", 0,
+                                                 bsteps, args.warmup)
+        forms["batched_mixed"] = run_batched_form(fg, problems, torch, device, "smooth", 1,
+                                                  bsteps, args.warmup)
 
     if rank != 0:
         return
@@ -347,6 +465,7 @@ def run_gpu(args):
                       "note": "FP64 issue rate measured on this GPU; the FP64 timestep is bound here"},
         "kernels": [{"name": k, "launches": c, "ms": t, "share": t / sum(x[2] for x in kernels)}
                     for k, c, t in kernels],
+        "forms": forms,
         "cpu_baseline": cpu,
         "clocks": clk.summary(),
         "gpu_launches": 15 * args.steps,

@@ -108,6 +108,8 @@ def _declare(L: ctypes.CDLL) -> None:
         "gb300_profile_count": [],
         "gb300_profile_entry": [I, ctypes.c_char_p, I, ctypes.POINTER(ctypes.c_longlong), P],
         "gb300_measure_fp64_fma_rate": [P],
+        "gb300_mixed_prepare": [M, P, P, V, ctypes.c_size_t, P, I],
+        "gb300_mixed_solve": [M, I, P, P, V, V, V, ctypes.c_size_t, P],
     }
     for name, args in status.items():
         fn = getattr(L, name)
@@ -115,6 +117,25 @@ def _declare(L: ctypes.CDLL) -> None:
     L.gb300_last_error_message.argtypes, L.gb300_last_error_message.restype = [], ctypes.c_char_p
     L.gb300_clear_error.argtypes, L.gb300_clear_error.restype = [], None
     L.gb300_get_stream.argtypes, L.gb300_get_stream.restype = [], ctypes.c_void_p
+    L.gb300_mixed_workspace_bytes.argtypes = [I, I]
+    L.gb300_mixed_workspace_bytes.restype = ctypes.c_size_t
+    IP = ctypes.POINTER(ctypes.c_int)
+    batch = {
+        "gb300_batch_create": [I, IP, IP, P, P, I, ctypes.POINTER(V)],
+        "gb300_batch_bind": [V, V, ctypes.c_size_t],
+        "gb300_batch_set_state": [V, I, P, P, D],
+        "gb300_batch_set_tuning": [V, I, I, I],
+        "gb300_batch_get_tuning": [V, IP, IP, IP, IP],
+        "gb300_batch_step": [V, I, I],
+        "gb300_batch_status": [V],
+        "gb300_batch_get_state": [V, I, P, P, P, P],
+    }
+    for name, args in batch.items():
+        fn = getattr(L, name)
+        fn.argtypes, fn.restype = args, ctypes.c_int
+    L.gb300_batch_pool_bytes.argtypes, L.gb300_batch_pool_bytes.restype = [V], ctypes.c_size_t
+    L.gb300_batch_cells.argtypes, L.gb300_batch_cells.restype = [V], ctypes.c_longlong
+    L.gb300_batch_destroy.argtypes, L.gb300_batch_destroy.restype = [V], None
     L.gb300_set_verbose(0)
 
 
@@ -144,4 +165,10 @@ def dptr(t) -> "ctypes._Pointer":
     return ctypes.cast(ctypes.c_void_p(t.data_ptr()), _dp)
 
 
-from .sim import DeviceSim  # noqa: E402,F401
+def vptr(t) -> ctypes.c_void_p:
+    """void* of a CUDA torch tensor."""
+    return ctypes.c_void_p(t.data_ptr())
+
+
+from .sim import DeviceSim, MixedSim  # noqa: E402,F401
+from .batch import Batch  # noqa: E402,F401

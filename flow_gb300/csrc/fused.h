@@ -22,4 +22,14 @@ int fused_solve(Mesh* mesh, int tt, double* P, double* rho, double* rho_old,
                 double* uF_x, double* uF_y, double* vF_x, double* vF_y,
                 double* reduce_array);
 
+// Mixed form: FP32 bulk arithmetic, FP64 density/energy and their
+// conservative updates.  The workspace holds every intermediate array.
+size_t mixed_workspace_bytes(int nx, int ny);
+// Byte offset of a cell-sized FP64 block of the workspace that is zero after
+// mixed_prepare (the first-sweep density, written only during a step).
+size_t mixed_zero_block_offset(int nx, int ny);
+int mixed_prepare(Mesh* mesh, double* rho, double* e, void* work, size_t bytes);
+int mixed_solve(Mesh* mesh, int tt, double* rho, double* e, float* rho_u,
+                float* rho_v, void* work, size_t bytes, double* reduce_array);
+
 }  // namespace flow

@@ -1,0 +1,897 @@
+// fused_tiles.cuh -- the tile-level device code of the fused timestep, shared
+// by the single-problem kernels (fused.cu) and the persistent batched kernel
+// (batched.cu).  Each tile_* function processes one CTA-sized tile (bx, by)
+// of one phase of the timestep for one problem described by StepArgs; a
+// thread may return early, but no tile function has a barrier after such a
+// return, so consecutive tiles can run back to back in one CTA.
+//
+// Two precision forms share the code (precision.cuh):
+//   R = double  the FP64 form behind solve_hydro_2d (GB300_MODE_FUSED);
+//   R = float   the mixed form: FP32 for the equation of state,
+//               accelerations, viscosity, shock heating, the CFL candidates
+//               and every flux; FP64 for the stored density and energy, their
+//               conservative update in the mass sweeps, the energy increment
+//               of shock heating and the dt minimum.
+//
+// Same scheme as the reference timestep (omp3/flow.c:10-52), reorganised for
+// GB300, where the FP64 issue rate (not HBM bandwidth) bounds the FP64 form:
+//   * no flux or velocity is computed twice: each is produced once per point
+//     and stored; only the 2-flop pressure is recomputed for neighbour faces;
+//   * ghost cells are written by the tile that produces the interior value
+//     (mirror), replacing the 19 ghost-fill launches per step;
+//   * comparisons, selections and minmod run on the integer pipes, divisions
+//     by the mesh spacing become multiplications by per-column / per-row
+//     reciprocals (exact on power-of-two meshes), data divisions start from a
+//     MUFU reciprocal with an FMA correction;
+//   * the momentum/velocity chain and the conservative updates keep the
+//     reference's evaluation order in the FP64 form, with correctly rounded
+//     quotients (precision.cuh msub/madd/qdiv/dsub);
+//   * the CFL minimum and dt/dt_h stay on the device (dt_slot).
+// Every tile is a column strip: 128 threads own 128 consecutive columns and
+// march a.rows rows (at most kMaxRows), carrying the values of previous rows
+// in registers.
+#pragma once
+
+#include <cstddef>
+
+#include "common.cuh"
+#include "precision.cuh"
+
+namespace flow {
+namespace tiles {
+
+
+constexpr int kCols = 128;
+constexpr int kMaxRows = 32;     // tallest tile (shared-memory row tables)
+constexpr int kDefaultRows = 16;
+constexpr double kG1 = kGam - 1.0;
+
+template <typename R>
+struct StepArgs {
+  int nx, ny, pad;
+  const double* edgedx;
+  const double* edgedy;
+  const double* celldx;
+  const double* celldy;
+  double* rho;      // FP64 cell state
+  double* e;
+  R* rho_r;         // the same fields in bulk precision (aliases for FP64)
+  R* e_r;
+  double* P;        // FP64 form only: the reference's P and rho_old outputs
+  double* rho_old;
+  R* u;
+  R* v;
+  R* rho_u;
+  R* rho_v;
+  R* Qxx;
+  R* Qyy;
+  R* F_x;
+  R* F_y;
+  R* uF_x;
+  R* uF_y;
+  R* vF_x;
+  R* vF_y;
+  double* ra;                  // caller scratch (reduce_array)
+  unsigned long long* min_slot;  // running CFL minimum (FP64 bit pattern)
+  double* dt_slot;             // [0] dt, [1] dt_h for the advection phase
+  double dt, dt_h, max_dt;     // Lagrangian-phase pair (host values), max_dt
+  int first_step;
+  int rows;                    // tile height, 1 .. kMaxRows
+};
+
+// Writes the value of interior point (ii, jj) of a w x h array into each of
+// its ghost mirror images (pad layers per side): column images negated when
+// flip_x, row images when flip_y, corner images by both.  This reproduces the
+// reflective fill of every ghost point whose mirror source is (ii, jj).
+template <typename T>
+__device__ __forceinline__ void mirror(T* a, int w, int h, int pad, int ii,
+                                       int jj, T val, bool flip_x, bool flip_y) {
+  int mc[2], mr[2];
+  int nc = 0, nr = 0;
+  if (jj < 2 * pad) mc[nc++] = 2 * pad - 1 - jj;
+  if (jj >= w - 2 * pad) mc[nc++] = 2 * (w - pad) - 1 - jj;
+  if (ii < 2 * pad) mr[nr++] = 2 * pad - 1 - ii;
+  if (ii >= h - 2 * pad) mr[nr++] = 2 * (h - pad) - 1 - ii;
+  if (nc == 0 && nr == 0) return;
+  const T vx = flip_x ? -val : val;
+  const T vy = flip_y ? -val : val;
+  const T vxy = flip_x ? -vy : vy;
+  for (int k = 0; k < nc; ++k) a[(size_t)ii * w + mc[k]] = vx;
+  for (int r = 0; r < nr; ++r) {
+    a[(size_t)mr[r] * w + jj] = vy;
+    for (int k = 0; k < nc; ++k) a[(size_t)mr[r] * w + mc[k]] = vxy;
+  }
+}
+
+// Stores an FP64 cell value, and its bulk-precision shadow in the mixed form,
+// with ghost mirrors.
+template <typename R>
+__device__ __forceinline__ void store_cell(double* a64, R* ar, int nx, int ny,
+                                           int pad, int ii, int jj, double val) {
+  const size_t c = cidx(nx, ii, jj);
+  a64[c] = val;
+  mirror(a64, nx, ny, pad, ii, jj, val, false, false);
+  if (Prec<R>::kMixed) {
+    const R vr = Prec<R>::from_d(val);
+    ar[c] = vr;
+    mirror(ar, nx, ny, pad, ii, jj, vr, false, false);
+  }
+}
+
+// ===========================================================================
+// Lagrangian phase.
+
+// Pressure (EOS on the fly) -> face momenta -> velocities.  Covers every cell
+// (the FP64 form writes P and rho_old for ghosts too, as equation_of_state and
+// the rho_old copy of the reference do) and every interior x/y face.  The
+// reciprocal of each face density is kept in F_x/F_y (free until the
+// advection phase) for the viscous update.  omp3/flow.c:55-70, 110-158.
+template <typename R>
+__device__ __forceinline__ void tile_lag_pressure(const StepArgs<R>& a, int bx, int by) {
+  using Pr = Prec<R>;
+  __shared__ R sP[kCols + 1], sR[kCols + 1];
+  __shared__ R s_ey[kMaxRows], s_iey[kMaxRows], s_wy0[kMaxRows], s_wy1[kMaxRows];
+  const int nx = a.nx, ny = a.ny, pad = a.pad;
+  const int t = threadIdx.x;
+  const int jj = bx * kCols + t;
+  const int i0 = by * a.rows;
+  const R g1 = R(kG1);
+  if (t < a.rows) {
+    const int ii = i0 + t;
+    if (ii >= 1 && ii < ny) {
+      const double ey = a.edgedy[ii];
+      s_ey[t] = R(ey);
+      s_iey[t] = R(1.0 / ey);
+      s_wy0[t] = R(a.celldy[ii] / (2.0 * ey));
+      s_wy1[t] = R(a.celldy[ii - 1] / (2.0 * ey));
+    }
+  }
+  R exr = R(0), iex = R(0), wx0 = R(0), wx1 = R(0);
+  if (jj >= 1 && jj < nx) {
+    const double ex = a.edgedx[jj];
+    exr = R(ex);
+    iex = R(1.0 / ex);
+    wx0 = R(a.celldx[jj] / (2.0 * ex));
+    wx1 = R(a.celldx[jj - 1] / (2.0 * ex));
+  }
+  const R dt = R(a.dt);
+  R P_dn = R(0), r_dn = R(0);  // cell (ii-1, jj)
+  if (i0 >= 1 && jj < nx) {
+    const size_t c = cidx(nx, i0 - 1, jj);
+    r_dn = a.rho_r[c];
+    P_dn = g1 * r_dn * a.e_r[c];
+  }
+  __syncthreads();
+  for (int k = 0; k < a.rows; ++k) {
+    const int ii = i0 + k;
+    if (ii >= ny) break;
+    R Pc = R(0), rc = R(0);
+    if (jj < nx) {
+      const size_t c = cidx(nx, ii, jj);
+      rc = a.rho_r[c];
+      Pc = g1 * rc * a.e_r[c];
+      if (!Pr::kMixed) {
+        a.P[c] = double(Pc);
+        a.rho_old[c] = double(rc);
+      }
+    }
+    sP[t + 1] = Pc;
+    sR[t + 1] = rc;
+    if (t == 0) {
+      R Pl = R(0), rl = R(0);
+      if (jj >= 1 && jj - 1 < nx) {
+        const size_t c = cidx(nx, ii, jj - 1);
+        rl = a.rho_r[c];
+        Pl = g1 * rl * a.e_r[c];
+      }
+      sP[0] = Pl;
+      sR[0] = rl;
+    }
+    __syncthreads();
+    if (ii >= pad && ii < ny - pad && jj >= pad && jj < nx + 1 - pad) {
+      const size_t f = fidx(nx, ii, jj);
+      const R mom = Pr::dsub(a.rho_u[f], dt * (Pc - sP[t]), exr, iex);
+      const R rbar = fma(rc, wx0, sR[t] * wx1);
+      const bool z = Pr::is_zero(rbar);
+      const R inv = z ? R(0) : Pr::rcp(rbar);
+      const R vel = z ? R(0) : Pr::qdiv(mom, rbar, inv);
+      a.rho_u[f] = mom;
+      a.u[f] = vel;
+      a.F_x[f] = inv;
+      a.uF_x[f] = rbar;
+      mirror(a.u, nx + 1, ny, pad, ii, jj, vel, true, false);
+    }
+    if (ii >= pad && ii < ny + 1 - pad && jj >= pad && jj < nx - pad) {
+      const size_t c = cidx(nx, ii, jj);
+      const R mom = Pr::dsub(a.rho_v[c], dt * (Pc - P_dn), s_ey[k], s_iey[k]);
+      const R rbar = fma(rc, s_wy0[k], r_dn * s_wy1[k]);
+      const bool z = Pr::is_zero(rbar);
+      const R inv = z ? R(0) : Pr::rcp(rbar);
+      const R vel = z ? R(0) : Pr::qdiv(mom, rbar, inv);
+      a.rho_v[c] = mom;
+      a.v[c] = vel;
+      a.F_y[c] = inv;
+      a.vF_y[c] = rbar;
+      mirror(a.v, nx, ny + 1, pad, ii, jj, vel, false, true);
+    }
+    P_dn = Pc;
+    r_dn = rc;
+    __syncthreads();
+  }
+}
+
+// Artificial viscous stresses on interior cells, omp3/flow.c:173-207.
+template <typename R>
+__device__ __forceinline__ R visc_stress(R crho, R lo, R mid, R hi, R hi2) {
+  using Pr = Prec<R>;
+  const R m0 = Pr::min0(mid - lo);
+  const R m1 = Pr::min0(hi - mid);
+  const R m2 = Pr::min0(hi2 - hi);
+  return crho * m1 * (R(0.5) * (Pr::abs(m2 - m1) + Pr::abs(m1 - m0)));
+}
+
+template <typename R>
+__device__ __forceinline__ void tile_lag_viscosity(const StepArgs<R>& a, int bx, int by) {
+  const int nx = a.nx, ny = a.ny, pad = a.pad;
+  const int jj = pad + bx * kCols + threadIdx.x;
+  const int i0 = pad + by * a.rows;
+  if (jj >= nx - pad) return;
+  const int i1 = min(i0 + a.rows, ny - pad);
+  R vm = a.v[cidx(nx, i0 - 1, jj)];
+  R v0 = a.v[cidx(nx, i0, jj)];
+  R vp = a.v[cidx(nx, i0 + 1, jj)];
+  for (int ii = i0; ii < i1; ++ii) {
+    const R vp2 = a.v[cidx(nx, ii + 2, jj)];
+    const size_t f = fidx(nx, ii, jj);
+    const size_t c = cidx(nx, ii, jj);
+    const R crho = R(-kCQ) * a.rho_r[c];
+    const R qx = visc_stress(crho, a.u[f - 1], a.u[f], a.u[f + 1], a.u[f + 2]);
+    const R qy = visc_stress(crho, vm, v0, vp, vp2);
+    a.Qxx[c] = qx;
+    a.Qyy[c] = qy;
+    mirror(a.Qxx, nx, ny, pad, ii, jj, qx, false, false);
+    mirror(a.Qyy, nx, ny, pad, ii, jj, qy, false, false);
+    vm = v0;
+    v0 = vp;
+    vp = vp2;
+  }
+}
+
+// Viscous acceleration of the face momenta and velocities,
+// omp3/flow.c:212-244.  The face-density reciprocals come from F_x/F_y.
+template <typename R>
+__device__ __forceinline__ void tile_lag_viscous_accel(const StepArgs<R>& a, int bx, int by) {
+  using Pr = Prec<R>;
+  __shared__ R s_cy[kMaxRows], s_icy[kMaxRows];
+  const int nx = a.nx, ny = a.ny, pad = a.pad;
+  const int jj = pad + bx * kCols + threadIdx.x;
+  const int i0 = pad + by * a.rows;
+  if (threadIdx.x < a.rows) {
+    const int ii = i0 + threadIdx.x;
+    if (ii < ny) {
+      s_cy[threadIdx.x] = R(a.celldy[ii]);
+      s_icy[threadIdx.x] = R(1.0 / a.celldy[ii]);
+    }
+  }
+  __syncthreads();
+  if (jj >= nx + 1 - pad) return;
+  const R cx = R(a.celldx[jj]);
+  const R icx = R(1.0 / a.celldx[jj]);
+  const R dt = R(a.dt);
+  const int i1 = min(i0 + a.rows, ny + 1 - pad);
+  R qy_dn = (jj < nx - pad) ? a.Qyy[cidx(nx, i0 - 1, jj)] : R(0);
+  for (int ii = i0; ii < i1; ++ii) {
+    const int k = ii - i0;
+    if (ii < ny - pad) {
+      const size_t f = fidx(nx, ii, jj);
+      const size_t c = cidx(nx, ii, jj);
+      const R mom = Pr::dsub(a.rho_u[f], dt * (a.Qxx[c] - a.Qxx[c - 1]), cx, icx);
+      const R inv = a.F_x[f];
+      const R vel = Pr::is_zero(inv) ? R(0) : Pr::qdiv(mom, a.uF_x[f], inv);
+      a.rho_u[f] = mom;
+      a.u[f] = vel;
+      mirror(a.u, nx + 1, ny, pad, ii, jj, vel, true, false);
+    }
+    if (jj < nx - pad) {
+      const size_t c = cidx(nx, ii, jj);
+      const R qy = a.Qyy[c];
+      const R mom = Pr::dsub(a.rho_v[c], dt * (qy - qy_dn), s_cy[k], s_icy[k]);
+      const R inv = a.F_y[c];
+      const R vel = Pr::is_zero(inv) ? R(0) : Pr::qdiv(mom, a.vF_y[c], inv);
+      a.rho_v[c] = mom;
+      a.v[c] = vel;
+      mirror(a.v, nx, ny + 1, pad, ii, jj, vel, false, true);
+      qy_dn = qy;
+    }
+  }
+}
+
+__device__ __forceinline__ unsigned long long warp_min_u64(unsigned long long x) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long y = __shfl_xor_sync(0xffffffffu, x, o);
+    x = (y < x) ? y : x;
+  }
+  return x;
+}
+
+// Shock heating and work (omp3/flow.c:248-290) fused with the CFL minimum of
+// set_timestep (omp3/flow.c:73-106) on the updated energy.  One atomicMin per
+// block on the FP64 bit pattern of its smallest candidate; the last block to
+// finish applies the leapfrog dt/dt_h rule (finish_dt).  In the mixed form
+// the FP32 energy change is added to the FP64 energy.
+template <typename R>
+__device__ __forceinline__ void tile_lag_energy_dt(const StepArgs<R>& a, int bx, int by) {
+  using Pr = Prec<R>;
+  __shared__ R s_icy[kMaxRows], s_cy[kMaxRows];
+  __shared__ unsigned long long s_warp[kCols / 32];
+  const int nx = a.nx, ny = a.ny, pad = a.pad;
+  const int jj = pad + bx * kCols + threadIdx.x;
+  const int i0 = pad + by * a.rows;
+  if (threadIdx.x < a.rows) {
+    const int ii = i0 + threadIdx.x;
+    if (ii < ny) {
+      s_cy[threadIdx.x] = R(a.celldy[ii]);
+      s_icy[threadIdx.x] = R(1.0 / a.celldy[ii]);
+    }
+  }
+  __syncthreads();
+  unsigned long long best = ~0ull;
+  if (jj < nx - pad) {
+    const R cx = R(a.celldx[jj]);
+    const R icx = R(1.0 / a.celldx[jj]);
+    const R dt_h = R(a.dt_h);
+    const int i1 = min(i0 + a.rows, ny - pad);
+    R v0 = a.v[cidx(nx, i0, jj)];
+    for (int ii = i0; ii < i1; ++ii) {
+      const int k = ii - i0;
+      const size_t c = cidx(nx, ii, jj);
+      const size_t f = fidx(nx, ii, jj);
+      const R v1 = a.v[c + nx];
+      const R r = a.rho_r[c];
+      const R er = a.e_r[c];
+      const R p = Pr::kMixed ? R(kG1) * r * er : R(a.P[c]);
+      const R qx = a.Qxx[c], qy = a.Qyy[c];
+      const bool rz = Pr::is_zero(r);
+      const R inv_r = rz ? R(0) : Pr::rcp(r);
+      const R dudx = (a.u[f + 1] - a.u[f]) * icx;
+      const R dvdy = (v1 - v0) * s_icy[k];
+      const R div_dt = (dudx + dvdy) * dt_h;
+      // e_q = e - dt_h (Qxx dudx + Qyy dvdy) / rho, kept as an increment.
+      const R dq = -(dt_h * fma(qx, dudx, qy * dvdy)) * inv_r;
+      const R e_q = er + dq;
+      const R rho_c = r * Pr::rcp(R(1) + div_dt);
+      const R e_c = fma(-(p * div_dt), inv_r, e_q);
+      const R work = (R(0.5) * div_dt) * fma(R(kG1) * e_c, rho_c, p) * inv_r;
+      double e_new;
+      if (Pr::kMixed) {
+        e_new = rz ? 0.0 : a.e[c] + Pr::to_d(dq - work);
+      } else {
+        e_new = rz ? 0.0 : double(e_q - work);
+      }
+      store_cell(a.e, a.e_r, nx, ny, pad, ii, jj, e_new);
+      // CFL: celldx / sqrt(c_s^2 + 2 Q / rho) with c_s^2 = gamma (gamma-1) e.
+      const R e_nr = Pr::from_d(e_new);
+      const R s2 = R(kGam * (kGam - 1.0)) * e_nr;
+      const R two_inv_r = inv_r + inv_r;
+      const R dtx = cx * Pr::rsqrt(fma(qx, two_inv_r, s2));
+      const R dty = s_cy[k] * Pr::rsqrt(fma(qy, two_inv_r, s2));
+      const unsigned long long mx = (unsigned long long)dbits(Pr::to_d(dtx));
+      const unsigned long long my = (unsigned long long)dbits(Pr::to_d(dty));
+      const unsigned long long m = (mx < my) ? mx : my;
+      best = (m < best) ? m : best;
+      v0 = v1;
+    }
+  }
+  best = warp_min_u64(best);
+  if ((threadIdx.x & 31) == 0) s_warp[threadIdx.x >> 5] = best;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long b = s_warp[0];
+    for (int w = 1; w < kCols / 32; ++w) b = (s_warp[w] < b) ? s_warp[w] : b;
+    atomicMin(a.min_slot, b);
+  }
+}
+
+// The leapfrog dt/dt_h rule of omp3/flow.c:103-105 applied to the finished
+// CFL minimum, in FP64 without contraction; resets the minimum slot.
+template <typename R>
+__device__ __forceinline__ void finish_dt(const StepArgs<R>& a) {
+  const unsigned long long g = atomicExch(a.min_slot, ~0ull);
+  const double cfl = d_min_pos(a.max_dt, dfrom((long long)g));
+  const double limited = dmin(cfl, __dmul_rn(FLOW_C_M, a.dt_h));
+  const double dt = __dmul_rn(0.5, __dadd_rn(__dmul_rn(kCT, limited), a.dt_h));
+  a.dt_slot[0] = dt;
+  a.dt_slot[1] = a.first_step ? dt : __dmul_rn(kCT, limited);
+}
+
+// ===========================================================================
+// Advection of mass and energy (omp3/flow.c:293-554).
+
+// Second-order upwind interpolation with the MC-limited slope, for the branch
+// already chosen by the wind sign: pos selects the left reconstruction
+// base + 0.5*m*(h - w*dt_h), otherwise base - 0.5*m*(h + w*dt_h).
+template <typename R>
+__device__ __forceinline__ R mc_face(bool pos, R da, R db, R dc, R half_inv,
+                                     R two_inv, R base, R h, R wdt) {
+  using Pr = Prec<R>;
+  const R mm = Pr::minmod(Pr::minmod(half_inv * da, two_inv * db), two_inv * dc);
+  const R w = h + (pos ? -wdt : wdt);
+  const R hm = pos ? R(0.5) * mm : R(-0.5) * mm;
+  return Pr::madd(hm, w, base);
+}
+
+// Mass and energy flux through one face.  The four cells straddle the face
+// (m2, m1 | p0, p1), vm/v0/vp are the face velocities around it, h_m/h_p the
+// cell widths on each side, area the face length, inv_h the reciprocal of the
+// face spacing and icd the reciprocal of the downstream cell width.  kSideV0:
+// take the Van Leer smoothness side from v0 (the y sweep, omp3/flow.c:477)
+// instead of the half-step velocity.
+template <typename R, bool kSideV0>
+__device__ __forceinline__ void mass_energy_flux(R vm, R v0, R vp, R rm2,
+                                                 R rm1, R r0, R rp1, R em2,
+                                                 R em1, R e0, R ep1, R inv_h,
+                                                 R h_m, R h_p, R icd, R area,
+                                                 R dt, R dt_h, R* F_out,
+                                                 R* eF_out) {
+  using Pr = Prec<R>;
+  const R half_inv = R(0.5) * inv_h, two_inv = R(2) * inv_h;
+  const R mm = Pr::minmod(half_inv * (vp - vm),
+                          Pr::minmod(two_inv * (v0 - vm), two_inv * (vp - v0)));
+  const R w_tc = Pr::msub(v0, R(0.5) * v0 * dt, mm);
+  const R jump = r0 - rm1;
+  R lim = R(0);
+  if (!Pr::is_zero(jump)) {
+    const bool up = kSideV0 ? Pr::ge0(v0) : Pr::ge0(w_tc);
+    const R num = up ? (rm1 - rm2) : (rp1 - r0);
+    // Van Leer: (s+|s|)/(1+|s|) with s = num/jump, i.e. 2 num/(jump+num)
+    // when num and jump share a sign, else 0.
+    if (Pr::same_sign_nz(num, jump)) {
+      lim = (num + num) * Pr::rcp(jump + num);
+    }
+  }
+  const R rho_up = Pr::ge0(w_tc) ? rm1 : r0;
+  const R wdt = w_tc * dt_h;
+  const R flux = Pr::madd(w_tc, rho_up,
+                          (R(0.5) * Pr::abs(w_tc)) * (R(1) - Pr::abs(wdt * icd)) * lim * jump);
+  const bool pos = Pr::gt0(w_tc);
+  const R e_face = mc_face(pos, pos ? e0 - em2 : ep1 - em1, pos ? em1 - em2 : e0 - em1,
+                           pos ? e0 - em1 : ep1 - e0, half_inv, two_inv,
+                           pos ? em1 : e0, pos ? h_m : h_p, wdt);
+  *F_out = flux;
+  *eF_out = area * e_face * flux;
+}
+
+// Conservative FP64 update of one cell from its two face fluxes (given in
+// bulk precision, converted exactly): vol = celldx*celldy and ivol its
+// reciprocal, a0/a1 the face lengths.  den is rho_old in the first sweep of a step and the new
+// density in the second (omp3/flow.c:416-432).  The FP64 form keeps the
+// reference's evaluation order; the mixed form contracts into FMAs.
+template <typename R, bool kFirst>
+__device__ __forceinline__ void mass_energy_update(double r_in, double e_in,
+                                                   double r_old, double dt_h,
+                                                   double vol, double ivol, double a0,
+                                                   double a1, R F0, R F1, R eF0,
+                                                   R eF1, double* r_out,
+                                                   double* e_out) {
+  using Pr = Prec<R>;
+  const double f0 = Pr::to_d(F0), f1 = Pr::to_d(F1);
+  const double de = Pr::to_d(eF1) - Pr::to_d(eF0);
+  double r_new, rho_e;
+  if (Pr::kMixed) {
+    const double coef = dt_h * ivol;
+    r_new = fma(-coef, fma(a1, f1, -(a0 * f0)), r_in);
+    rho_e = fma(-coef, de, r_old * e_in);
+  } else {
+    const double net = __dadd_rn(__dmul_rn(a1, f1), -__dmul_rn(a0, f0));
+    r_new = Prec<double>::dsub(r_in, __dmul_rn(dt_h, net), vol, ivol);
+    rho_e = Prec<double>::dsub(__dmul_rn(r_old, e_in), __dmul_rn(dt_h, de), vol, ivol);
+  }
+  const double den = kFirst ? r_old : r_new;
+  *r_out = r_new;
+  if (d_is_zero(den)) {
+    *e_out = 0.0;
+  } else if (Pr::kMixed) {
+    // Quotient from the FP32 reciprocal of den and one FP64 correction.
+    const double r0 = Pr::to_d(Pr::rcp(Pr::from_d(den)));
+    const double q = rho_e * r0;
+    *e_out = fma(r0, fma(-den, q, rho_e), q);
+  } else {
+    *e_out = Prec<double>::qdiv(rho_e, den, d_rcp(den));
+  }
+}
+
+template <typename R>
+struct SweepArgs {
+  const double* r_in;  // FP64 density and energy entering the sweep
+  const double* e_in;
+  const R* r_in_r;     // the same in bulk precision (aliases for FP64)
+  const R* e_in_r;
+  double* r_out;
+  double* e_out;
+  R* r_out_r;
+  R* e_out_r;
+};
+
+// x sweep: CTAs own 127 cells and compute the 128 faces around them (the last
+// face is shared with the next CTA and written only by its owner).  In the
+// second sweep of a step the old density of a cell is read from rho just
+// before the same thread overwrites that cell.
+template <typename R, bool kFirst>
+__device__ __forceinline__ void tile_mass_sweep_x(const StepArgs<R>& a,
+                                                        const SweepArgs<R>& s, int bx, int by) {
+  __shared__ R sF[kCols], seF[kCols];
+  __shared__ double s_coef[kMaxRows], s_cyd[kMaxRows], s_ey0[kMaxRows], s_ey1[kMaxRows];
+  const int nx = a.nx, ny = a.ny, pad = a.pad;
+  const int t = threadIdx.x;
+  const int jj = pad + bx * (kCols - 1) + t;  // face (and cell) column
+  const int i0 = pad + by * a.rows;
+  const double dt = a.dt_slot[0], dt_h = a.dt_slot[1];
+  if (t < a.rows) {
+    const int ii = i0 + t;
+    if (ii < ny - pad) {
+      s_coef[t] = 1.0 / a.celldy[ii];
+      s_cyd[t] = a.celldy[ii];
+      s_ey0[t] = a.edgedy[ii];
+      s_ey1[t] = a.edgedy[ii + 1];
+    }
+  }
+  const bool face_ok = jj < nx + 1 - pad;
+  const bool cell_ok = (t < kCols - 1) && (jj < nx - pad);
+  const bool face_owner = face_ok && (t < kCols - 1);
+  R iex = R(0), cxm = R(0), cx0 = R(0), icx_r = R(0);
+  double icx = 0.0;
+  if (face_ok) {
+    iex = R(1.0 / a.edgedx[jj]);
+    cxm = R(a.celldx[jj - 1]);
+    cx0 = R(a.celldx[jj]);
+    icx = 1.0 / a.celldx[jj];
+    icx_r = R(icx);
+  }
+  const R dt_r = R(dt), dt_h_r = R(dt_h);
+  __syncthreads();
+  const int i1 = min(i0 + a.rows, ny - pad);
+  for (int ii = i0; ii < i1; ++ii) {
+    const int k = ii - i0;
+    R F = R(0), eF = R(0);
+    if (face_ok) {
+      const size_t f = fidx(nx, ii, jj);
+      const size_t c = cidx(nx, ii, jj);
+      mass_energy_flux<R, false>(a.u[f - 1], a.u[f], a.u[f + 1], s.r_in_r[c - 2],
+                                 s.r_in_r[c - 1], s.r_in_r[c], s.r_in_r[c + 1],
+                                 s.e_in_r[c - 2], s.e_in_r[c - 1], s.e_in_r[c],
+                                 s.e_in_r[c + 1], iex, cxm, cx0, icx_r,
+                                 R(s_ey0[k]), dt_r, dt_h_r, &F, &eF);
+      if (face_owner) {
+        a.F_x[f] = F;
+        mirror(a.F_x, nx + 1, ny, pad, ii, jj, F, true, false);
+      }
+    }
+    sF[t] = F;
+    seF[t] = eF;
+    __syncthreads();
+    if (cell_ok) {
+      const size_t c = cidx(nx, ii, jj);
+      const double r_old = kFirst ? s.r_in[c] : a.rho[c];
+      double r_new, e_new;
+      mass_energy_update<R, kFirst>(s.r_in[c], s.e_in[c], r_old, dt_h,
+                                    a.celldx[jj] * s_cyd[k], s_coef[k] * icx,
+                                    s_ey0[k], s_ey1[k], sF[t],
+                                    sF[t + 1], seF[t], seF[t + 1], &r_new, &e_new);
+      store_cell(s.r_out, s.r_out_r, nx, ny, pad, ii, jj, r_new);
+      store_cell(s.e_out, s.e_out_r, nx, ny, pad, ii, jj, e_new);
+    }
+    __syncthreads();
+  }
+}
+
+// y sweep: each thread marches down its column; face row ii+1 is computed
+// in iteration ii and reused by the cell below.
+template <typename R, bool kFirst>
+__device__ __forceinline__ void tile_mass_sweep_y(const StepArgs<R>& a,
+                                                        const SweepArgs<R>& s, int bx, int by) {
+  __shared__ R s_iey[kMaxRows + 1], s_cy[kMaxRows + 2], s_icy[kMaxRows + 1];
+  __shared__ double s_coef[kMaxRows], s_cyd[kMaxRows];
+  const int nx = a.nx, ny = a.ny, pad = a.pad;
+  const int jj = pad + bx * kCols + threadIdx.x;
+  const int i0 = pad + by * a.rows;
+  const double dt = a.dt_slot[0], dt_h = a.dt_slot[1];
+  // Face rows i0 .. i0+a.rows, cell rows i0-1 .. i0+a.rows.
+  if (threadIdx.x < a.rows + 2) {
+    const int ii = i0 - 1 + threadIdx.x;
+    if (ii < ny) s_cy[threadIdx.x] = R(a.celldy[ii]);
+  }
+  if (threadIdx.x < a.rows + 1) {
+    const int ii = i0 + threadIdx.x;
+    if (ii < ny) {
+      s_iey[threadIdx.x] = R(1.0 / a.edgedy[ii]);
+      s_icy[threadIdx.x] = R(1.0 / a.celldy[ii]);
+      if (threadIdx.x < a.rows) {
+        s_coef[threadIdx.x] = 1.0 / a.celldy[ii];
+        s_cyd[threadIdx.x] = a.celldy[ii];
+      }
+    }
+  }
+  __syncthreads();
+  if (jj >= nx - pad) return;
+  const double icx = 1.0 / a.celldx[jj];
+  const double ex0 = a.edgedx[jj], ex1 = a.edgedx[jj + 1];
+  const R ex0_r = R(ex0), dt_r = R(dt), dt_h_r = R(dt_h);
+  const int i1 = min(i0 + a.rows, ny - pad);
+  const int last_face = ny - pad;  // the north boundary face row
+  // Windows at face row f: cells f-2..f+1, velocities f-1..f+1.
+  R r[4], e[4], w[3];
+  for (int q = 0; q < 4; ++q) {
+    const size_t c = cidx(nx, i0 - 2 + q, jj);
+    r[q] = s.r_in_r[c];
+    e[q] = s.e_in_r[c];
+  }
+  for (int q = 0; q < 3; ++q) w[q] = a.v[cidx(nx, i0 - 1 + q, jj)];
+  R F0, eF0;
+  mass_energy_flux<R, true>(w[0], w[1], w[2], r[0], r[1], r[2], r[3], e[0], e[1],
+                            e[2], e[3], s_iey[0], s_cy[0], s_cy[1], s_icy[0],
+                            ex0_r, dt_r, dt_h_r, &F0, &eF0);
+  {
+    const size_t c = cidx(nx, i0, jj);
+    a.F_y[c] = F0;
+    mirror(a.F_y, nx, ny + 1, pad, i0, jj, F0, false, true);
+  }
+  for (int ii = i0; ii < i1; ++ii) {
+    const int k = ii - i0;
+    for (int q = 0; q < 3; ++q) {
+      r[q] = r[q + 1];
+      e[q] = e[q + 1];
+    }
+    const size_t c_next = cidx(nx, ii + 2, jj);
+    r[3] = s.r_in_r[c_next];
+    e[3] = s.e_in_r[c_next];
+    w[0] = w[1];
+    w[1] = w[2];
+    w[2] = a.v[cidx(nx, ii + 2, jj)];
+    R F1, eF1;
+    mass_energy_flux<R, true>(w[0], w[1], w[2], r[0], r[1], r[2], r[3], e[0],
+                              e[1], e[2], e[3], s_iey[k + 1], s_cy[k + 1],
+                              s_cy[k + 2], s_icy[k + 1], ex0_r, dt_r, dt_h_r, &F1,
+                              &eF1);
+    if (ii + 1 < i1 || ii + 1 == last_face) {
+      const size_t c = cidx(nx, ii + 1, jj);
+      a.F_y[c] = F1;
+      mirror(a.F_y, nx, ny + 1, pad, ii + 1, jj, F1, false, true);
+    }
+    const size_t c = cidx(nx, ii, jj);
+    const double r_old = kFirst ? s.r_in[c] : a.rho[c];
+    double r_new, e_new;
+    mass_energy_update<R, kFirst>(s.r_in[c], s.e_in[c], r_old, dt_h,
+                                  a.celldx[jj] * s_cyd[k], s_coef[k] * icx, ex0, ex1,
+                                  F0, F1, eF0, eF1, &r_new, &e_new);
+    store_cell(s.r_out, s.r_out_r, nx, ny, pad, ii, jj, r_new);
+    store_cell(s.e_out, s.e_out_r, nx, ny, pad, ii, jj, e_new);
+    F0 = F1;
+    eF0 = eF1;
+  }
+}
+
+// ===========================================================================
+// Advection of momentum (omp3/flow.c:557-970).
+
+// MC-limited upwind value of a velocity at a flux point from its four
+// neighbours along the direction (m2, m1 | p0, p1): omp3/flow.c:791-820.
+template <typename R>
+__device__ __forceinline__ R momentum_upwind(R wind, R m2, R m1, R p0, R p1,
+                                             R inv_h, R d_left, R d_right,
+                                             R dt_h) {
+  const bool pos = Prec<R>::gt0(wind);
+  return mc_face(pos, pos ? p0 - m2 : p1 - m1, pos ? m1 - m2 : p0 - m1,
+                 pos ? p0 - m1 : p1 - p0, R(0.5) * inv_h, R(2) * inv_h,
+                 pos ? m1 : p0, pos ? d_left : d_right, wind * dt_h);
+}
+
+// uF_x on interior cells (omp3/flow.c:778-823).
+template <typename R>
+__device__ __forceinline__ void tile_flux_uFx(const StepArgs<R>& a, int bx, int by) {
+  __shared__ R s_hey[kMaxRows];
+  const int nx = a.nx, ny = a.ny, pad = a.pad;
+  const int jj = pad + bx * kCols + threadIdx.x;
+  const int i0 = pad + by * a.rows;
+  if (threadIdx.x < a.rows && i0 + (int)threadIdx.x < ny) {
+    s_hey[threadIdx.x] = R(a.edgedy[i0 + threadIdx.x] * 0.5);
+  }
+  __syncthreads();
+  if (jj >= nx - pad) return;
+  const R dt_h = R(a.dt_slot[1]);
+  const R iex = R(1.0 / a.edgedx[jj]);
+  const R cxl = R(a.celldx[jj - 1]), cxr = R(a.celldx[jj]);
+  const int i1 = min(i0 + a.rows, ny - pad);
+  for (int ii = i0; ii < i1; ++ii) {
+    const size_t f = fidx(nx, ii, jj);
+    const R u0 = a.u[f], u1 = a.u[f + 1];
+    const R mass = s_hey[ii - i0] * (a.F_x[f] + a.F_x[f + 1]);
+    const R wind = R(0.5) * (u0 + u1);
+    const R val = mass * momentum_upwind(wind, a.u[f - 1], u0, u1, a.u[f + 2], iex,
+                                         cxl, cxr, dt_h);
+    a.uF_x[cidx(nx, ii, jj)] = val;
+    mirror(a.uF_x, nx, ny, pad, ii, jj, val, false, false);
+  }
+}
+
+// uF_y on corners (omp3/flow.c:826-874).
+template <typename R>
+__device__ __forceinline__ void tile_flux_uFy(const StepArgs<R>& a, int bx, int by) {
+  __shared__ R s_iey[kMaxRows], s_cy[kMaxRows + 1];
+  const int nx = a.nx, ny = a.ny, pad = a.pad;
+  const int jj = pad + bx * kCols + threadIdx.x;
+  const int i0 = pad + by * a.rows;
+  if (threadIdx.x < a.rows + 1) {
+    const int ii = i0 - 1 + threadIdx.x;
+    if (ii < ny) s_cy[threadIdx.x] = R(a.celldy[ii]);
+    if (threadIdx.x >= 1 && ii < ny) s_iey[threadIdx.x - 1] = R(1.0 / a.edgedy[ii]);
+  }
+  __syncthreads();
+  if (jj >= nx + 1 - pad) return;
+  const R dt_h = R(a.dt_slot[1]);
+  const R ex = R(a.edgedx[jj]);
+  const int i1 = min(i0 + a.rows, ny + 1 - pad);
+  R um2 = a.u[fidx(nx, i0 - 2, jj)];
+  R um1 = a.u[fidx(nx, i0 - 1, jj)];
+  R u0 = a.u[fidx(nx, i0, jj)];
+  for (int ii = i0; ii < i1; ++ii) {
+    const int k = ii - i0;
+    const R up = a.u[fidx(nx, ii + 1, jj)];
+    const size_t c = cidx(nx, ii, jj);
+    const R mass = ex * R(0.5) * (a.F_y[c] + a.F_y[c - 1]);
+    const R wind = R(0.5) * (a.v[c - 1] + a.v[c]);
+    const R val = mass * momentum_upwind(wind, um2, um1, u0, up, s_iey[k], s_cy[k],
+                                         s_cy[k + 1], dt_h);
+    a.uF_y[fidx(nx, ii, jj)] = val;
+    mirror(a.uF_y, nx + 1, ny + 1, pad, ii, jj, val, false, false);
+    um2 = um1;
+    um1 = u0;
+    u0 = up;
+  }
+}
+
+// vF_x on corners (omp3/flow.c:877-925).
+template <typename R>
+__device__ __forceinline__ void tile_flux_vFx(const StepArgs<R>& a, int bx, int by) {
+  __shared__ R s_hcy[kMaxRows];
+  const int nx = a.nx, ny = a.ny, pad = a.pad;
+  const int jj = pad + bx * kCols + threadIdx.x;
+  const int i0 = pad + by * a.rows;
+  if (threadIdx.x < a.rows && i0 + (int)threadIdx.x < ny) {
+    s_hcy[threadIdx.x] = R(a.celldy[i0 + threadIdx.x] * 0.5);
+  }
+  __syncthreads();
+  if (jj >= nx + 1 - pad) return;
+  const R dt_h = R(a.dt_slot[1]);
+  const R iex = R(1.0 / a.edgedx[jj]);
+  const R cxl = R(a.celldx[jj - 1]), cxr = R(a.celldx[jj]);
+  const int i1 = min(i0 + a.rows, ny + 1 - pad);
+  R u_dn = a.u[fidx(nx, i0 - 1, jj)], F_dn = a.F_x[fidx(nx, i0 - 1, jj)];
+  for (int ii = i0; ii < i1; ++ii) {
+    const size_t f = fidx(nx, ii, jj);
+    const size_t c = cidx(nx, ii, jj);
+    const R u0 = a.u[f], F0 = a.F_x[f];
+    const R mass = s_hcy[ii - i0] * (F0 + F_dn);
+    const R wind = R(0.5) * (u0 + u_dn);
+    const R val = mass * momentum_upwind(wind, a.v[c - 2], a.v[c - 1], a.v[c],
+                                         a.v[c + 1], iex, cxl, cxr, dt_h);
+    a.vF_x[f] = val;
+    mirror(a.vF_x, nx + 1, ny + 1, pad, ii, jj, val, false, false);
+    u_dn = u0;
+    F_dn = F0;
+  }
+}
+
+// vF_y on interior cells (omp3/flow.c:928-970).
+template <typename R>
+__device__ __forceinline__ void tile_flux_vFy(const StepArgs<R>& a, int bx, int by) {
+  __shared__ R s_iey[kMaxRows], s_cy[kMaxRows + 1];
+  const int nx = a.nx, ny = a.ny, pad = a.pad;
+  const int jj = pad + bx * kCols + threadIdx.x;
+  const int i0 = pad + by * a.rows;
+  if (threadIdx.x < a.rows + 1) {
+    const int ii = i0 - 1 + threadIdx.x;
+    if (ii < ny) s_cy[threadIdx.x] = R(a.celldy[ii]);
+    if (threadIdx.x >= 1 && ii < ny) s_iey[threadIdx.x - 1] = R(1.0 / a.edgedy[ii]);
+  }
+  __syncthreads();
+  if (jj >= nx - pad) return;
+  const R dt_h = R(a.dt_slot[1]);
+  const R cx = R(a.celldx[jj]);
+  const int i1 = min(i0 + a.rows, ny - pad);
+  R vm = a.v[cidx(nx, i0 - 1, jj)];
+  R v0 = a.v[cidx(nx, i0, jj)];
+  R vp = a.v[cidx(nx, i0 + 1, jj)];
+  R F0 = a.F_y[cidx(nx, i0, jj)];
+  for (int ii = i0; ii < i1; ++ii) {
+    const int k = ii - i0;
+    const R vp2 = a.v[cidx(nx, ii + 2, jj)];
+    const R F1 = a.F_y[cidx(nx, ii + 1, jj)];
+    const R mass = cx * R(0.5) * (F0 + F1);
+    const R wind = R(0.5) * (v0 + vp);
+    const R val = mass * momentum_upwind(wind, vm, v0, vp, vp2, s_iey[k], s_cy[k],
+                                         s_cy[k + 1], dt_h);
+    a.vF_y[cidx(nx, ii, jj)] = val;
+    mirror(a.vF_y, nx, ny, pad, ii, jj, val, false, false);
+    vm = v0;
+    v0 = vp;
+    vp = vp2;
+    F0 = F1;
+  }
+}
+
+// Momentum updates (omp3/flow.c:577-668, 683-771).  kWhich: 0 rho_u by uF_x,
+// 1 rho_u by uF_y, 2 rho_v by vF_x, 3 rho_v by vF_y; kVel recomputes the
+// velocity from the post-advection density.
+template <typename R, int kWhich, bool kVel>
+__device__ __forceinline__ void tile_momentum_update(const StepArgs<R>& a, int bx, int by) {
+  using Pr = Prec<R>;
+  constexpr bool kU = kWhich < 2;
+  __shared__ R s_h[kMaxRows], s_row[kMaxRows], s_wy0[kMaxRows], s_wy1[kMaxRows];
+  const int nx = a.nx, ny = a.ny, pad = a.pad;
+  const int jj = pad + bx * kCols + threadIdx.x;
+  const int i0 = pad + by * a.rows;
+  const double dt_h = a.dt_slot[1];
+  if (threadIdx.x < a.rows) {
+    const int ii = i0 + threadIdx.x;
+    if (ii < ny) {
+      // Row factor of the flux divergence: 1/celldy for x fluxes of rho_u
+      // and rho_v, 1/edgedy for the y fluxes.
+      const double h = (kWhich == 0 || kWhich == 2) ? a.celldy[ii] : a.edgedy[ii];
+      s_h[threadIdx.x] = R(h);
+      s_row[threadIdx.x] = R(1.0 / h);
+      if (!kU && kVel) {
+        const double ey = a.edgedy[ii];
+        s_wy0[threadIdx.x] = R(a.celldy[ii] / (2.0 * ey));
+        s_wy1[threadIdx.x] = R(a.celldy[ii - 1] / (2.0 * ey));
+      }
+    }
+  }
+  __syncthreads();
+  const int col_end = kU ? nx + 1 - pad : nx - pad;
+  const int row_end = kU ? ny - pad : ny + 1 - pad;
+  if (jj >= col_end) return;
+  const double hx = (kWhich == 0 || kWhich == 2) ? a.edgedx[jj] : a.celldx[jj];
+  const R hx_r = R(hx);
+  const R ihx = R(1.0 / hx);
+  const R dt_h_r = R(dt_h);
+  R wx0 = R(0), wx1 = R(0);
+  if (kU && kVel) {
+    const double ex = a.edgedx[jj];
+    wx0 = R(a.celldx[jj] / (2.0 * ex));
+    wx1 = R(a.celldx[jj - 1] / (2.0 * ex));
+  }
+  const int i1 = min(i0 + a.rows, row_end);
+  for (int ii = i0; ii < i1; ++ii) {
+    const int k = ii - i0;
+    const size_t f = fidx(nx, ii, jj);
+    const size_t c = cidx(nx, ii, jj);
+    R diff;
+    if (kWhich == 0) diff = a.uF_x[c] - a.uF_x[c - 1];
+    else if (kWhich == 1) diff = a.uF_y[f + (nx + 1)] - a.uF_y[f];
+    else if (kWhich == 2) diff = a.vF_x[f + 1] - a.vF_x[f];
+    else diff = a.vF_y[c] - a.vF_y[c - nx];
+    R* mom = kU ? a.rho_u + f : a.rho_v + c;
+    // mom - dt_h * diff / (hx * hy), the divisor rounded as the reference
+    // forms it (omp3/flow.c:581-584).
+    const R m = Pr::dsub(*mom, dt_h_r * diff, hx_r * s_h[k], s_row[k] * ihx);
+    *mom = m;
+    if (kVel) {
+      R rbar;
+      if (kU) rbar = fma(a.rho_r[c], wx0, a.rho_r[c - 1] * wx1);
+      else rbar = fma(a.rho_r[c], s_wy0[k], a.rho_r[c - nx] * s_wy1[k]);
+      const R vel = Pr::is_zero(rbar) ? R(0) : Pr::qdiv(m, rbar, Pr::rcp(rbar));
+      if (kU) {
+        a.u[f] = vel;
+        mirror(a.u, nx + 1, ny, pad, ii, jj, vel, true, false);
+      } else {
+        a.v[c] = vel;
+        mirror(a.v, nx, ny + 1, pad, ii, jj, vel, false, true);
+      }
+    }
+  }
+}
+
+
+}  // namespace tiles
+}  // namespace flow

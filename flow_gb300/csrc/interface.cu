@@ -553,4 +553,39 @@ int gb300_conservation(int nx, int ny, int pad, const double* rho,
   return st_conservation(nx, ny, pad, rho, e, reduce_array, out, sync);
 }
 
+// ===========================================================================
+// Part 3: the mixed-precision form.
+
+size_t gb300_mixed_workspace_bytes(int local_nx, int local_ny) {
+  return mixed_workspace_bytes(local_nx, local_ny);
+}
+
+int gb300_mixed_prepare(Mesh* mesh, double* rho, double* e, void* workspace,
+                        size_t bytes, double* reduce_array,
+                        int initial_timestep) {
+  if (!mesh) return record_error(GB300_ERR_ARG, "gb300_mixed_prepare: mesh is NULL");
+  FLOW_TRY(check_mesh(mesh, mesh->local_nx, mesh->local_ny, "gb300_mixed_prepare"));
+  FLOW_TRY(mixed_prepare(mesh, rho, e, workspace, bytes));
+  if (!initial_timestep) return GB300_OK;
+  // The driver's set_timestep(first_step = 0) before the loop (main.c:64-66)
+  // with the zero viscous stresses of a fresh state: a workspace block that
+  // mixed_prepare left zero serves as Qxx = Qyy = 0.
+  const double* zeros = reinterpret_cast<const double*>(
+      static_cast<const char*>(workspace) +
+      mixed_zero_block_offset(mesh->local_nx, mesh->local_ny));
+  return st_set_timestep(mesh->local_nx, mesh->local_ny, zeros, zeros, rho, e,
+                         mesh, reduce_array, 0, mesh->celldx, mesh->celldy);
+}
+
+int gb300_mixed_solve(Mesh* mesh, int tt, double* rho, double* e, float* rho_u,
+                      float* rho_v, void* workspace, size_t bytes,
+                      double* reduce_array) {
+  if (!mesh) return record_error(GB300_ERR_ARG, "gb300_mixed_solve: mesh is NULL");
+  FLOW_TRY(check_mesh(mesh, mesh->local_nx, mesh->local_ny, "gb300_mixed_solve"));
+  if (g_verbose && mesh->rank == 0) {
+    printf("Timestep:        %.12e\n", mesh->dt);
+  }
+  return mixed_solve(mesh, tt, rho, e, rho_u, rho_v, workspace, bytes, reduce_array);
+}
+
 }  // extern "C"

@@ -186,17 +186,20 @@ def two_region(n: int, rng: np.random.Generator) -> Problem:
 def fourier_field(n: int, rng: np.random.Generator, modes: int = 16,
                   kmax: int = 8, amplitude: float = 0.1) -> np.ndarray:
     """Sum of `modes` random Fourier modes with integer wavenumbers 1..kmax in
-    each direction, random phases, amplitudes scaled so sum |a_k| = amplitude."""
+    each direction, random phases, amplitudes scaled so sum |a_k| = amplitude.
+    Evaluated separably: cos(a + b) = cos a cos b - sin a sin b."""
     x = (np.arange(n) + 0.5) / n
     kx = rng.integers(1, kmax + 1, size=modes)
     ky = rng.integers(1, kmax + 1, size=modes)
     ph = rng.uniform(0.0, 2.0 * math.pi, size=modes)
     amp = rng.uniform(0.0, 1.0, size=modes)
     amp *= amplitude / amp.sum()
-    f = np.zeros((n, n))
-    for k in range(modes):
-        f += amp[k] * np.cos(2 * math.pi * (kx[k] * x[None, :] + ky[k] * x[:, None]) + ph[k])
-    return f
+    ax = 2 * math.pi * kx[:, None] * x[None, :] + ph[:, None]      # modes x n
+    ay = 2 * math.pi * ky[:, None] * x[None, :]
+    cx, sx = np.cos(ax) * amp[:, None], np.sin(ax) * amp[:, None]
+    cy, sy = np.cos(ay), np.sin(ay)
+    # f[i, j] = sum_k amp_k (cos(ay_k[i]) cos(ax_k[j]) - sin(ay_k[i]) sin(ax_k[j]))
+    return cy.T @ cx - sy.T @ sx
 
 
 def smooth_random(n: int, rng: np.random.Generator) -> Problem:

@@ -119,3 +119,80 @@ class DeviceSim:
         if st != GB300_OK:
             check()
         return float(out[0]), float(out[1])
+
+
+class MixedSim:
+    """One problem in the mixed-precision form: FP64 density and specific
+    energy, FP32 momenta, every other array in a device workspace."""
+
+    def __init__(self, prob: Problem, device: str = "cuda:0"):
+        torch = _torch()
+        self.torch = torch
+        self.prob = prob
+        self.device = torch.device(device)
+        nx, ny = prob.nx, prob.ny
+        self.nx, self.ny = nx, ny
+        f64 = dict(dtype=torch.float64, device=self.device)
+        f32 = dict(dtype=torch.float32, device=self.device)
+        self.rho = torch.from_numpy(np.ascontiguousarray(prob.rho, dtype=np.float64).reshape(-1)).to(self.device)
+        self.e = torch.from_numpy(np.ascontiguousarray(prob.e, dtype=np.float64).reshape(-1)).to(self.device)
+        self.rho_u = torch.zeros((nx + 1) * (ny + 1), **f32)
+        self.rho_v = torch.zeros((nx + 1) * (ny + 1), **f32)
+        self.reduce = torch.zeros(nx * ny, **f64)
+        L = lib()
+        self.work_bytes = int(L.gb300_mixed_workspace_bytes(nx, ny))
+        self.work = torch.zeros(self.work_bytes, dtype=torch.uint8, device=self.device)
+        self.mesh_arrays = {k: torch.from_numpy(np.ascontiguousarray(getattr(prob, k))).to(self.device)
+                            for k in ("edgex", "edgey", "edgedx", "edgedy", "celldx", "celldy")}
+        m = Mesh()
+        m.global_nx, m.global_ny = prob.gnx, prob.gny
+        m.local_nx, m.local_ny = nx, ny
+        m.pad, m.x_off, m.y_off, m.rank, m.nranks = PAD, 0, 0, 0, 1
+        for i in range(4):
+            m.neighbours[i] = -1
+        m.width, m.height = prob.width, prob.height
+        m.max_dt, m.sim_end = prob.max_dt, prob.sim_end
+        m.dt = C_T * prob.dt_param
+        m.dt_h = m.dt
+        for k, t in self.mesh_arrays.items():
+            setattr(m, k, dptr(t))
+        self.mesh = m
+        self.tt = 0
+        for f in (self.rho, self.e):
+            L.handle_boundary_2d(nx, ny, ctypes.byref(m), dptr(f), 0, 1)
+        check()
+        from . import vptr
+        self.vptr = vptr
+        if L.gb300_mixed_prepare(ctypes.byref(m), dptr(self.rho), dptr(self.e), vptr(self.work),
+                                 self.work_bytes, dptr(self.reduce), 1) != GB300_OK:
+            check()
+
+    def step(self) -> None:
+        L = lib()
+        st = L.gb300_mixed_solve(ctypes.byref(self.mesh), self.tt, dptr(self.rho), dptr(self.e),
+                                 self.vptr(self.rho_u), self.vptr(self.rho_v), self.vptr(self.work),
+                                 self.work_bytes, dptr(self.reduce))
+        if st != GB300_OK:
+            check()
+        self.tt += 1
+
+    def run(self, steps: int) -> None:
+        for _ in range(steps):
+            self.step()
+
+    def interior(self, name: str) -> np.ndarray:
+        nx, ny, p = self.nx, self.ny, PAD
+        a = getattr(self, name).cpu().numpy().astype(np.float64)
+        if name == "rho_u":
+            return a[: ny * (nx + 1)].reshape(ny, nx + 1)[p:ny - p, p:nx + 1 - p]
+        if name == "rho_v":
+            return a[: (ny + 1) * nx].reshape(ny + 1, nx)[p:ny + 1 - p, p:nx - p]
+        return a[: nx * ny].reshape(ny, nx)[p:ny - p, p:nx - p]
+
+    def conservation(self) -> tuple[float, float]:
+        out = (ctypes.c_double * 2)()
+        st = lib().gb300_conservation(self.nx, self.ny, PAD, dptr(self.rho), dptr(self.e),
+                                      dptr(self.reduce), ctypes.cast(out, ctypes.POINTER(ctypes.c_double)), 1)
+        if st != GB300_OK:
+            check()
+        return float(out[0]), float(out[1])

@@ -5,8 +5,8 @@
  * Part 1 is the reference's own kernel-set interface, with identical names,
  * argument order and meaning, so that an unmodified host driver (main.c) can
  * select this set the way it selects omp3 or cuda (`KERNELS=gb300`).  Part 2
- * adds status-returning control functions.  Part 3 is the mixed-precision and
- * batched forms.
+ * adds status-returning control functions.  Part 3 is the mixed-precision
+ * form.
  *
  * Memory: every array argument is a DEVICE pointer (as for the reference cuda
  * set).  The Mesh struct is host memory; its edgedx/edgedy/celldx/celldy
@@ -189,6 +189,71 @@ int gb300_profile_reset(void);
 int gb300_profile_count(void);
 int gb300_profile_entry(int i, char* name, int name_len, long long* launches,
                         double* total_ms);
+
+/* ===== Part 3: the mixed-precision form ================================== */
+
+/* Same scheme and step sequence as solve_hydro_2d, with FP32 arithmetic for
+ * the equation of state, accelerations, viscosity, shock heating, the CFL
+ * candidates and all fluxes, and FP64 for the stored density and specific
+ * energy, their conservative update in advection, the energy increment of
+ * shock heating, the dt minimum and the conservation totals.  Momenta are
+ * FP32 face arrays ((nx+1)*(ny+1) floats, same layout as the FP64 ones).
+ * Every other array lives in a caller-provided device workspace of
+ * gb300_mixed_workspace_bytes() bytes (the form never allocates). */
+size_t gb300_mixed_workspace_bytes(int local_nx, int local_ny);
+
+/* Zeroes the workspace and derives its FP32 copies of rho and e (whose
+ * ghosts must already be filled); with initial_timestep = 1 also performs the
+ * driver's first set_timestep (first_step = 0, zero viscous stresses). */
+int gb300_mixed_prepare(Mesh* mesh, double* rho, double* e, void* workspace,
+                        size_t bytes, double* reduce_array,
+                        int initial_timestep);
+
+/* One timestep; updates mesh->dt and mesh->dt_h like solve_hydro_2d. */
+int gb300_mixed_solve(Mesh* mesh, int tt, double* rho, double* e, float* rho_u,
+                      float* rho_v, void* workspace, size_t bytes,
+                      double* reduce_array);
+
+/* ===== Part 4: batched ensembles ========================================== */
+
+/* Many independent problems of different sizes, each with its own dt,
+ * advanced together: one persistent cooperative kernel launch per timestep
+ * runs every phase of the step over a flattened list of (instance, tile) work
+ * items, separated by bounded grid barriers; pairs of steps replay a captured
+ * CUDA graph.  precision 0 = FP64 form, 1 = mixed form.  Every instance is a
+ * uniform mesh of global_nx x global_ny interior cells (pad 2) over
+ * width x height, with reflective walls.  All device memory is one
+ * caller-provided pool of gb300_batch_pool_bytes() bytes. */
+typedef struct GB300Batch GB300Batch;
+
+int gb300_batch_create(int n, const int* global_nx, const int* global_ny,
+                       const double* width, const double* height, int precision,
+                       GB300Batch** out);
+size_t gb300_batch_pool_bytes(const GB300Batch* batch);
+/* Lays the instances out in the pool (zeroed) and builds the work lists. */
+int gb300_batch_bind(GB300Batch* batch, void* pool, size_t bytes);
+/* Host interior density / specific energy (global_ny x global_nx, row-major)
+ * of instance i, ghost fill, and the driver's first set_timestep with the
+ * params dt dt_param (main.c:30, 64-66). */
+int gb300_batch_set_state(GB300Batch* batch, int i, const double* rho,
+                          const double* e, double dt_param);
+/* Tile height (1..32 rows), CTAs per SM of the persistent launch (0 = as many
+ * as fit) and work order (0 largest instance first, 1 input order). */
+int gb300_batch_set_tuning(GB300Batch* batch, int rows, int ctas_per_sm,
+                           int order);
+int gb300_batch_get_tuning(const GB300Batch* batch, int* rows,
+                           int* ctas_per_sm, int* order, int* grid);
+/* Advances every instance by `steps` timesteps (asynchronous on the current
+ * stream); use_graph replays pairs of steps from a captured CUDA graph. */
+int gb300_batch_step(GB300Batch* batch, int steps, int use_graph);
+/* Synchronises and returns GB300_ERR_TIMEOUT if a grid barrier ran out. */
+int gb300_batch_status(GB300Batch* batch);
+/* Interior fields (host, optional), dt/dt_h pair and interior totals of rho
+ * and rho*e of instance i. */
+int gb300_batch_get_state(GB300Batch* batch, int i, double* rho, double* e,
+                          double* dt_pair, double* totals);
+long long gb300_batch_cells(const GB300Batch* batch);
+void gb300_batch_destroy(GB300Batch* batch);
 
 /* Measured FP64 FMA issue rate of the current GPU (FMA instructions per
  * second per GPU), the compute roofline of the FP64 timestep.  Allocates a

@@ -1,0 +1,95 @@
+"""The batched form (one persistent cooperative launch per timestep over many
+instances of different sizes, each with its own dt) against the
+single-problem fused step: every instance must match it bit for bit, in both
+precision forms, with or without the captured CUDA graph and for every tile
+shape; the FP64 instances must also match the oracle (1e-12 per cell for
+density and energy)."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from tolerance import FP64_TOL, cell_rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def fg():
+    import flow_gb300
+    flow_gb300.lib()
+    flow_gb300.set_mode(flow_gb300.MODE_FUSED)
+    return flow_gb300
+
+
+def ensemble():
+    from flow_gb300 import problems
+    rng = np.random.default_rng(7)
+    return [problems.sod(40, 36), problems.sedov(64), problems.two_region(48, rng),
+            problems.two_region(24, rng), problems.smooth_random(33, rng)]
+
+
+def single(fg, prob, steps, precision):
+    sim = fg.DeviceSim(prob) if precision == 0 else fg.MixedSim(prob)
+    if precision == 0:
+        sim.initial_timestep()
+    sim.run(steps)
+    return sim
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("use_graph", [False, True])
+def test_batch_matches_single_problem_step(fg, precision, use_graph):
+    probs = ensemble()
+    steps = 9
+    b = fg.Batch(probs, precision=precision)
+    b.step(steps, use_graph=use_graph)
+    b.status()
+    for i, p in enumerate(probs):
+        rho, e, dt, _ = b.state(i)
+        sim = single(fg, p, steps, precision)
+        assert np.array_equal(rho, sim.interior("rho")), (i, "rho")
+        assert np.array_equal(e, sim.interior("e")), (i, "e")
+        assert dt[0] == sim.mesh.dt and dt[1] == sim.mesh.dt_h, i
+
+
+@pytest.mark.parametrize("tuning", [(8, 0, 0), (32, 1, 1), (16, 2, 0)])
+def test_batch_tile_shapes_give_identical_results(fg, tuning):
+    probs = ensemble()[:3]
+    ref = fg.Batch(probs, precision=0)
+    ref.step(6)
+    b = fg.Batch(probs, precision=0)
+    b.set_tuning(*tuning)
+    b.step(6)
+    b.status()
+    for i in range(len(probs)):
+        assert np.array_equal(b.state(i)[0], ref.state(i)[0])
+        assert np.array_equal(b.state(i)[1], ref.state(i)[1])
+
+
+def test_batch_fp64_matches_oracle(fg):
+    probs = ensemble()[:3]
+    steps = 20
+    b = fg.Batch(probs, precision=0)
+    b.step(steps)
+    for i, p in enumerate(probs):
+        hm = O.HostMesh(p.gnx, p.gny, dt=p.dt_param)
+        st = O.HostState(hm)
+        O.fill_fields(hm, st, p.interior(p.rho), p.interior(p.e))
+        O.initial_timestep(hm, st)
+        O.run(hm, st, steps)
+        rho, e, dt, tot = b.state(i)
+        assert cell_rel_err(rho, st.interior("rho")) <= FP64_TOL
+        assert cell_rel_err(e, st.interior("e")) <= FP64_TOL
+        assert abs(dt[0] - hm.mesh.dt) <= FP64_TOL * hm.mesh.dt
+        m0 = float(p.interior(p.rho).sum())
+        assert abs(tot[0] - m0) <= 1e-13 * m0
+
+
+def test_batch_rejects_bad_arguments(fg):
+    import ctypes
+    L = fg.lib()
+    h = ctypes.c_void_p()
+    one = (ctypes.c_int * 1)(1)
+    assert L.gb300_batch_create(1, one, one, None, None, 0, ctypes.byref(h)) == 2
+    L.gb300_batch_clear = None
+    fg.lib().gb300_clear_error()
