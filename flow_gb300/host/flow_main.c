@@ -74,7 +74,7 @@ static int validate(const int nx, const int ny, const int pad,
   if (fp) fclose(fp);
   if (!have || !get_key_value_parameter(base, "flow.tests", keys, values, &n) || n < 2) {
     printf("Warning. Test entry was not found, could NOT validate.\n");
-    printf("density total %.12e, energy total %.12e\n", dtot, etot);
+    printf("density total %.17e, energy total %.17e\n", dtot, etot);
     free(keys);
     return 1;
   }

@@ -26,12 +26,19 @@
 #ifndef FLOW_GB300_MESH_H
 #define FLOW_GB300_MESH_H
 
+/* A build inside the arch project can use arch's own Mesh/SharedData: define
+ * FLOW_EXTERNAL_MESH_HEADER (e.g. "../mesh.h") when compiling the kernel set.
+ * The kernel set only reads the fields listed above by name. */
+enum { FLOW_NORTH = 0, FLOW_EAST = 1, FLOW_SOUTH = 2, FLOW_WEST = 3 };
+#define FLOW_EDGE (-1) /* neighbour value at a physical (reflective) wall */
+
+#ifdef FLOW_EXTERNAL_MESH_HEADER
+#include FLOW_EXTERNAL_MESH_HEADER
+#else
+
 #ifdef __cplusplus
 extern "C" {
 #endif
-
-enum { FLOW_NORTH = 0, FLOW_EAST = 1, FLOW_SOUTH = 2, FLOW_WEST = 3 };
-#define FLOW_EDGE (-1) /* neighbour value at a physical (reflective) wall */
 
 typedef struct {
   int global_nx, global_ny; /* interior cells of the whole problem */
@@ -70,5 +77,7 @@ typedef struct {
 #ifdef __cplusplus
 }
 #endif
+
+#endif /* FLOW_EXTERNAL_MESH_HEADER */
 
 #endif /* FLOW_GB300_MESH_H */

@@ -76,9 +76,12 @@ def have_reference() -> bool:
 
 
 def lib(kind: str = "port") -> ctypes.CDLL:
-    """``port`` (strict restatement), ``fast`` (timed flags) or ``reference``."""
+    """``port`` (strict restatement), ``fast`` (timed flags), ``reference``
+    (omp3/flow.c, strict IEEE evaluation) or ``reference_default`` (omp3/flow.c
+    with the reference's default -O3 -march=native flags)."""
     return _load({"port": "libflow_oracle.so", "fast": "libflow_oracle_fast.so",
-                  "reference": os.path.join("_ref", "libflow_ref.so")}[kind])
+                  "reference": os.path.join("_ref", "libflow_ref.so"),
+                  "reference_default": os.path.join("_ref", "libflow_ref_default.so")}[kind])
 
 
 def _declare(lib: ctypes.CDLL) -> None:
@@ -226,7 +229,8 @@ def fill_fields(hm: HostMesh, st: HostState, rho_int: np.ndarray, e_int: np.ndar
 
 
 def sod_boxes():
-    """Sod tube of BASELINE config 0: right state everywhere, left half high."""
+    """Sod shock tube (the 512x512 CPU-runnable case): right state everywhere,
+    left half high."""
     return [(0.125, 2.0, 0.0, 0.0, 1.0, 1.0), (1.0, 2.5, 0.0, 0.0, 0.5, 1.0)]
 
 

@@ -7,7 +7,9 @@ oracle/_ref/libflow_ref.so from omp3/flow.c with the arch shim):
 
 Each case stores its initial interior density/energy, the params dt, the
 step count, and every array of the reference host state after the run
-(main.c:52-62 layout), plus the dt/dt_h history.  The reference's own
+(main.c:52-62 layout), plus the dt/dt_h history; the state fields are also
+stored as the reference's default build (-march=native, FMA contraction)
+computes them, which measures the reference's own rounding variation.  The reference's own
 known-answer vector (flow.tests:1) is checked separately by
 tests/test_oracle.py.
 """
@@ -23,6 +25,8 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 
 from oracle import oracle as O  # noqa: E402
+
+STATE_FIELDS = ("rho", "e", "u", "v", "rho_u", "rho_v")
 
 
 def _smooth(n_x, n_y, rng, modes=16, kmax=8, amp=0.1):
@@ -62,6 +66,8 @@ def cases():
     r = 1.0 + _smooth(20, 28, rng)
     e = 1.0 + _smooth(20, 28, rng)
     out["smooth_20x28"] = dict(rho=r, e=e, dt=_cfl(20, 28, e), steps=21)
+    _, r, e = _boxes_state(151, 93, O.flow_params_boxes())
+    out["refproblem_151x93"] = dict(rho=r, e=e, dt=1e-3, steps=41)
     r = np.array([[1.0, 0.5], [0.25, 0.75], [0.6, 0.9]])
     e = np.array([[2.0, 1.0], [1.5, 3.0], [2.5, 0.8]])
     out["tiny_2x3"] = dict(rho=r, e=e, dt=_cfl(2, 3, e), steps=9)
@@ -81,13 +87,34 @@ def run_case(kind, c):
     return hm, st, np.array(hist)
 
 
+def write_reference_case():
+    """The reference's known-answer case in the reference params format,
+    restated from its problem (flow.params:1-6), and its golden totals
+    (flow.tests:1), for the C-driver test."""
+    lines = ["problem_0 density=0.125 energy=2.0 xpos=0.0 ypos=0.0 width=1.0 height=1.0",
+             "problem_1 density=1.0 energy=2.5 xpos=0.4 ypos=0.4 width=0.2 height=0.2",
+             "dt            1.0e-3", "nx            4096", "ny            4096",
+             "iterations    100", "visit_dump    0"]
+    with open(os.path.join(HERE, "flow.params"), "w") as f:
+        f.write("\n".join(lines) + "\n")
+    with open("/root/reference/flow.tests") as f:
+        golden = f.read().strip()
+    with open(os.path.join(HERE, "flow.tests"), "w") as f:
+        f.write(golden + "\n")
+
+
 def main():
+    write_reference_case()
     if not O.have_reference():
         O.build()
     assert O.have_reference(), "needs the reference sources to build oracle/_ref"
     for name, c in cases().items():
         hm, st, hist = run_case("reference", c)
+        # The reference built with its default flags: how far its own builds
+        # differ per cell (rounding only), stored for the state fields.
+        _, st_d, _ = run_case("reference_default", c)
         arrays = {f"out_{k}": v for k, v in st.a.items() if k != "reduce"}
+        arrays.update({f"default_out_{k}": st_d.a[k] for k in STATE_FIELDS})
         np.savez_compressed(os.path.join(HERE, f"{name}.npz"), rho0=c["rho"], e0=c["e"],
                             dt_param=c["dt"], steps=c["steps"], dt_hist=hist, **arrays)
         print(name, hm.gnx, hm.gny, c["steps"], "dt", hist[-1])
