@@ -62,6 +62,8 @@ def parse_args():
     p.add_argument("--size", type=int, default=N_CELLS_SIDE)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--fp64-only", action="store_true", help="skip the mixed/batched forms")
+    p.add_argument("--sod-size", type=int, default=8192,
+                   help="side of the Sod tube of the mixed form (0 skips it)")
     p.add_argument("--batch-steps", type=int, default=20,
                    help="timed steps of each batched form (a sample of its 200/1000)")
     return p.parse_args()
@@ -212,6 +214,11 @@ def field_errors(fg, got, want, names=("rho", "e")):
     for k in names:
         a = got.interior(k)
         b = want.interior(k)
+        if abs(b).max() == 0.0:
+            # A field that stays zero in the FP64 path (rho_v of a tube split
+            # along x): absolute errors instead.
+            out[k] = {"l1_abs": float(abs(a - b).mean()), "linf_abs": float(abs(a - b).max())}
+            continue
         out[k] = {"l1": float(abs(a - b).sum() / abs(b).sum()),
                   "linf": float(abs(a - b).max() / abs(b).max())}
     return out
@@ -400,19 +407,37 @@ def run_gpu(args):
     # ---- the mixed-precision form on the same workload ----
     forms = {}
     if not args.fp64_only:
-        mixed, msim = run_mixed_form(fg, problems, torch, device, n, args.steps, args.warmup)
-        # Error against the FP64 path after the same number of steps from the
-        # same initial state (the FP64 path itself matches the CPU oracle to
-        # ~1e-13 per cell).
-        ref = fg.DeviceSim(problems.sedov(n), device)
-        ref.initial_timestep()
-        ref.run(args.steps + args.warmup)
-        mixed["errors_vs_fp64"] = field_errors(fg, msim, ref)
-        mixed["mass_drift"] = abs(msim.conservation()[0] - ref.conservation()[0]) / ref.conservation()[0]
-        mixed["speedup_vs_fp64"] = mixed["value"] / (value / world)
-        forms["mixed"] = mixed
-        del msim, ref, sim, sim2
+        del sim, sim2
         torch.cuda.empty_cache()
+        # The mixed form on the FP64 workload, then on the 8192^2 Sod tube.
+        for workload, size in (("sedov", n), ("sod", args.sod_size)):
+            if size <= 0:
+                continue
+            mixed, msim = run_mixed_form(fg, problems, torch, device, size, args.steps,
+                                         args.warmup, workload=workload)
+            # Error against the FP64 path after the same number of steps from
+            # the same initial state (the FP64 path itself matches the CPU
+            # oracle to ~1e-13 per cell).
+            prob_ref = problems.sedov(size) if workload == "sedov" else problems.sod(size)
+            ref = fg.DeviceSim(prob_ref, device)
+            ref.initial_timestep()
+            t0 = torch.cuda.Event(enable_timing=True)
+            t1 = torch.cuda.Event(enable_timing=True)
+            t0.record()
+            ref.run(args.steps + args.warmup)
+            t1.record()
+            torch.cuda.synchronize()
+            fp64_value = size * size * (args.steps + args.warmup) / (t0.elapsed_time(t1) * 1e-3)
+            mixed["errors_vs_fp64"] = field_errors(fg, msim, ref,
+                                                   names=("rho", "e", "rho_u", "rho_v"))
+            cm, cr = msim.conservation(), ref.conservation()
+            mixed["mass_drift"] = abs(cm[0] - cr[0]) / cr[0]
+            mixed["energy_drift"] = abs(cm[1] - cr[1]) / cr[1]
+            mixed["fp64_value_same_workload"] = fp64_value
+            mixed["speedup_vs_fp64"] = mixed["value"] / fp64_value
+            forms["mixed" if workload == "sedov" else f"mixed_sod_{size}"] = mixed
+            del msim, ref
+            torch.cuda.empty_cache()
         bsteps = min(args.steps, args.batch_steps)
         forms["batched_fp64"] = run_batched_form(fg, problems, torch, device, "two_region", 0,
                                                  bsteps, args.warmup)

@@ -379,7 +379,13 @@ __device__ __forceinline__ void tile_lag_energy_dt(const StepArgs<R>& a, int bx,
       const unsigned long long mx = (unsigned long long)dbits(Pr::to_d(dtx));
       const unsigned long long my = (unsigned long long)dbits(Pr::to_d(dty));
       const unsigned long long m = (mx < my) ? mx : my;
-      best = (m < best) ? m : best;
+      // The reference squares c_s = sqrt(gamma (gamma-1) e), so a cell whose
+      // energy went negative gives a NaN candidate whatever Q is, and its dt
+      // is then the minimum over the other cells (the 4096^2 known-answer
+      // problem does this on its first step, which runs at Courant ~0.9).
+      // Skip such cells rather than use gamma (gamma-1) e + 2Q/rho directly.
+      const bool e_neg = Pr::kMixed ? (e_nr < R(0)) : d_lt0(e_new);
+      best = (!e_neg && m < best) ? m : best;
       v0 = v1;
     }
   }

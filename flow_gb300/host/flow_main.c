@@ -4,7 +4,10 @@
  * over the GPU arch layer (libflow_gb300_arch.so) and the kernel set
  * (libflow_gb300.so).
  *
- *   flow.gb300 <params file> [--quiet]
+ *   flow.gb300 <params file> [--quiet] [--exact]
+ *
+ * --exact selects the stage-by-stage step (GB300_MODE_EXACT) instead of the
+ * fused one.
  *
  * Reads nx, ny, iterations, dt, visit_dump and problem_N boxes from the params
  * file, and width/height/max_dt/sim_end from ../arch.params (defaults 1, 1,
@@ -92,10 +95,19 @@ static int validate(const int nx, const int ny, const int pad,
 
 int main(int argc, char** argv) {
   if (argc < 2) {
-    TERMINATE("usage: ./flow.gb300 <parameter_filename> [--quiet]\n");
+    TERMINATE("usage: ./flow.gb300 <parameter_filename> [--quiet] [--exact]\n");
   }
   const char* params = argv[1];
-  const int quiet = argc > 2 && strcmp(argv[2], "--quiet") == 0;
+  int quiet = 0;
+  for (int k = 2; k < argc; ++k) {
+    if (strcmp(argv[k], "--quiet") == 0) {
+      quiet = 1;
+    } else if (strcmp(argv[k], "--exact") == 0) {
+      gb300_set_mode(GB300_MODE_EXACT);
+    } else {
+      TERMINATE("unknown option %s\n", argv[k]);
+    }
+  }
   gb300_set_verbose(!quiet);
 
   Mesh mesh;

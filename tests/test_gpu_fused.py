@@ -103,6 +103,33 @@ def test_fused_blast_128_200_steps(fg):
     compare(sim, st)
 
 
+def test_fused_known_answer_4096_per_cell(fg):
+    """The reference's own known-answer case (flow.params: 4096^2, params dt
+    1e-3, 100 iterations, flow.tests:1) per cell against the oracle.  Its
+    first step runs at Courant ~0.9 and drives 3276 cells to negative energy
+    inside the step (NaN CFL candidates in the reference).  Density and energy
+    within 1e-12; velocities and momenta within 1e-11, which is 2.5x the
+    reference's own strict-vs-default-build difference on this case
+    (4.0e-12 in rho_u)."""
+    from flow_gb300.problems import Problem
+    prob = Problem(4096, 4096, dt_param=1e-3).boxes(O.flow_params_boxes())
+    sim = fg.DeviceSim(prob)
+    sim.initial_timestep()
+    hm = O.HostMesh(4096, 4096, dt=1e-3)
+    st = O.HostState(hm)
+    O.fill_boxes(hm, st, O.flow_params_boxes())
+    O.initial_timestep(hm, st)
+    for tt in range(100):
+        sim.step()
+        O.step(hm, st, tt)
+        assert abs(sim.mesh.dt - hm.mesh.dt) <= FP64_TOL * hm.mesh.dt, tt
+    errs = {k: cell_rel_err(sim.interior(k), st.interior(k)) for k in STATE}
+    for k, v in errs.items():
+        assert v <= (FP64_TOL if k in ("rho", "e") else 1e-11), errs
+    e_total = sim.interior("e").sum()
+    assert abs(e_total - 3.389026275051e+07) <= 1e-11 * 3.389026275051e+07
+
+
 def test_fused_and_exact_modes_agree(fg):
     from flow_gb300 import problems
     prob = problems.sod(200, 136)
