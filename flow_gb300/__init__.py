@@ -103,6 +103,7 @@ def _declare(L: ctypes.CDLL) -> None:
         "gb300_synchronize": [],
         "gb300_solve_hydro_2d": [M, I] + [P] * 17,
         "gb300_conservation": [I, I, I, P, P, P, P, I],
+        "gb300_conservation_noalloc": [I, I, I, P, P, P],
         "gb300_profile_enable": [I],
         "gb300_profile_reset": [],
         "gb300_profile_count": [],

@@ -32,7 +32,8 @@ UNIT_FLAGS = {
     "stages.cu": ["--fmad=false"],
 }
 
-SOURCES = ["stages.cu", "interface.cu", "fused.cu", "batched.cu", "profile.cu", "peaks.cu"]
+SOURCES = ["stages.cu", "interface.cu", "fused.cu", "batched.cu", "profile.cu", "peaks.cu",
+           "noalloc.cu"]
 
 
 def _nvcc() -> str:

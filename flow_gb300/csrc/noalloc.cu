@@ -1,0 +1,174 @@
+// noalloc.cu -- gb300_conservation_noalloc: the conservation totals of
+// print_conservation (omp3/flow.c:973-995) without a caller-supplied
+// reduce_array and without allocating any device memory.
+//
+// The reduction's scratch is one file-scope __device__ array of fixed size
+// (kNoAllocMaxRows row partials, 256 KiB).  Each interior row is summed by one
+// warp into its own pair of partials; the last block to finish (ticket in the
+// scratch header) adds the row partials in row order with a fixed 256-thread
+// pattern.  The result does not depend on the grid, so repeated calls on the
+// same state return identical totals; it differs from gb300_conservation only
+// by the order of the additions.
+#include <mutex>
+
+#include "../../include/flow_gb300.h"
+#include "fused.h"
+
+namespace flow {
+namespace {
+
+constexpr int kNoAllocMaxRows = GB300_NOALLOC_MAX_ROWS;
+constexpr int kNoAllocThreads = 256;
+constexpr int kNoAllocMaxDevices = 64;
+
+// Header (in doubles): [0] ticket (u64), [1] mass total, [2] energy total;
+// the row partials start at kRowBase, two per row.
+constexpr int kTicket = 0;
+constexpr int kMass = 1;
+constexpr int kEnergy = 2;
+constexpr int kRowBase = 32;  // keeps the partials 256-byte aligned
+constexpr int kScratchDoubles = kRowBase + 2 * kNoAllocMaxRows;
+
+static __device__ __align__(256) double g_noalloc_scratch[kScratchDoubles];
+
+__device__ __forceinline__ double lane_sum(double x) {
+  for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+  return x;
+}
+
+__global__ void __launch_bounds__(kNoAllocThreads)
+    k_conservation_rows(int nx, int ny, int pad, const double* __restrict__ rho,
+                        const double* __restrict__ e, double* scratch) {
+  const int rows = ny - 2 * pad;
+  const int lane = threadIdx.x & 31;
+  const int warps = gridDim.x * (kNoAllocThreads / 32);
+  for (int r = blockIdx.x * (kNoAllocThreads / 32) + (threadIdx.x >> 5); r < rows;
+       r += warps) {
+    const size_t row = (size_t)(pad + r) * nx;
+    double ms = 0.0, es = 0.0;
+    for (int jj = pad + lane; jj < nx - pad; jj += 32) {
+      const double d = rho[row + jj];
+      ms += d;
+      es += d * e[row + jj];
+    }
+    ms = lane_sum(ms);
+    es = lane_sum(es);
+    if (lane == 0) {
+      scratch[kRowBase + 2 * r] = ms;
+      scratch[kRowBase + 2 * r + 1] = es;
+    }
+  }
+  __shared__ bool s_last;
+  __shared__ double s_m[kNoAllocThreads / 32], s_e[kNoAllocThreads / 32];
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long* ticket = reinterpret_cast<unsigned long long*>(scratch + kTicket);
+    s_last = atomicAdd(ticket, 1ull) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  double a = 0.0, b = 0.0;
+  for (int r = threadIdx.x; r < rows; r += kNoAllocThreads) {
+    a += __ldcg(scratch + kRowBase + 2 * r);
+    b += __ldcg(scratch + kRowBase + 2 * r + 1);
+  }
+  a = lane_sum(a);
+  b = lane_sum(b);
+  if (lane == 0) {
+    s_m[threadIdx.x >> 5] = a;
+    s_e[threadIdx.x >> 5] = b;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double ta = 0.0, tb = 0.0;
+    for (int k = 0; k < kNoAllocThreads / 32; ++k) {
+      ta += s_m[k];
+      tb += s_e[k];
+    }
+    scratch[kMass] = ta;
+    scratch[kEnergy] = tb;
+    // Leave the ticket at zero for the next call.
+    *reinterpret_cast<unsigned long long*>(scratch + kTicket) = 0ull;
+  }
+}
+
+std::mutex g_symbol_lock;
+double* g_symbol_addr[kNoAllocMaxDevices] = {};
+
+// Device address of the scratch on the current device, looked up once per
+// device with cudaGetSymbolAddress.
+int scratch_address(double** out) {
+  int dev = -1;
+  cudaError_t err = cudaGetDevice(&dev);
+  if (err != cudaSuccess) {
+    return record_error(GB300_ERR_CUDA, "conservation_noalloc: cudaGetDevice: %s",
+                        cudaGetErrorString(err));
+  }
+  if (dev < 0 || dev >= kNoAllocMaxDevices) {
+    return record_error(GB300_ERR_ARG, "conservation_noalloc: device %d out of range", dev);
+  }
+  std::lock_guard<std::mutex> guard(g_symbol_lock);
+  if (!g_symbol_addr[dev]) {
+    void* p = nullptr;
+    err = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (err != cudaSuccess || !p) {
+      return record_error(GB300_ERR_CUDA,
+                          "conservation_noalloc: cudaGetSymbolAddress on device %d: %s", dev,
+                          cudaGetErrorString(err));
+    }
+    g_symbol_addr[dev] = static_cast<double*>(p);
+  }
+  *out = g_symbol_addr[dev];
+  return GB300_OK;
+}
+
+}  // namespace
+}  // namespace flow
+
+using namespace flow;
+
+extern "C" int gb300_conservation_noalloc(int nx, int ny, int pad, const double* rho,
+                                          const double* e, double* out) {
+  if (!rho || !e || !out) {
+    return record_error(GB300_ERR_ARG, "conservation_noalloc: rho, e and out must be non-NULL");
+  }
+  if (pad < 0 || nx - 2 * pad < 1 || ny - 2 * pad < 1) {
+    return record_error(GB300_ERR_ARG,
+                        "conservation_noalloc: need >= 1 interior cell per axis "
+                        "(nx=%d ny=%d pad=%d)", nx, ny, pad);
+  }
+  const int rows = ny - 2 * pad;
+  if (rows > kNoAllocMaxRows) {
+    return record_error(GB300_ERR_ARG,
+                        "conservation_noalloc: %d interior rows exceed the static scratch "
+                        "limit of %d rows; use gb300_conservation with a reduce_array",
+                        rows, kNoAllocMaxRows);
+  }
+  double* scratch = nullptr;
+  const int st = scratch_address(&scratch);
+  if (st != GB300_OK) return st;
+  cudaStream_t s = current_stream();
+  // The ticket must be zero when the kernel starts.  Static device memory
+  // starts zeroed and every completed call leaves it at zero; clearing it
+  // here also covers a call whose launch failed part way.
+  cudaError_t err = cudaMemsetAsync(scratch + kTicket, 0, sizeof(double), s);
+  if (err != cudaSuccess) {
+    return record_error(GB300_ERR_CUDA, "conservation_noalloc: %s", cudaGetErrorString(err));
+  }
+  int blocks = (rows + kNoAllocThreads / 32 - 1) / (kNoAllocThreads / 32);
+  if (blocks > 8 * 152) blocks = 8 * 152;
+  k_conservation_rows<<<blocks, kNoAllocThreads, 0, s>>>(nx, ny, pad, rho, e, scratch);
+  const int lst = check_launch("conservation_noalloc");
+  if (lst != GB300_OK) return lst;
+  double tot[2];
+  err = cudaMemcpyAsync(tot, scratch + kMass, sizeof(tot), cudaMemcpyDeviceToHost, s);
+  if (err == cudaSuccess) err = cudaStreamSynchronize(s);
+  if (err != cudaSuccess) {
+    return record_error(GB300_ERR_CUDA, "conservation_noalloc: %s", cudaGetErrorString(err));
+  }
+  out[0] = tot[0];
+  out[1] = tot[1];
+  return GB300_OK;
+}

@@ -182,6 +182,32 @@ int gb300_conservation(int nx, int ny, int pad, const double* rho,
                        const double* e, double* reduce_array, double* out,
                        int sync);
 
+/* No counterpart in the reference.  The same interior totals as
+ * gb300_conservation (out[0] = sum rho, out[1] = sum rho*e, host array,
+ * synchronous on the current stream), for callers that hold only the density
+ * and energy arrays and must not allocate device memory: a monitoring or
+ * validation hook between timesteps (cudaMalloc/cudaFree would synchronise
+ * the whole device and stall other streams' work), or a run whose ensemble
+ * fills HBM.  It allocates nothing: its scratch is a fixed 256 KiB
+ * __device__ array inside libflow_gb300.so, holding one pair of partial sums
+ * per interior row, so meshes with more than GB300_NOALLOC_MAX_ROWS interior
+ * rows are rejected with GB300_ERR_ARG.
+ *   - The first call on each device looks up the scratch address with
+ *     cudaGetSymbolAddress (with that device current); make that first call
+ *     before any stream capture begins.
+ *   - The scratch's ticket counter must be zero when the kernel starts: it is
+ *     zero at load, every call clears it on the stream before launching, and
+ *     the kernel leaves it at zero.
+ *   - All calls on one device share the scratch: two calls in flight at once
+ *     (different streams or host threads) race and return wrong totals.
+ *     Serialise them, or use gb300_conservation with separate reduce_arrays.
+ * The additions run in a fixed order (row sums, then rows in order), so the
+ * totals can differ from gb300_conservation's in the last bits, and repeated
+ * calls on the same state return identical totals. */
+#define GB300_NOALLOC_MAX_ROWS 16384
+int gb300_conservation_noalloc(int nx, int ny, int pad, const double* rho,
+                               const double* e, double* out);
+
 /* Per-kernel CUDA-event timing of the fused timestep: enable, run steps,
  * then read one (name, launches, total milliseconds) entry per kernel. */
 int gb300_profile_enable(int on);
