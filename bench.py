@@ -52,6 +52,13 @@ KERNEL_BYTES_PER_CELL = {
     "update_rho_v": 8 * 3,
 }
 
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per interior cell of
+# one launch, from an ncu capture of the FP64 fused kernel on Sedov 2048^2
+# (4.19 M cells, 197.3 MB per launch); scaled to a launch by its cell count.
+NCU_TRAFFIC_BYTES_PER_CELL = {
+    "mass_sweep_y": 197.3e6 / 2048 ** 2,
+}
+
 
 def parse_args():
     p = argparse.ArgumentParser()
@@ -453,13 +460,8 @@ def run_gpu(args):
     cells = (nx - 4) * (ny - 4)
     bytes_launch = KERNEL_BYTES_PER_CELL.get(name, B_ALG_FP64) * cells
     achieved = bytes_launch / (total / nl * 1e-3) / 1e9
-    traffic = None
-    tpath = os.path.join(ROOT, "profiles", "traffic_per_cell.json")
-    if os.path.exists(tpath):
-        with open(tpath) as f:
-            tb = json.load(f).get("fp64", {}).get(name)
-        if tb is not None:
-            traffic = tb * cells
+    tb = NCU_TRAFFIC_BYTES_PER_CELL.get(name)
+    traffic = tb * cells if tb is not None else None
     fma_rate = fg.ctypes.c_double()
     L.gb300_measure_fp64_fma_rate(fg.ctypes.byref(fma_rate))
 
