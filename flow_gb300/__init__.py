@@ -109,6 +109,9 @@ def _declare(L: ctypes.CDLL) -> None:
         "gb300_profile_count": [],
         "gb300_profile_entry": [I, ctypes.c_char_p, I, ctypes.POINTER(ctypes.c_longlong), P],
         "gb300_measure_fp64_fma_rate": [P],
+        "gb300_check_fp64_helpers": [ctypes.c_longlong, ctypes.c_ulonglong,
+                                     ctypes.POINTER(ctypes.c_longlong),
+                                     ctypes.POINTER(ctypes.c_longlong), P],
         "gb300_mixed_prepare": [M, P, P, V, ctypes.c_size_t, P, I],
         "gb300_mixed_solve": [M, I, P, P, V, V, V, ctypes.c_size_t, P],
     }

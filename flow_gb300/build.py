@@ -33,7 +33,7 @@ UNIT_FLAGS = {
 }
 
 SOURCES = ["stages.cu", "interface.cu", "fused.cu", "batched.cu", "profile.cu", "peaks.cu",
-           "noalloc.cu"]
+           "noalloc.cu", "selftest.cu"]
 
 
 def _nvcc() -> str:

@@ -16,8 +16,31 @@
 
 namespace flow {
 
-__device__ __forceinline__ long long dbits(double x) { return __double_as_longlong(x); }
-__device__ __forceinline__ double dfrom(long long b) { return __longlong_as_double(b); }
+// Bit casts written as inline PTX moves, which the compiler cannot see
+// through: with the plain intrinsics it folds integer tests such as
+// "bits << 1 == 0" or "bits & ~sign" back into FP64 compares (DSETP) and
+// absolute values, which occupy the FP64 pipe again.
+__device__ __forceinline__ long long dbits(double x) {
+  long long b;
+  asm("mov.b64 %0, %1;" : "=l"(b) : "d"(x));
+  return b;
+}
+__device__ __forceinline__ double dfrom(long long b) {
+  double x;
+  asm("mov.b64 %0, %1;" : "=d"(x) : "l"(b));
+  return x;
+}
+__device__ __forceinline__ int dhi(double x) { return (int)(dbits(x) >> 32); }
+__device__ __forceinline__ int dlo(double x) { return (int)dbits(x); }
+__device__ __forceinline__ double dfrom2(int hi, int lo) {
+  double x;
+  asm("mov.b64 %0, {%1, %2};" : "=d"(x) : "r"(lo), "r"(hi));
+  return x;
+}
+// -x with an integer instruction.
+__device__ __forceinline__ double d_neg(double x) {
+  return dfrom2(dhi(x) ^ (int)0x80000000, dlo(x));
+}
 
 __device__ __forceinline__ bool d_is_zero(double x) { return (dbits(x) << 1) == 0; }
 // x > 0.0
@@ -52,6 +75,43 @@ __device__ __forceinline__ double d_minmod(double a, double b) {
   return same ? ((ma < mb) ? a : b) : 0.0;
 }
 
+// x * 0.5 and x * 2 on the integer pipes, with the IEEE result for every
+// input (zeros, subnormals, overflow to infinity, infinities and NaNs kept).
+// For a normal x away from the range ends only the exponent field of the
+// high word changes; at the low end the magnitude bits are linear in the
+// value (exponent fields 0 and 1), so halving is a rounded shift.
+__device__ __forceinline__ double d_half(double x) {
+  const int hi = dhi(x);
+  const unsigned ex = (unsigned)hi & 0x7ff00000u;
+  if (ex - 0x00200000u < 0x7ff00000u - 0x00200000u) {
+    return dfrom2(hi - 0x00100000, dlo(x));
+  }
+  const long long b = dbits(x);
+  const long long mag = b & 0x7fffffffffffffffLL;
+  if (mag >= 0x7ff0000000000000LL) return x;
+  const long long h = (mag >> 1) + (mag & (mag >> 1) & 1);  // round half to even
+  return dfrom((b ^ mag) | h);
+}
+__device__ __forceinline__ double d_twice(double x) {
+  const int hi = dhi(x);
+  const unsigned ex = (unsigned)hi & 0x7ff00000u;
+  if (ex - 0x00100000u < 0x7fe00000u - 0x00100000u) {
+    return dfrom2(hi + 0x00100000, dlo(x));
+  }
+  const long long b = dbits(x);
+  const long long mag = b & 0x7fffffffffffffffLL;
+  const long long sign = b ^ mag;
+  if (ex == 0u) return dfrom(sign | (mag << 1));
+  if (ex == 0x7fe00000u) return dfrom(sign | 0x7ff0000000000000LL);
+  return x;
+}
+// True for a positive normal power of two (an exactly invertible spacing).
+__device__ __forceinline__ bool d_is_pow2(double x) {
+  const long long b = dbits(x);
+  const unsigned ex = (unsigned)(b >> 52);  // sign bit lands above the field
+  return (b & 0x000fffffffffffffLL) == 0 && ex - 1u < 0x7feu;
+}
+
 // 1/x for finite normal non-zero x: MUFU seed, two Newton-Raphson steps.
 __device__ __forceinline__ double d_rcp(double x) {
   double r;
@@ -61,12 +121,24 @@ __device__ __forceinline__ double d_rcp(double x) {
   e = fma(-x, r, 1.0);
   return fma(r, e, r);
 }
+// n/d for finite normal non-zero d when 1/d itself is not needed: one Newton
+// step on the MUFU seed (relative error ~2^-20 measured -> ~2^-40), the
+// quotient from it, and one residual correction q + r (n - d q) (-> ~2^-80):
+// the correctly rounded quotient except in vanishingly rare near-ties, as
+// d_rcp followed by qdiv gives, in 5 FP64 instructions instead of 7.
+__device__ __forceinline__ double d_div(double n, double d) {
+  double r;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(d));
+  r = fma(r, fma(-d, r, 1.0), r);
+  const double q = n * r;
+  return fma(r, fma(-d, q, n), q);
+}
 // 1/sqrt(x) for finite normal positive x: MUFU seed, two Newton steps on
 // r <- r + r*(0.5 - 0.5*x*r*r).
 __device__ __forceinline__ double d_rsqrt(double x) {
   double r;
   asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
-  const double h = 0.5 * x;
+  const double h = d_half(x);
   double t = fma(-h * r, r, 0.5);
   r = fma(r, t, r);
   t = fma(-h * r, r, 0.5);

@@ -118,6 +118,36 @@ __device__ __forceinline__ void store_cell(double* a64, R* ar, int nx, int ny,
   }
 }
 
+// True when every mesh spacing (celldx, edgedx, celldy, edgedy) within two
+// entries of the block's columns [col0, col0 + kCols) and rows
+// [row0, row0 + rows) is a power of two -- the uniform power-of-two meshes of
+// the benchmark problems -- so that divisions by those spacings are exact as
+// multiplications by their reciprocals.  Block-uniform (barrier).
+template <typename R>
+__device__ __forceinline__ bool block_mesh_pow2(const StepArgs<R>& a, int col0, int row0) {
+  bool ok = true;
+  for (int j = col0 - 2 + (int)threadIdx.x; j < col0 + kCols + 2; j += kCols) {
+    if (j >= 0 && j <= a.nx) ok = ok && d_is_pow2(a.celldx[j]) && d_is_pow2(a.edgedx[j]);
+  }
+  for (int i = row0 - 2 + (int)threadIdx.x; i < row0 + a.rows + 2; i += kCols) {
+    if (i >= 0 && i <= a.ny) ok = ok && d_is_pow2(a.celldy[i]) && d_is_pow2(a.edgedy[i]);
+  }
+  return __syncthreads_and(ok) != 0;
+}
+
+// Runs tile(kPow2) with kPow2 = true for FP64 tiles whose mesh spacings are
+// all powers of two.
+#define FLOW_POW2_DISPATCH(R, a, col0, row0, CALL_TRUE, CALL_FALSE)          \
+  do {                                                                      \
+    if constexpr (!Prec<R>::kMixed) {                                       \
+      if (block_mesh_pow2(a, col0, row0)) {                                 \
+        CALL_TRUE;                                                          \
+        return;                                                             \
+      }                                                                     \
+    }                                                                       \
+    CALL_FALSE;                                                             \
+  } while (0)
+
 // ===========================================================================
 // Lagrangian phase.
 
@@ -126,8 +156,8 @@ __device__ __forceinline__ void store_cell(double* a64, R* ar, int nx, int ny,
 // the rho_old copy of the reference do) and every interior x/y face.  The
 // reciprocal of each face density is kept in F_x/F_y (free until the
 // advection phase) for the viscous update.  omp3/flow.c:55-70, 110-158.
-template <typename R>
-__device__ __forceinline__ void tile_lag_pressure(const StepArgs<R>& a, int bx, int by) {
+template <typename R, bool kP2>
+__device__ __forceinline__ void tile_lag_pressure_impl(const StepArgs<R>& a, int bx, int by) {
   using Pr = Prec<R>;
   __shared__ R sP[kCols + 1], sR[kCols + 1];
   __shared__ R s_ey[kMaxRows], s_iey[kMaxRows], s_wy0[kMaxRows], s_wy1[kMaxRows];
@@ -190,7 +220,7 @@ __device__ __forceinline__ void tile_lag_pressure(const StepArgs<R>& a, int bx, 
     __syncthreads();
     if (ii >= pad && ii < ny - pad && jj >= pad && jj < nx + 1 - pad) {
       const size_t f = fidx(nx, ii, jj);
-      const R mom = Pr::dsub(a.rho_u[f], dt * (Pc - sP[t]), exr, iex);
+      const R mom = Pr::template dsub<kP2>(a.rho_u[f], dt * (Pc - sP[t]), exr, iex);
       const R rbar = fma(rc, wx0, sR[t] * wx1);
       const bool z = Pr::is_zero(rbar);
       const R inv = z ? R(0) : Pr::rcp(rbar);
@@ -203,7 +233,7 @@ __device__ __forceinline__ void tile_lag_pressure(const StepArgs<R>& a, int bx, 
     }
     if (ii >= pad && ii < ny + 1 - pad && jj >= pad && jj < nx - pad) {
       const size_t c = cidx(nx, ii, jj);
-      const R mom = Pr::dsub(a.rho_v[c], dt * (Pc - P_dn), s_ey[k], s_iey[k]);
+      const R mom = Pr::template dsub<kP2>(a.rho_v[c], dt * (Pc - P_dn), s_ey[k], s_iey[k]);
       const R rbar = fma(rc, s_wy0[k], r_dn * s_wy1[k]);
       const bool z = Pr::is_zero(rbar);
       const R inv = z ? R(0) : Pr::rcp(rbar);
@@ -220,6 +250,12 @@ __device__ __forceinline__ void tile_lag_pressure(const StepArgs<R>& a, int bx, 
   }
 }
 
+template <typename R>
+__device__ __forceinline__ void tile_lag_pressure(const StepArgs<R>& a, int bx, int by) {
+  FLOW_POW2_DISPATCH(R, a, bx * kCols, by * a.rows, (tile_lag_pressure_impl<R, true>(a, bx, by)),
+                     (tile_lag_pressure_impl<R, false>(a, bx, by)));
+}
+
 // Artificial viscous stresses on interior cells, omp3/flow.c:173-207.
 template <typename R>
 __device__ __forceinline__ R visc_stress(R crho, R lo, R mid, R hi, R hi2) {
@@ -227,7 +263,7 @@ __device__ __forceinline__ R visc_stress(R crho, R lo, R mid, R hi, R hi2) {
   const R m0 = Pr::min0(mid - lo);
   const R m1 = Pr::min0(hi - mid);
   const R m2 = Pr::min0(hi2 - hi);
-  return crho * m1 * (R(0.5) * (Pr::abs(m2 - m1) + Pr::abs(m1 - m0)));
+  return crho * m1 * Pr::half(Pr::abs(m2 - m1) + Pr::abs(m1 - m0));
 }
 
 template <typename R>
@@ -259,8 +295,8 @@ __device__ __forceinline__ void tile_lag_viscosity(const StepArgs<R>& a, int bx,
 
 // Viscous acceleration of the face momenta and velocities,
 // omp3/flow.c:212-244.  The face-density reciprocals come from F_x/F_y.
-template <typename R>
-__device__ __forceinline__ void tile_lag_viscous_accel(const StepArgs<R>& a, int bx, int by) {
+template <typename R, bool kP2>
+__device__ __forceinline__ void tile_lag_viscous_accel_impl(const StepArgs<R>& a, int bx, int by) {
   using Pr = Prec<R>;
   __shared__ R s_cy[kMaxRows], s_icy[kMaxRows];
   const int nx = a.nx, ny = a.ny, pad = a.pad;
@@ -285,7 +321,7 @@ __device__ __forceinline__ void tile_lag_viscous_accel(const StepArgs<R>& a, int
     if (ii < ny - pad) {
       const size_t f = fidx(nx, ii, jj);
       const size_t c = cidx(nx, ii, jj);
-      const R mom = Pr::dsub(a.rho_u[f], dt * (a.Qxx[c] - a.Qxx[c - 1]), cx, icx);
+      const R mom = Pr::template dsub<kP2>(a.rho_u[f], dt * (a.Qxx[c] - a.Qxx[c - 1]), cx, icx);
       const R inv = a.F_x[f];
       const R vel = Pr::is_zero(inv) ? R(0) : Pr::qdiv(mom, a.uF_x[f], inv);
       a.rho_u[f] = mom;
@@ -295,7 +331,7 @@ __device__ __forceinline__ void tile_lag_viscous_accel(const StepArgs<R>& a, int
     if (jj < nx - pad) {
       const size_t c = cidx(nx, ii, jj);
       const R qy = a.Qyy[c];
-      const R mom = Pr::dsub(a.rho_v[c], dt * (qy - qy_dn), s_cy[k], s_icy[k]);
+      const R mom = Pr::template dsub<kP2>(a.rho_v[c], dt * (qy - qy_dn), s_cy[k], s_icy[k]);
       const R inv = a.F_y[c];
       const R vel = Pr::is_zero(inv) ? R(0) : Pr::qdiv(mom, a.vF_y[c], inv);
       a.rho_v[c] = mom;
@@ -304,6 +340,13 @@ __device__ __forceinline__ void tile_lag_viscous_accel(const StepArgs<R>& a, int
       qy_dn = qy;
     }
   }
+}
+
+template <typename R>
+__device__ __forceinline__ void tile_lag_viscous_accel(const StepArgs<R>& a, int bx, int by) {
+  FLOW_POW2_DISPATCH(R, a, a.pad + bx * kCols, a.pad + by * a.rows,
+                     (tile_lag_viscous_accel_impl<R, true>(a, bx, by)),
+                     (tile_lag_viscous_accel_impl<R, false>(a, bx, by)));
 }
 
 __device__ __forceinline__ unsigned long long warp_min_u64(unsigned long long x) {
@@ -362,7 +405,7 @@ __device__ __forceinline__ void tile_lag_energy_dt(const StepArgs<R>& a, int bx,
       const R e_q = er + dq;
       const R rho_c = r * Pr::rcp(R(1) + div_dt);
       const R e_c = fma(-(p * div_dt), inv_r, e_q);
-      const R work = (R(0.5) * div_dt) * fma(R(kG1) * e_c, rho_c, p) * inv_r;
+      const R work = Pr::half(div_dt) * fma(R(kG1) * e_c, rho_c, p) * inv_r;
       double e_new;
       if (Pr::kMixed) {
         e_new = rz ? 0.0 : a.e[c] + Pr::to_d(dq - work);
@@ -373,7 +416,7 @@ __device__ __forceinline__ void tile_lag_energy_dt(const StepArgs<R>& a, int bx,
       // CFL: celldx / sqrt(c_s^2 + 2 Q / rho) with c_s^2 = gamma (gamma-1) e.
       const R e_nr = Pr::from_d(e_new);
       const R s2 = R(kGam * (kGam - 1.0)) * e_nr;
-      const R two_inv_r = inv_r + inv_r;
+      const R two_inv_r = Pr::twice(inv_r);
       const R dtx = cx * Pr::rsqrt(fma(qx, two_inv_r, s2));
       const R dty = s_cy[k] * Pr::rsqrt(fma(qy, two_inv_r, s2));
       const unsigned long long mx = (unsigned long long)dbits(Pr::to_d(dtx));
@@ -414,16 +457,28 @@ __device__ __forceinline__ void finish_dt(const StepArgs<R>& a) {
 // ===========================================================================
 // Advection of mass and energy (omp3/flow.c:293-554).
 
-// Second-order upwind interpolation with the MC-limited slope, for the branch
-// already chosen by the wind sign: pos selects the left reconstruction
-// base + 0.5*m*(h - w*dt_h), otherwise base - 0.5*m*(h + w*dt_h).
+// Second-order upwind interpolation with the MC-limited slope from the four
+// values straddling the point (m2, m1 | p0, p1), for the branch chosen by
+// the wind sign: pos reconstructs from the left, base m1 + 0.5*m*(h - w*dt_h)
+// with differences (p0-m2, m1-m2, p0-m1); otherwise from the right, base
+// p0 - 0.5*m*(h + w*dt_h) with (p1-m1, p0-m1, p1-p0).  The operands are
+// selected before subtracting, so each difference is one FP64 instruction.
+// The slope minmod(0.5 da/h', 2 db/h', 2 dc/h') is formed as
+// minmod(0.5 da, 2 db, 2 dc) times inv_h = 1/h' > 0: scaling by a positive
+// factor keeps the selection (rounding is monotonic, and arguments that round
+// to a tie give the same value), so the result is the same number with one
+// multiplication instead of three; halving, doubling and negation are exact
+// integer operations.
 template <typename R>
-__device__ __forceinline__ R mc_face(bool pos, R da, R db, R dc, R half_inv,
-                                     R two_inv, R base, R h, R wdt) {
+__device__ __forceinline__ R mc_face(bool pos, R m2, R m1, R p0, R p1, R inv_h, R h, R wdt) {
   using Pr = Prec<R>;
-  const R mm = Pr::minmod(Pr::minmod(half_inv * da, two_inv * db), two_inv * dc);
-  const R w = h + (pos ? -wdt : wdt);
-  const R hm = pos ? R(0.5) * mm : R(-0.5) * mm;
+  const R a0 = pos ? p0 : p1;
+  const R a1 = pos ? m2 : m1;
+  const R base = pos ? m1 : p0;
+  const R mm = inv_h * Pr::minmod(Pr::minmod(Pr::half(a0 - a1), Pr::twice(base - a1)),
+                                  Pr::twice(a0 - base));
+  const R w = h + (pos ? Pr::neg(wdt) : wdt);
+  const R hm = Pr::half(pos ? mm : Pr::neg(mm));
   return Pr::madd(hm, w, base);
 }
 
@@ -441,29 +496,27 @@ __device__ __forceinline__ void mass_energy_flux(R vm, R v0, R vp, R rm2,
                                                  R dt, R dt_h, R* F_out,
                                                  R* eF_out) {
   using Pr = Prec<R>;
-  const R half_inv = R(0.5) * inv_h, two_inv = R(2) * inv_h;
-  const R mm = Pr::minmod(half_inv * (vp - vm),
-                          Pr::minmod(two_inv * (v0 - vm), two_inv * (vp - v0)));
-  const R w_tc = Pr::msub(v0, R(0.5) * v0 * dt, mm);
+  // minmod(0.5 (vp-vm)/h, 2 (v0-vm)/h, 2 (vp-v0)/h), scaled once (mc_face).
+  const R mm = inv_h * Pr::minmod(Pr::half(vp - vm),
+                                  Pr::minmod(Pr::twice(v0 - vm), Pr::twice(vp - v0)));
+  const R w_tc = Pr::msub(v0, Pr::half(v0) * dt, mm);
   const R jump = r0 - rm1;
   R lim = R(0);
   if (!Pr::is_zero(jump)) {
     const bool up = kSideV0 ? Pr::ge0(v0) : Pr::ge0(w_tc);
-    const R num = up ? (rm1 - rm2) : (rp1 - r0);
+    const R num = (up ? rm1 : rp1) - (up ? rm2 : r0);
     // Van Leer: (s+|s|)/(1+|s|) with s = num/jump, i.e. 2 num/(jump+num)
     // when num and jump share a sign, else 0.
     if (Pr::same_sign_nz(num, jump)) {
-      lim = (num + num) * Pr::rcp(jump + num);
+      lim = Pr::twice(num) * Pr::rcp(jump + num);
     }
   }
   const R rho_up = Pr::ge0(w_tc) ? rm1 : r0;
   const R wdt = w_tc * dt_h;
   const R flux = Pr::madd(w_tc, rho_up,
-                          (R(0.5) * Pr::abs(w_tc)) * (R(1) - Pr::abs(wdt * icd)) * lim * jump);
+                          Pr::half(Pr::abs(w_tc)) * (R(1) - Pr::abs(wdt * icd)) * lim * jump);
   const bool pos = Pr::gt0(w_tc);
-  const R e_face = mc_face(pos, pos ? e0 - em2 : ep1 - em1, pos ? em1 - em2 : e0 - em1,
-                           pos ? e0 - em1 : ep1 - e0, half_inv, two_inv,
-                           pos ? em1 : e0, pos ? h_m : h_p, wdt);
+  const R e_face = mc_face(pos, em2, em1, e0, ep1, inv_h, pos ? h_m : h_p, wdt);
   *F_out = flux;
   *eF_out = area * e_face * flux;
 }
@@ -473,7 +526,7 @@ __device__ __forceinline__ void mass_energy_flux(R vm, R v0, R vp, R rm2,
 // reciprocal, a0/a1 the face lengths.  den is rho_old in the first sweep of a step and the new
 // density in the second (omp3/flow.c:416-432).  The FP64 form keeps the
 // reference's evaluation order; the mixed form contracts into FMAs.
-template <typename R, bool kFirst>
+template <typename R, bool kFirst, bool kP2>
 __device__ __forceinline__ void mass_energy_update(double r_in, double e_in,
                                                    double r_old, double dt_h,
                                                    double vol, double ivol, double a0,
@@ -490,8 +543,8 @@ __device__ __forceinline__ void mass_energy_update(double r_in, double e_in,
     rho_e = fma(-coef, de, r_old * e_in);
   } else {
     const double net = __dadd_rn(__dmul_rn(a1, f1), -__dmul_rn(a0, f0));
-    r_new = Prec<double>::dsub(r_in, __dmul_rn(dt_h, net), vol, ivol);
-    rho_e = Prec<double>::dsub(__dmul_rn(r_old, e_in), __dmul_rn(dt_h, de), vol, ivol);
+    r_new = Prec<double>::dsub<kP2>(r_in, __dmul_rn(dt_h, net), vol, ivol);
+    rho_e = Prec<double>::dsub<kP2>(__dmul_rn(r_old, e_in), __dmul_rn(dt_h, de), vol, ivol);
   }
   const double den = kFirst ? r_old : r_new;
   *r_out = r_new;
@@ -503,7 +556,7 @@ __device__ __forceinline__ void mass_energy_update(double r_in, double e_in,
     const double q = rho_e * r0;
     *e_out = fma(r0, fma(-den, q, rho_e), q);
   } else {
-    *e_out = Prec<double>::qdiv(rho_e, den, d_rcp(den));
+    *e_out = Prec<double>::div(rho_e, den);
   }
 }
 
@@ -523,9 +576,9 @@ struct SweepArgs {
 // face is shared with the next CTA and written only by its owner).  In the
 // second sweep of a step the old density of a cell is read from rho just
 // before the same thread overwrites that cell.
-template <typename R, bool kFirst>
-__device__ __forceinline__ void tile_mass_sweep_x(const StepArgs<R>& a,
-                                                        const SweepArgs<R>& s, int bx, int by) {
+template <typename R, bool kFirst, bool kP2>
+__device__ __forceinline__ void tile_mass_sweep_x_impl(const StepArgs<R>& a,
+                                                       const SweepArgs<R>& s, int bx, int by) {
   __shared__ R sF[kCols], seF[kCols];
   __shared__ double s_coef[kMaxRows], s_cyd[kMaxRows], s_ey0[kMaxRows], s_ey1[kMaxRows];
   const int nx = a.nx, ny = a.ny, pad = a.pad;
@@ -580,8 +633,8 @@ __device__ __forceinline__ void tile_mass_sweep_x(const StepArgs<R>& a,
       const size_t c = cidx(nx, ii, jj);
       const double r_old = kFirst ? s.r_in[c] : a.rho[c];
       double r_new, e_new;
-      mass_energy_update<R, kFirst>(s.r_in[c], s.e_in[c], r_old, dt_h,
-                                    a.celldx[jj] * s_cyd[k], s_coef[k] * icx,
+      mass_energy_update<R, kFirst, kP2>(s.r_in[c], s.e_in[c], r_old, dt_h,
+                                         a.celldx[jj] * s_cyd[k], s_coef[k] * icx,
                                     s_ey0[k], s_ey1[k], sF[t],
                                     sF[t + 1], seF[t], seF[t + 1], &r_new, &e_new);
       store_cell(s.r_out, s.r_out_r, nx, ny, pad, ii, jj, r_new);
@@ -591,11 +644,19 @@ __device__ __forceinline__ void tile_mass_sweep_x(const StepArgs<R>& a,
   }
 }
 
+template <typename R, bool kFirst>
+__device__ __forceinline__ void tile_mass_sweep_x(const StepArgs<R>& a, const SweepArgs<R>& s,
+                                                  int bx, int by) {
+  FLOW_POW2_DISPATCH(R, a, a.pad + bx * (kCols - 1), a.pad + by * a.rows,
+                     (tile_mass_sweep_x_impl<R, kFirst, true>(a, s, bx, by)),
+                     (tile_mass_sweep_x_impl<R, kFirst, false>(a, s, bx, by)));
+}
+
 // y sweep: each thread marches down its column; face row ii+1 is computed
 // in iteration ii and reused by the cell below.
-template <typename R, bool kFirst>
-__device__ __forceinline__ void tile_mass_sweep_y(const StepArgs<R>& a,
-                                                        const SweepArgs<R>& s, int bx, int by) {
+template <typename R, bool kFirst, bool kP2>
+__device__ __forceinline__ void tile_mass_sweep_y_impl(const StepArgs<R>& a,
+                                                       const SweepArgs<R>& s, int bx, int by) {
   __shared__ R s_iey[kMaxRows + 1], s_cy[kMaxRows + 2], s_icy[kMaxRows + 1];
   __shared__ double s_coef[kMaxRows], s_cyd[kMaxRows];
   const int nx = a.nx, ny = a.ny, pad = a.pad;
@@ -667,14 +728,22 @@ __device__ __forceinline__ void tile_mass_sweep_y(const StepArgs<R>& a,
     const size_t c = cidx(nx, ii, jj);
     const double r_old = kFirst ? s.r_in[c] : a.rho[c];
     double r_new, e_new;
-    mass_energy_update<R, kFirst>(s.r_in[c], s.e_in[c], r_old, dt_h,
-                                  a.celldx[jj] * s_cyd[k], s_coef[k] * icx, ex0, ex1,
-                                  F0, F1, eF0, eF1, &r_new, &e_new);
+    mass_energy_update<R, kFirst, kP2>(s.r_in[c], s.e_in[c], r_old, dt_h,
+                                       a.celldx[jj] * s_cyd[k], s_coef[k] * icx, ex0, ex1,
+                                       F0, F1, eF0, eF1, &r_new, &e_new);
     store_cell(s.r_out, s.r_out_r, nx, ny, pad, ii, jj, r_new);
     store_cell(s.e_out, s.e_out_r, nx, ny, pad, ii, jj, e_new);
     F0 = F1;
     eF0 = eF1;
   }
+}
+
+template <typename R, bool kFirst>
+__device__ __forceinline__ void tile_mass_sweep_y(const StepArgs<R>& a, const SweepArgs<R>& s,
+                                                  int bx, int by) {
+  FLOW_POW2_DISPATCH(R, a, a.pad + bx * kCols, a.pad + by * a.rows,
+                     (tile_mass_sweep_y_impl<R, kFirst, true>(a, s, bx, by)),
+                     (tile_mass_sweep_y_impl<R, kFirst, false>(a, s, bx, by)));
 }
 
 // ===========================================================================
@@ -687,9 +756,7 @@ __device__ __forceinline__ R momentum_upwind(R wind, R m2, R m1, R p0, R p1,
                                              R inv_h, R d_left, R d_right,
                                              R dt_h) {
   const bool pos = Prec<R>::gt0(wind);
-  return mc_face(pos, pos ? p0 - m2 : p1 - m1, pos ? m1 - m2 : p0 - m1,
-                 pos ? p0 - m1 : p1 - p0, R(0.5) * inv_h, R(2) * inv_h,
-                 pos ? m1 : p0, pos ? d_left : d_right, wind * dt_h);
+  return mc_face(pos, m2, m1, p0, p1, inv_h, pos ? d_left : d_right, wind * dt_h);
 }
 
 // uF_x on interior cells (omp3/flow.c:778-823).
@@ -712,7 +779,7 @@ __device__ __forceinline__ void tile_flux_uFx(const StepArgs<R>& a, int bx, int 
     const size_t f = fidx(nx, ii, jj);
     const R u0 = a.u[f], u1 = a.u[f + 1];
     const R mass = s_hey[ii - i0] * (a.F_x[f] + a.F_x[f + 1]);
-    const R wind = R(0.5) * (u0 + u1);
+    const R wind = Prec<R>::half(u0 + u1);
     const R val = mass * momentum_upwind(wind, a.u[f - 1], u0, u1, a.u[f + 2], iex,
                                          cxl, cxr, dt_h);
     a.uF_x[cidx(nx, ii, jj)] = val;
@@ -735,7 +802,7 @@ __device__ __forceinline__ void tile_flux_uFy(const StepArgs<R>& a, int bx, int 
   __syncthreads();
   if (jj >= nx + 1 - pad) return;
   const R dt_h = R(a.dt_slot[1]);
-  const R ex = R(a.edgedx[jj]);
+  const R hex = Prec<R>::half(R(a.edgedx[jj]));  // edgedx * 0.5
   const int i1 = min(i0 + a.rows, ny + 1 - pad);
   R um2 = a.u[fidx(nx, i0 - 2, jj)];
   R um1 = a.u[fidx(nx, i0 - 1, jj)];
@@ -744,8 +811,8 @@ __device__ __forceinline__ void tile_flux_uFy(const StepArgs<R>& a, int bx, int 
     const int k = ii - i0;
     const R up = a.u[fidx(nx, ii + 1, jj)];
     const size_t c = cidx(nx, ii, jj);
-    const R mass = ex * R(0.5) * (a.F_y[c] + a.F_y[c - 1]);
-    const R wind = R(0.5) * (a.v[c - 1] + a.v[c]);
+    const R mass = hex * (a.F_y[c] + a.F_y[c - 1]);
+    const R wind = Prec<R>::half(a.v[c - 1] + a.v[c]);
     const R val = mass * momentum_upwind(wind, um2, um1, u0, up, s_iey[k], s_cy[k],
                                          s_cy[k + 1], dt_h);
     a.uF_y[fidx(nx, ii, jj)] = val;
@@ -778,7 +845,7 @@ __device__ __forceinline__ void tile_flux_vFx(const StepArgs<R>& a, int bx, int 
     const size_t c = cidx(nx, ii, jj);
     const R u0 = a.u[f], F0 = a.F_x[f];
     const R mass = s_hcy[ii - i0] * (F0 + F_dn);
-    const R wind = R(0.5) * (u0 + u_dn);
+    const R wind = Prec<R>::half(u0 + u_dn);
     const R val = mass * momentum_upwind(wind, a.v[c - 2], a.v[c - 1], a.v[c],
                                          a.v[c + 1], iex, cxl, cxr, dt_h);
     a.vF_x[f] = val;
@@ -803,7 +870,7 @@ __device__ __forceinline__ void tile_flux_vFy(const StepArgs<R>& a, int bx, int 
   __syncthreads();
   if (jj >= nx - pad) return;
   const R dt_h = R(a.dt_slot[1]);
-  const R cx = R(a.celldx[jj]);
+  const R hcx = Prec<R>::half(R(a.celldx[jj]));  // celldx * 0.5
   const int i1 = min(i0 + a.rows, ny - pad);
   R vm = a.v[cidx(nx, i0 - 1, jj)];
   R v0 = a.v[cidx(nx, i0, jj)];
@@ -813,8 +880,8 @@ __device__ __forceinline__ void tile_flux_vFy(const StepArgs<R>& a, int bx, int 
     const int k = ii - i0;
     const R vp2 = a.v[cidx(nx, ii + 2, jj)];
     const R F1 = a.F_y[cidx(nx, ii + 1, jj)];
-    const R mass = cx * R(0.5) * (F0 + F1);
-    const R wind = R(0.5) * (v0 + vp);
+    const R mass = hcx * (F0 + F1);
+    const R wind = Prec<R>::half(v0 + vp);
     const R val = mass * momentum_upwind(wind, vm, v0, vp, vp2, s_iey[k], s_cy[k],
                                          s_cy[k + 1], dt_h);
     a.vF_y[cidx(nx, ii, jj)] = val;
@@ -829,8 +896,8 @@ __device__ __forceinline__ void tile_flux_vFy(const StepArgs<R>& a, int bx, int 
 // Momentum updates (omp3/flow.c:577-668, 683-771).  kWhich: 0 rho_u by uF_x,
 // 1 rho_u by uF_y, 2 rho_v by vF_x, 3 rho_v by vF_y; kVel recomputes the
 // velocity from the post-advection density.
-template <typename R, int kWhich, bool kVel>
-__device__ __forceinline__ void tile_momentum_update(const StepArgs<R>& a, int bx, int by) {
+template <typename R, int kWhich, bool kVel, bool kP2>
+__device__ __forceinline__ void tile_momentum_update_impl(const StepArgs<R>& a, int bx, int by) {
   using Pr = Prec<R>;
   constexpr bool kU = kWhich < 2;
   __shared__ R s_h[kMaxRows], s_row[kMaxRows], s_wy0[kMaxRows], s_wy1[kMaxRows];
@@ -880,13 +947,13 @@ __device__ __forceinline__ void tile_momentum_update(const StepArgs<R>& a, int b
     R* mom = kU ? a.rho_u + f : a.rho_v + c;
     // mom - dt_h * diff / (hx * hy), the divisor rounded as the reference
     // forms it (omp3/flow.c:581-584).
-    const R m = Pr::dsub(*mom, dt_h_r * diff, hx_r * s_h[k], s_row[k] * ihx);
+    const R m = Pr::template dsub<kP2>(*mom, dt_h_r * diff, hx_r * s_h[k], s_row[k] * ihx);
     *mom = m;
     if (kVel) {
       R rbar;
       if (kU) rbar = fma(a.rho_r[c], wx0, a.rho_r[c - 1] * wx1);
       else rbar = fma(a.rho_r[c], s_wy0[k], a.rho_r[c - nx] * s_wy1[k]);
-      const R vel = Pr::is_zero(rbar) ? R(0) : Pr::qdiv(m, rbar, Pr::rcp(rbar));
+      const R vel = Pr::is_zero(rbar) ? R(0) : Pr::div(m, rbar);
       if (kU) {
         a.u[f] = vel;
         mirror(a.u, nx + 1, ny, pad, ii, jj, vel, true, false);
@@ -898,6 +965,12 @@ __device__ __forceinline__ void tile_momentum_update(const StepArgs<R>& a, int b
   }
 }
 
+template <typename R, int kWhich, bool kVel>
+__device__ __forceinline__ void tile_momentum_update(const StepArgs<R>& a, int bx, int by) {
+  FLOW_POW2_DISPATCH(R, a, a.pad + bx * kCols, a.pad + by * a.rows,
+                     (tile_momentum_update_impl<R, kWhich, kVel, true>(a, bx, by)),
+                     (tile_momentum_update_impl<R, kWhich, kVel, false>(a, bx, by)));
+}
 
 }  // namespace tiles
 }  // namespace flow

@@ -52,11 +52,20 @@ struct Prec<double> {
     const double q = n * inv;
     return fma(inv, fma(-d, q, n), q);
   }
+  // n / d when the reciprocal is not needed otherwise.
+  __device__ static __forceinline__ double div(double n, double d) { return d_div(n, d); }
   // m - t/d with the quotient rounded before the difference, as the
   // reference evaluates a momentum or mass update by a mesh spacing d.
+  // kPow2: d is a power of two, so t*inv is already the exact quotient and
+  // the correction (always zero then) is skipped.
+  template <bool kPow2 = false>
   __device__ static __forceinline__ double dsub(double m, double t, double d, double inv) {
-    return __dadd_rn(m, -qdiv(t, d, inv));
+    return __dadd_rn(m, -(kPow2 ? __dmul_rn(t, inv) : qdiv(t, d, inv)));
   }
+  // x * 0.5 and x * 2, exact, on the integer pipes.
+  __device__ static __forceinline__ double half(double x) { return d_half(x); }
+  __device__ static __forceinline__ double neg(double x) { return d_neg(x); }
+  __device__ static __forceinline__ double twice(double x) { return d_twice(x); }
 };
 
 __device__ __forceinline__ double f32_to_f64(float f) {
@@ -111,9 +120,14 @@ struct Prec<float> {
   __device__ static __forceinline__ float msub(float m, float t, float s) { return fmaf(-t, s, m); }
   __device__ static __forceinline__ float madd(float h, float w, float b) { return fmaf(h, w, b); }
   __device__ static __forceinline__ float qdiv(float n, float, float inv) { return n * inv; }
+  __device__ static __forceinline__ float div(float n, float d) { return n * rcp(d); }
+  template <bool kPow2 = false>
   __device__ static __forceinline__ float dsub(float m, float t, float, float inv) {
     return fmaf(-t, inv, m);
   }
+  __device__ static __forceinline__ float half(float x) { return 0.5f * x; }
+  __device__ static __forceinline__ float neg(float x) { return -x; }
+  __device__ static __forceinline__ float twice(float x) { return x + x; }
 };
 
 }  // namespace flow

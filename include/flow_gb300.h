@@ -286,6 +286,18 @@ void gb300_batch_destroy(GB300Batch* batch);
  * small scratch buffer; not for use inside stream capture. */
 int gb300_measure_fp64_fma_rate(double* fma_per_s);
 
+/* Self-check of the FP64 helpers the fused kernels use in place of IEEE
+ * operations, on n hashed inputs (synchronous; allocates a small buffer):
+ *   counts[0]  x*0.5 on the integer pipes != IEEE x*0.5 (every bit pattern)
+ *   counts[1]  x*2 on the integer pipes != IEEE x*2
+ *   counts[2]  power-of-two test wrong
+ *   counts[3]  one-Newton-step quotient with one correction != IEEE n/d
+ *   counts[4]  Newton reciprocal + one correction quotient != IEEE n/d
+ * max_ulp[0..1]: the largest gaps of counts[3..4] in units in the last
+ * place; max_seed_rel_err: the largest |rcp.approx(d) * d - 1|. */
+int gb300_check_fp64_helpers(long long n, unsigned long long seed, long long* counts,
+                             long long* max_ulp, double* max_seed_rel_err);
+
 #ifdef __cplusplus
 }
 #endif
