@@ -367,6 +367,7 @@ template <typename R>
 __device__ __forceinline__ void tile_lag_energy_dt(const StepArgs<R>& a, int bx, int by) {
   using Pr = Prec<R>;
   __shared__ R s_icy[kMaxRows], s_cy[kMaxRows];
+  __shared__ double s_icy2[kMaxRows];
   __shared__ unsigned long long s_warp[kCols / 32];
   const int nx = a.nx, ny = a.ny, pad = a.pad;
   const int jj = pad + bx * kCols + threadIdx.x;
@@ -376,13 +377,18 @@ __device__ __forceinline__ void tile_lag_energy_dt(const StepArgs<R>& a, int bx,
     if (ii < ny) {
       s_cy[threadIdx.x] = R(a.celldy[ii]);
       s_icy[threadIdx.x] = R(1.0 / a.celldy[ii]);
+      s_icy2[threadIdx.x] = 1.0 / (a.celldy[ii] * a.celldy[ii]);
     }
   }
   __syncthreads();
   unsigned long long best = ~0ull;
+  // FP64 form: the thread's largest 1/dt^2 key so far, with its S and spacing.
+  long long kbest = -1;
+  double s_best = 0.0, c_best = 0.0;
   if (jj < nx - pad) {
     const R cx = R(a.celldx[jj]);
     const R icx = R(1.0 / a.celldx[jj]);
+    const double icx2 = 1.0 / (a.celldx[jj] * a.celldx[jj]);
     const R dt_h = R(a.dt_h);
     const int i1 = min(i0 + a.rows, ny - pad);
     R v0 = a.v[cidx(nx, i0, jj)];
@@ -414,24 +420,45 @@ __device__ __forceinline__ void tile_lag_energy_dt(const StepArgs<R>& a, int bx,
       }
       store_cell(a.e, a.e_r, nx, ny, pad, ii, jj, e_new);
       // CFL: celldx / sqrt(c_s^2 + 2 Q / rho) with c_s^2 = gamma (gamma-1) e.
-      const R e_nr = Pr::from_d(e_new);
-      const R s2 = R(kGam * (kGam - 1.0)) * e_nr;
-      const R two_inv_r = Pr::twice(inv_r);
-      const R dtx = cx * Pr::rsqrt(fma(qx, two_inv_r, s2));
-      const R dty = s_cy[k] * Pr::rsqrt(fma(qy, two_inv_r, s2));
-      const unsigned long long mx = (unsigned long long)dbits(Pr::to_d(dtx));
-      const unsigned long long my = (unsigned long long)dbits(Pr::to_d(dty));
-      const unsigned long long m = (mx < my) ? mx : my;
       // The reference squares c_s = sqrt(gamma (gamma-1) e), so a cell whose
       // energy went negative gives a NaN candidate whatever Q is, and its dt
       // is then the minimum over the other cells (the 4096^2 known-answer
       // problem does this on its first step, which runs at Courant ~0.9).
       // Skip such cells rather than use gamma (gamma-1) e + 2Q/rho directly.
+      const R e_nr = Pr::from_d(e_new);
+      const R s2 = R(kGam * (kGam - 1.0)) * e_nr;
+      const R two_inv_r = Pr::twice(inv_r);
+      const R sx = fma(qx, two_inv_r, s2);
+      const R sy = fma(qy, two_inv_r, s2);
       const bool e_neg = Pr::kMixed ? (e_nr < R(0)) : d_lt0(e_new);
-      best = (!e_neg && m < best) ? m : best;
+      if constexpr (Pr::kMixed) {
+        const unsigned long long mx = (unsigned long long)dbits(Pr::to_d(cx * Pr::rsqrt(sx)));
+        const unsigned long long my =
+            (unsigned long long)dbits(Pr::to_d(s_cy[k] * Pr::rsqrt(sy)));
+        const unsigned long long m = (mx < my) ? mx : my;
+        best = (!e_neg && m < best) ? m : best;
+      } else {
+        // Rank the candidates by the key S / h^2 = 1/dt^2 (the largest key
+        // is the smallest dt) and take the square root only for the
+        // thread's winner after the loop.  Keys in [+0, +inf] only: a
+        // negative or NaN S is a NaN candidate in the reference.
+        const long long kx = e_neg ? -1 : dbits(sx * icx2);
+        const long long ky = e_neg ? -1 : dbits(sy * s_icy2[k]);
+        if (kx >= 0 && kx <= 0x7ff0000000000000LL && kx > kbest) {
+          kbest = kx;
+          s_best = sx;
+          c_best = cx;
+        }
+        if (ky >= 0 && ky <= 0x7ff0000000000000LL && ky > kbest) {
+          kbest = ky;
+          s_best = sy;
+          c_best = s_cy[k];
+        }
+      }
       v0 = v1;
     }
   }
+  if (!Pr::kMixed && kbest >= 0) best = (unsigned long long)dbits(c_best * d_rsqrt(s_best));
   best = warp_min_u64(best);
   if ((threadIdx.x & 31) == 0) s_warp[threadIdx.x >> 5] = best;
   __syncthreads();
