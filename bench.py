@@ -53,10 +53,12 @@ KERNEL_BYTES_PER_CELL = {
 }
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per interior cell of
-# one launch, from an ncu capture of the FP64 fused kernel on Sedov 2048^2
-# (4.19 M cells, 197.3 MB per launch); scaled to a launch by its cell count.
+# one launch, from an ncu capture of the FP64 fused kernels on Sedov 2048^2
+# (4.19 M cells); scaled to a launch by its cell count.
 NCU_TRAFFIC_BYTES_PER_CELL = {
-    "mass_sweep_y": 197.3e6 / 2048 ** 2,
+    "mass_sweep_y": (108.8e6 + 58.4e6) / 2048 ** 2,
+    "lag_energy_dt": (236.7e6 + 23.0e6) / 2048 ** 2,
+    "flux_uFy": (102.1e6 + 13.3e6) / 2048 ** 2,
 }
 
 
