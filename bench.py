@@ -282,13 +282,43 @@ def run_batched_form(fg, problems, torch, device, kind, precision, steps, warmup
         del ref
     del b
     torch.cuda.empty_cache()
+    seq = run_sequential_ensemble(fg, torch, device, probs, precision, warmup=1, steps=2)
     b_alg = B_ALG_FP64 if precision == 0 else B_ALG_MIXED
     return {"workload": f"batch_{kind}_{'fp64' if precision == 0 else 'mixed'}",
             "instances": len(probs), "cells": cells, "value": value, "unit": UNIT,
             "ms_per_step": ms / steps, "steps_timed": steps, "steps_total": total_steps,
             "graph": True, "tuning": tune,
             "hbm_fraction_of_step": value * b_alg / (measured_peaks()[0] * 1e9),
-            "errors_vs_fp64_single_problem": errs}
+            "errors_vs_fp64_single_problem": errs,
+            "sequential_same_ensemble": seq,
+            "speedup_vs_sequential": value / seq["value"]}
+
+
+def run_sequential_ensemble(fg, torch, device, probs, precision, warmup, steps):
+    """The same ensemble advanced one problem at a time through the
+    single-problem path of the same precision (solve_hydro_2d per instance, or
+    gb300_mixed_solve), each instance its own arrays: what a caller without
+    the batched form would run."""
+    sims = [(fg.DeviceSim if precision == 0 else fg.MixedSim)(p, device) for p in probs]
+    if precision == 0:
+        for s in sims:
+            s.initial_timestep()
+    for _ in range(warmup):
+        for s in sims:
+            s.step()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        for s in sims:
+            s.step()
+    torch.cuda.synchronize()
+    el = time.perf_counter() - t0
+    cells = sum(p.gnx * p.gny for p in probs)
+    del sims
+    torch.cuda.empty_cache()
+    return {"value": cells * steps / el, "unit": UNIT, "steps_timed": steps,
+            "ms_per_step": el * 1e3 / steps,
+            "what": "per-instance single-problem steps, host-timed (each step reads dt back)"}
 
 
 def run_mixed_form(fg, problems, torch, device, n, steps, warmup, ref_state=None, workload="sedov"):
@@ -438,7 +468,7 @@ def run_gpu(args):
             torch.cuda.synchronize()
             fp64_value = size * size * (args.steps + args.warmup) / (t0.elapsed_time(t1) * 1e-3)
             mixed["errors_vs_fp64"] = field_errors(fg, msim, ref,
-                                                   names=("rho", "e", "rho_u", "rho_v"))
+                                                   names=("rho", "e", "u", "v", "rho_u", "rho_v"))
             cm, cr = msim.conservation(), ref.conservation()
             mixed["mass_drift"] = abs(cm[0] - cr[0]) / cr[0]
             mixed["energy_drift"] = abs(cm[1] - cr[1]) / cr[1]

@@ -123,6 +123,8 @@ def _declare(L: ctypes.CDLL) -> None:
     L.gb300_get_stream.argtypes, L.gb300_get_stream.restype = [], ctypes.c_void_p
     L.gb300_mixed_workspace_bytes.argtypes = [I, I]
     L.gb300_mixed_workspace_bytes.restype = ctypes.c_size_t
+    L.gb300_mixed_workspace_offset.argtypes = [I, I, I]
+    L.gb300_mixed_workspace_offset.restype = ctypes.c_size_t
     IP = ctypes.POINTER(ctypes.c_int)
     batch = {
         "gb300_batch_create": [I, IP, IP, P, P, I, ctypes.POINTER(V)],

@@ -286,6 +286,13 @@ size_t mixed_workspace_bytes(int nx, int ny) { return mixed_layout(nx, ny).total
 
 size_t mixed_zero_block_offset(int nx, int ny) { return mixed_layout(nx, ny).s_r; }
 
+size_t mixed_workspace_offset(int nx, int ny, int field) {
+  const MixedLayout L = mixed_layout(nx, ny);
+  if (field == GB300_MIXED_U) return L.u;
+  if (field == GB300_MIXED_V) return L.v;
+  return (size_t)-1;
+}
+
 int mixed_prepare(Mesh* mesh, double* rho, double* e, void* work, size_t bytes) {
   const int nx = mesh->local_nx, ny = mesh->local_ny;
   const MixedLayout L = mixed_layout(nx, ny);

@@ -28,6 +28,8 @@ size_t mixed_workspace_bytes(int nx, int ny);
 // Byte offset of a cell-sized FP64 block of the workspace that is zero after
 // mixed_prepare (the first-sweep density, written only during a step).
 size_t mixed_zero_block_offset(int nx, int ny);
+// Byte offset of the FP32 velocity u (GB300_MIXED_U) or v (GB300_MIXED_V).
+size_t mixed_workspace_offset(int nx, int ny, int field);
 int mixed_prepare(Mesh* mesh, double* rho, double* e, void* work, size_t bytes);
 int mixed_solve(Mesh* mesh, int tt, double* rho, double* e, float* rho_u,
                 float* rho_v, void* work, size_t bytes, double* reduce_array);

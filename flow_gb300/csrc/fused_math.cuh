@@ -105,6 +105,22 @@ __device__ __forceinline__ double d_twice(double x) {
   if (ex == 0x7fe00000u) return dfrom(sign | 0x7ff0000000000000LL);
   return x;
 }
+// x * p for p a positive normal power of two (an exact reciprocal of a
+// power-of-two mesh spacing): an add to the exponent field when x and the
+// result are normal, x itself for a zero; the rare rest (subnormal input or
+// result, overflow, infinity, NaN) takes the FP64 multiply in a called
+// function, so the common path issues no FP64 instruction.
+static __device__ __noinline__ double d_mul_slow(double x, double p) { return __dmul_rn(x, p); }
+__device__ __forceinline__ double d_mul_pow2(double x, double p) {
+  const int hx = dhi(x);
+  const int k = ((dhi(p) >> 20) & 0x7ff) - 1023;
+  const int ex = (hx >> 20) & 0x7ff;
+  if ((unsigned)(ex - 1) < 2046u && (unsigned)(ex + k - 1) < 2046u) {
+    return dfrom2((int)((unsigned)hx + ((unsigned)k << 20)), dlo(x));
+  }
+  if ((dbits(x) << 1) == 0) return x;
+  return d_mul_slow(x, p);
+}
 // True for a positive normal power of two (an exactly invertible spacing).
 __device__ __forceinline__ bool d_is_pow2(double x) {
   const long long b = dbits(x);

@@ -363,8 +363,8 @@ __device__ __forceinline__ unsigned long long warp_min_u64(unsigned long long x)
 // block on the FP64 bit pattern of its smallest candidate; the last block to
 // finish applies the leapfrog dt/dt_h rule (finish_dt).  In the mixed form
 // the FP32 energy change is added to the FP64 energy.
-template <typename R>
-__device__ __forceinline__ void tile_lag_energy_dt(const StepArgs<R>& a, int bx, int by) {
+template <typename R, bool kP2>
+__device__ __forceinline__ void tile_lag_energy_dt_impl(const StepArgs<R>& a, int bx, int by) {
   using Pr = Prec<R>;
   __shared__ R s_icy[kMaxRows], s_cy[kMaxRows];
   __shared__ double s_icy2[kMaxRows];
@@ -403,8 +403,8 @@ __device__ __forceinline__ void tile_lag_energy_dt(const StepArgs<R>& a, int bx,
       const R qx = a.Qxx[c], qy = a.Qyy[c];
       const bool rz = Pr::is_zero(r);
       const R inv_r = rz ? R(0) : Pr::rcp(r);
-      const R dudx = (a.u[f + 1] - a.u[f]) * icx;
-      const R dvdy = (v1 - v0) * s_icy[k];
+      const R dudx = Pr::template mulp<kP2>(a.u[f + 1] - a.u[f], icx);
+      const R dvdy = Pr::template mulp<kP2>(v1 - v0, s_icy[k]);
       const R div_dt = (dudx + dvdy) * dt_h;
       // e_q = e - dt_h (Qxx dudx + Qyy dvdy) / rho, kept as an increment.
       const R dq = -(dt_h * fma(qx, dudx, qy * dvdy)) * inv_r;
@@ -442,8 +442,8 @@ __device__ __forceinline__ void tile_lag_energy_dt(const StepArgs<R>& a, int bx,
         // is the smallest dt) and take the square root only for the
         // thread's winner after the loop.  Keys in [+0, +inf] only: a
         // negative or NaN S is a NaN candidate in the reference.
-        const long long kx = e_neg ? -1 : dbits(sx * icx2);
-        const long long ky = e_neg ? -1 : dbits(sy * s_icy2[k]);
+        const long long kx = e_neg ? -1 : dbits(Prec<double>::mulp<kP2>(sx, icx2));
+        const long long ky = e_neg ? -1 : dbits(Prec<double>::mulp<kP2>(sy, s_icy2[k]));
         if (kx >= 0 && kx <= 0x7ff0000000000000LL && kx > kbest) {
           kbest = kx;
           s_best = sx;
@@ -467,6 +467,13 @@ __device__ __forceinline__ void tile_lag_energy_dt(const StepArgs<R>& a, int bx,
     for (int w = 1; w < kCols / 32; ++w) b = (s_warp[w] < b) ? s_warp[w] : b;
     atomicMin(a.min_slot, b);
   }
+}
+
+template <typename R>
+__device__ __forceinline__ void tile_lag_energy_dt(const StepArgs<R>& a, int bx, int by) {
+  FLOW_POW2_DISPATCH(R, a, a.pad + bx * kCols, a.pad + by * a.rows,
+                     (tile_lag_energy_dt_impl<R, true>(a, bx, by)),
+                     (tile_lag_energy_dt_impl<R, false>(a, bx, by)));
 }
 
 // The leapfrog dt/dt_h rule of omp3/flow.c:103-105 applied to the finished
@@ -496,14 +503,15 @@ __device__ __forceinline__ void finish_dt(const StepArgs<R>& a) {
 // to a tie give the same value), so the result is the same number with one
 // multiplication instead of three; halving, doubling and negation are exact
 // integer operations.
-template <typename R>
+template <typename R, bool kP2>
 __device__ __forceinline__ R mc_face(bool pos, R m2, R m1, R p0, R p1, R inv_h, R h, R wdt) {
   using Pr = Prec<R>;
   const R a0 = pos ? p0 : p1;
   const R a1 = pos ? m2 : m1;
   const R base = pos ? m1 : p0;
-  const R mm = inv_h * Pr::minmod(Pr::minmod(Pr::half(a0 - a1), Pr::twice(base - a1)),
-                                  Pr::twice(a0 - base));
+  const R mm = Pr::template mulp<kP2>(
+      Pr::minmod(Pr::minmod(Pr::half(a0 - a1), Pr::twice(base - a1)), Pr::twice(a0 - base)),
+      inv_h);
   const R w = h + (pos ? Pr::neg(wdt) : wdt);
   const R hm = Pr::half(pos ? mm : Pr::neg(mm));
   return Pr::madd(hm, w, base);
@@ -515,7 +523,7 @@ __device__ __forceinline__ R mc_face(bool pos, R m2, R m1, R p0, R p1, R inv_h, 
 // face spacing and icd the reciprocal of the downstream cell width.  kSideV0:
 // take the Van Leer smoothness side from v0 (the y sweep, omp3/flow.c:477)
 // instead of the half-step velocity.
-template <typename R, bool kSideV0>
+template <typename R, bool kSideV0, bool kP2>
 __device__ __forceinline__ void mass_energy_flux(R vm, R v0, R vp, R rm2,
                                                  R rm1, R r0, R rp1, R em2,
                                                  R em1, R e0, R ep1, R inv_h,
@@ -524,8 +532,8 @@ __device__ __forceinline__ void mass_energy_flux(R vm, R v0, R vp, R rm2,
                                                  R* eF_out) {
   using Pr = Prec<R>;
   // minmod(0.5 (vp-vm)/h, 2 (v0-vm)/h, 2 (vp-v0)/h), scaled once (mc_face).
-  const R mm = inv_h * Pr::minmod(Pr::half(vp - vm),
-                                  Pr::minmod(Pr::twice(v0 - vm), Pr::twice(vp - v0)));
+  const R mm = Pr::template mulp<kP2>(
+      Pr::minmod(Pr::half(vp - vm), Pr::minmod(Pr::twice(v0 - vm), Pr::twice(vp - v0))), inv_h);
   const R w_tc = Pr::msub(v0, Pr::half(v0) * dt, mm);
   const R jump = r0 - rm1;
   R lim = R(0);
@@ -541,9 +549,9 @@ __device__ __forceinline__ void mass_energy_flux(R vm, R v0, R vp, R rm2,
   const R rho_up = Pr::ge0(w_tc) ? rm1 : r0;
   const R wdt = w_tc * dt_h;
   const R flux = Pr::madd(w_tc, rho_up,
-                          Pr::half(Pr::abs(w_tc)) * (R(1) - Pr::abs(wdt * icd)) * lim * jump);
+                          Pr::half(Pr::abs(w_tc)) * (R(1) - Pr::abs(Pr::template mulp<kP2>(wdt, icd))) * lim * jump);
   const bool pos = Pr::gt0(w_tc);
-  const R e_face = mc_face(pos, em2, em1, e0, ep1, inv_h, pos ? h_m : h_p, wdt);
+  const R e_face = mc_face<R, kP2>(pos, em2, em1, e0, ep1, inv_h, pos ? h_m : h_p, wdt);
   *F_out = flux;
   *eF_out = area * e_face * flux;
 }
@@ -643,7 +651,7 @@ __device__ __forceinline__ void tile_mass_sweep_x_impl(const StepArgs<R>& a,
     if (face_ok) {
       const size_t f = fidx(nx, ii, jj);
       const size_t c = cidx(nx, ii, jj);
-      mass_energy_flux<R, false>(a.u[f - 1], a.u[f], a.u[f + 1], s.r_in_r[c - 2],
+      mass_energy_flux<R, false, kP2>(a.u[f - 1], a.u[f], a.u[f + 1], s.r_in_r[c - 2],
                                  s.r_in_r[c - 1], s.r_in_r[c], s.r_in_r[c + 1],
                                  s.e_in_r[c - 2], s.e_in_r[c - 1], s.e_in_r[c],
                                  s.e_in_r[c + 1], iex, cxm, cx0, icx_r,
@@ -661,9 +669,10 @@ __device__ __forceinline__ void tile_mass_sweep_x_impl(const StepArgs<R>& a,
       const double r_old = kFirst ? s.r_in[c] : a.rho[c];
       double r_new, e_new;
       mass_energy_update<R, kFirst, kP2>(s.r_in[c], s.e_in[c], r_old, dt_h,
-                                         a.celldx[jj] * s_cyd[k], s_coef[k] * icx,
-                                    s_ey0[k], s_ey1[k], sF[t],
-                                    sF[t + 1], seF[t], seF[t + 1], &r_new, &e_new);
+                                         a.celldx[jj] * s_cyd[k],
+                                         Prec<double>::mulp<kP2>(s_coef[k], icx),
+                                         s_ey0[k], s_ey1[k], sF[t],
+                                         sF[t + 1], seF[t], seF[t + 1], &r_new, &e_new);
       store_cell(s.r_out, s.r_out_r, nx, ny, pad, ii, jj, r_new);
       store_cell(s.e_out, s.e_out_r, nx, ny, pad, ii, jj, e_new);
     }
@@ -722,7 +731,7 @@ __device__ __forceinline__ void tile_mass_sweep_y_impl(const StepArgs<R>& a,
   }
   for (int q = 0; q < 3; ++q) w[q] = a.v[cidx(nx, i0 - 1 + q, jj)];
   R F0, eF0;
-  mass_energy_flux<R, true>(w[0], w[1], w[2], r[0], r[1], r[2], r[3], e[0], e[1],
+  mass_energy_flux<R, true, kP2>(w[0], w[1], w[2], r[0], r[1], r[2], r[3], e[0], e[1],
                             e[2], e[3], s_iey[0], s_cy[0], s_cy[1], s_icy[0],
                             ex0_r, dt_r, dt_h_r, &F0, &eF0);
   {
@@ -743,7 +752,7 @@ __device__ __forceinline__ void tile_mass_sweep_y_impl(const StepArgs<R>& a,
     w[1] = w[2];
     w[2] = a.v[cidx(nx, ii + 2, jj)];
     R F1, eF1;
-    mass_energy_flux<R, true>(w[0], w[1], w[2], r[0], r[1], r[2], r[3], e[0],
+    mass_energy_flux<R, true, kP2>(w[0], w[1], w[2], r[0], r[1], r[2], r[3], e[0],
                               e[1], e[2], e[3], s_iey[k + 1], s_cy[k + 1],
                               s_cy[k + 2], s_icy[k + 1], ex0_r, dt_r, dt_h_r, &F1,
                               &eF1);
@@ -756,7 +765,8 @@ __device__ __forceinline__ void tile_mass_sweep_y_impl(const StepArgs<R>& a,
     const double r_old = kFirst ? s.r_in[c] : a.rho[c];
     double r_new, e_new;
     mass_energy_update<R, kFirst, kP2>(s.r_in[c], s.e_in[c], r_old, dt_h,
-                                       a.celldx[jj] * s_cyd[k], s_coef[k] * icx, ex0, ex1,
+                                       a.celldx[jj] * s_cyd[k],
+                                       Prec<double>::mulp<kP2>(s_coef[k], icx), ex0, ex1,
                                        F0, F1, eF0, eF1, &r_new, &e_new);
     store_cell(s.r_out, s.r_out_r, nx, ny, pad, ii, jj, r_new);
     store_cell(s.e_out, s.e_out_r, nx, ny, pad, ii, jj, e_new);
@@ -778,17 +788,17 @@ __device__ __forceinline__ void tile_mass_sweep_y(const StepArgs<R>& a, const Sw
 
 // MC-limited upwind value of a velocity at a flux point from its four
 // neighbours along the direction (m2, m1 | p0, p1): omp3/flow.c:791-820.
-template <typename R>
+template <typename R, bool kP2>
 __device__ __forceinline__ R momentum_upwind(R wind, R m2, R m1, R p0, R p1,
                                              R inv_h, R d_left, R d_right,
                                              R dt_h) {
   const bool pos = Prec<R>::gt0(wind);
-  return mc_face(pos, m2, m1, p0, p1, inv_h, pos ? d_left : d_right, wind * dt_h);
+  return mc_face<R, kP2>(pos, m2, m1, p0, p1, inv_h, pos ? d_left : d_right, wind * dt_h);
 }
 
 // uF_x on interior cells (omp3/flow.c:778-823).
-template <typename R>
-__device__ __forceinline__ void tile_flux_uFx(const StepArgs<R>& a, int bx, int by) {
+template <typename R, bool kP2>
+__device__ __forceinline__ void tile_flux_uFx_impl(const StepArgs<R>& a, int bx, int by) {
   __shared__ R s_hey[kMaxRows];
   const int nx = a.nx, ny = a.ny, pad = a.pad;
   const int jj = pad + bx * kCols + threadIdx.x;
@@ -807,7 +817,7 @@ __device__ __forceinline__ void tile_flux_uFx(const StepArgs<R>& a, int bx, int 
     const R u0 = a.u[f], u1 = a.u[f + 1];
     const R mass = s_hey[ii - i0] * (a.F_x[f] + a.F_x[f + 1]);
     const R wind = Prec<R>::half(u0 + u1);
-    const R val = mass * momentum_upwind(wind, a.u[f - 1], u0, u1, a.u[f + 2], iex,
+    const R val = mass * momentum_upwind<R, kP2>(wind, a.u[f - 1], u0, u1, a.u[f + 2], iex,
                                          cxl, cxr, dt_h);
     a.uF_x[cidx(nx, ii, jj)] = val;
     mirror(a.uF_x, nx, ny, pad, ii, jj, val, false, false);
@@ -815,8 +825,8 @@ __device__ __forceinline__ void tile_flux_uFx(const StepArgs<R>& a, int bx, int 
 }
 
 // uF_y on corners (omp3/flow.c:826-874).
-template <typename R>
-__device__ __forceinline__ void tile_flux_uFy(const StepArgs<R>& a, int bx, int by) {
+template <typename R, bool kP2>
+__device__ __forceinline__ void tile_flux_uFy_impl(const StepArgs<R>& a, int bx, int by) {
   __shared__ R s_iey[kMaxRows], s_cy[kMaxRows + 1];
   const int nx = a.nx, ny = a.ny, pad = a.pad;
   const int jj = pad + bx * kCols + threadIdx.x;
@@ -840,7 +850,7 @@ __device__ __forceinline__ void tile_flux_uFy(const StepArgs<R>& a, int bx, int 
     const size_t c = cidx(nx, ii, jj);
     const R mass = hex * (a.F_y[c] + a.F_y[c - 1]);
     const R wind = Prec<R>::half(a.v[c - 1] + a.v[c]);
-    const R val = mass * momentum_upwind(wind, um2, um1, u0, up, s_iey[k], s_cy[k],
+    const R val = mass * momentum_upwind<R, kP2>(wind, um2, um1, u0, up, s_iey[k], s_cy[k],
                                          s_cy[k + 1], dt_h);
     a.uF_y[fidx(nx, ii, jj)] = val;
     mirror(a.uF_y, nx + 1, ny + 1, pad, ii, jj, val, false, false);
@@ -851,8 +861,8 @@ __device__ __forceinline__ void tile_flux_uFy(const StepArgs<R>& a, int bx, int 
 }
 
 // vF_x on corners (omp3/flow.c:877-925).
-template <typename R>
-__device__ __forceinline__ void tile_flux_vFx(const StepArgs<R>& a, int bx, int by) {
+template <typename R, bool kP2>
+__device__ __forceinline__ void tile_flux_vFx_impl(const StepArgs<R>& a, int bx, int by) {
   __shared__ R s_hcy[kMaxRows];
   const int nx = a.nx, ny = a.ny, pad = a.pad;
   const int jj = pad + bx * kCols + threadIdx.x;
@@ -873,7 +883,7 @@ __device__ __forceinline__ void tile_flux_vFx(const StepArgs<R>& a, int bx, int 
     const R u0 = a.u[f], F0 = a.F_x[f];
     const R mass = s_hcy[ii - i0] * (F0 + F_dn);
     const R wind = Prec<R>::half(u0 + u_dn);
-    const R val = mass * momentum_upwind(wind, a.v[c - 2], a.v[c - 1], a.v[c],
+    const R val = mass * momentum_upwind<R, kP2>(wind, a.v[c - 2], a.v[c - 1], a.v[c],
                                          a.v[c + 1], iex, cxl, cxr, dt_h);
     a.vF_x[f] = val;
     mirror(a.vF_x, nx + 1, ny + 1, pad, ii, jj, val, false, false);
@@ -883,8 +893,8 @@ __device__ __forceinline__ void tile_flux_vFx(const StepArgs<R>& a, int bx, int 
 }
 
 // vF_y on interior cells (omp3/flow.c:928-970).
-template <typename R>
-__device__ __forceinline__ void tile_flux_vFy(const StepArgs<R>& a, int bx, int by) {
+template <typename R, bool kP2>
+__device__ __forceinline__ void tile_flux_vFy_impl(const StepArgs<R>& a, int bx, int by) {
   __shared__ R s_iey[kMaxRows], s_cy[kMaxRows + 1];
   const int nx = a.nx, ny = a.ny, pad = a.pad;
   const int jj = pad + bx * kCols + threadIdx.x;
@@ -909,7 +919,7 @@ __device__ __forceinline__ void tile_flux_vFy(const StepArgs<R>& a, int bx, int 
     const R F1 = a.F_y[cidx(nx, ii + 1, jj)];
     const R mass = hcx * (F0 + F1);
     const R wind = Prec<R>::half(v0 + vp);
-    const R val = mass * momentum_upwind(wind, vm, v0, vp, vp2, s_iey[k], s_cy[k],
+    const R val = mass * momentum_upwind<R, kP2>(wind, vm, v0, vp, vp2, s_iey[k], s_cy[k],
                                          s_cy[k + 1], dt_h);
     a.vF_y[cidx(nx, ii, jj)] = val;
     mirror(a.vF_y, nx, ny, pad, ii, jj, val, false, false);
@@ -918,6 +928,31 @@ __device__ __forceinline__ void tile_flux_vFy(const StepArgs<R>& a, int bx, int 
     vp = vp2;
     F0 = F1;
   }
+}
+
+template <typename R>
+__device__ __forceinline__ void tile_flux_uFx(const StepArgs<R>& a, int bx, int by) {
+  FLOW_POW2_DISPATCH(R, a, a.pad + bx * kCols, a.pad + by * a.rows,
+                     (tile_flux_uFx_impl<R, true>(a, bx, by)),
+                     (tile_flux_uFx_impl<R, false>(a, bx, by)));
+}
+template <typename R>
+__device__ __forceinline__ void tile_flux_uFy(const StepArgs<R>& a, int bx, int by) {
+  FLOW_POW2_DISPATCH(R, a, a.pad + bx * kCols, a.pad + by * a.rows,
+                     (tile_flux_uFy_impl<R, true>(a, bx, by)),
+                     (tile_flux_uFy_impl<R, false>(a, bx, by)));
+}
+template <typename R>
+__device__ __forceinline__ void tile_flux_vFx(const StepArgs<R>& a, int bx, int by) {
+  FLOW_POW2_DISPATCH(R, a, a.pad + bx * kCols, a.pad + by * a.rows,
+                     (tile_flux_vFx_impl<R, true>(a, bx, by)),
+                     (tile_flux_vFx_impl<R, false>(a, bx, by)));
+}
+template <typename R>
+__device__ __forceinline__ void tile_flux_vFy(const StepArgs<R>& a, int bx, int by) {
+  FLOW_POW2_DISPATCH(R, a, a.pad + bx * kCols, a.pad + by * a.rows,
+                     (tile_flux_vFy_impl<R, true>(a, bx, by)),
+                     (tile_flux_vFy_impl<R, false>(a, bx, by)));
 }
 
 // Momentum updates (omp3/flow.c:577-668, 683-771).  kWhich: 0 rho_u by uF_x,
@@ -974,7 +1009,8 @@ __device__ __forceinline__ void tile_momentum_update_impl(const StepArgs<R>& a, 
     R* mom = kU ? a.rho_u + f : a.rho_v + c;
     // mom - dt_h * diff / (hx * hy), the divisor rounded as the reference
     // forms it (omp3/flow.c:581-584).
-    const R m = Pr::template dsub<kP2>(*mom, dt_h_r * diff, hx_r * s_h[k], s_row[k] * ihx);
+    const R m = Pr::template dsub<kP2>(*mom, dt_h_r * diff, hx_r * s_h[k],
+                                       Pr::template mulp<kP2>(s_row[k], ihx));
     *mom = m;
     if (kVel) {
       R rbar;

@@ -560,6 +560,10 @@ size_t gb300_mixed_workspace_bytes(int local_nx, int local_ny) {
   return mixed_workspace_bytes(local_nx, local_ny);
 }
 
+size_t gb300_mixed_workspace_offset(int local_nx, int local_ny, int field) {
+  return mixed_workspace_offset(local_nx, local_ny, field);
+}
+
 int gb300_mixed_prepare(Mesh* mesh, double* rho, double* e, void* workspace,
                         size_t bytes, double* reduce_array,
                         int initial_timestep) {

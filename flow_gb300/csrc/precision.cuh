@@ -60,7 +60,12 @@ struct Prec<double> {
   // the correction (always zero then) is skipped.
   template <bool kPow2 = false>
   __device__ static __forceinline__ double dsub(double m, double t, double d, double inv) {
-    return __dadd_rn(m, -(kPow2 ? __dmul_rn(t, inv) : qdiv(t, d, inv)));
+    return __dadd_rn(m, -(kPow2 ? d_mul_pow2(t, inv) : qdiv(t, d, inv)));
+  }
+  // x * p; kPow2: p is a power of two and the product an exponent add.
+  template <bool kPow2 = false>
+  __device__ static __forceinline__ double mulp(double x, double p) {
+    return kPow2 ? d_mul_pow2(x, p) : x * p;
   }
   // x * 0.5 and x * 2, exact, on the integer pipes.
   __device__ static __forceinline__ double half(double x) { return d_half(x); }
@@ -125,6 +130,8 @@ struct Prec<float> {
   __device__ static __forceinline__ float dsub(float m, float t, float, float inv) {
     return fmaf(-t, inv, m);
   }
+  template <bool kPow2 = false>
+  __device__ static __forceinline__ float mulp(float x, float p) { return x * p; }
   __device__ static __forceinline__ float half(float x) { return 0.5f * x; }
   __device__ static __forceinline__ float neg(float x) { return -x; }
   __device__ static __forceinline__ float twice(float x) { return x + x; }

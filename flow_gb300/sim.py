@@ -182,6 +182,14 @@ class MixedSim:
 
     def interior(self, name: str) -> np.ndarray:
         nx, ny, p = self.nx, self.ny, PAD
+        if name in ("u", "v"):
+            # FP32 velocities inside the workspace (gb300_mixed_workspace_offset).
+            off = int(lib().gb300_mixed_workspace_offset(nx, ny, 0 if name == "u" else 1))
+            n = (nx + 1) * (ny + 1)
+            a = self.work[off:off + 4 * n].view(self.torch.float32).cpu().numpy().astype(np.float64)
+            if name == "u":
+                return a[: ny * (nx + 1)].reshape(ny, nx + 1)[p:ny - p, p:nx + 1 - p]
+            return a[: (ny + 1) * nx].reshape(ny + 1, nx)[p:ny + 1 - p, p:nx - p]
         a = getattr(self, name).cpu().numpy().astype(np.float64)
         if name == "rho_u":
             return a[: ny * (nx + 1)].reshape(ny, nx + 1)[p:ny - p, p:nx + 1 - p]

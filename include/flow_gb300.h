@@ -228,6 +228,13 @@ int gb300_profile_entry(int i, char* name, int name_len, long long* launches,
  * gb300_mixed_workspace_bytes() bytes (the form never allocates). */
 size_t gb300_mixed_workspace_bytes(int local_nx, int local_ny);
 
+/* Byte offset inside the workspace of the form's FP32 velocities, laid out
+ * like the FP64 ones (x faces (nx+1) per row, y faces nx per row):
+ * field 0 = u, 1 = v; (size_t)-1 for any other field. */
+#define GB300_MIXED_U 0
+#define GB300_MIXED_V 1
+size_t gb300_mixed_workspace_offset(int local_nx, int local_ny, int field);
+
 /* Zeroes the workspace and derives its FP32 copies of rho and e (whose
  * ghosts must already be filled); with initial_timestep = 1 also performs the
  * driver's first set_timestep (first_step = 0, zero viscous stresses). */
@@ -293,6 +300,7 @@ int gb300_measure_fp64_fma_rate(double* fma_per_s);
  *   counts[2]  power-of-two test wrong
  *   counts[3]  one-Newton-step quotient with one correction != IEEE n/d
  *   counts[4]  Newton reciprocal + one correction quotient != IEEE n/d
+ *   counts[5]  x times a power of two on the integer pipes != IEEE product
  * max_ulp[0..1]: the largest gaps of counts[3..4] in units in the last
  * place; max_seed_rel_err: the largest |rcp.approx(d) * d - 1|. */
 int gb300_check_fp64_helpers(long long n, unsigned long long seed, long long* counts,

@@ -37,7 +37,7 @@ def run_pair(fg, prob, steps):
 
 def errors(sim, st):
     out = {}
-    for k in ("rho", "e", "rho_u", "rho_v"):
+    for k in ("rho", "e", "u", "v", "rho_u", "rho_v"):
         out[k] = (l1_rel(sim.interior(k), st.interior(k)), linf_rel(sim.interior(k), st.interior(k)))
     return out
 
@@ -48,7 +48,7 @@ def test_mixed_sod_256_100_steps(fg):
     err = errors(sim, st)
     print("mixed sod256 L1/Linf", err)
     assert err["rho"][0] <= 1e-5 and err["e"][0] <= 1e-5
-    assert err["rho_u"][0] <= 1e-4
+    assert err["rho_u"][0] <= 1e-4 and err["u"][0] <= 1e-4
     m1 = sim.conservation()[0]
     assert abs(m1 - m0) <= 1e-12 * m0
     assert abs(sim.mesh.dt - hm.mesh.dt) <= 1e-4 * hm.mesh.dt
@@ -60,6 +60,7 @@ def test_mixed_blast_128_200_steps(fg):
     err = errors(sim, st)
     print("mixed blast128 L1/Linf", err)
     assert err["rho"][0] <= 1e-5 and err["e"][0] <= 1e-4
+    assert err["u"][0] <= 1e-4 and err["v"][0] <= 1e-4
     assert np.isfinite(sim.interior("e")).all() and sim.interior("e").min() > 0
     assert abs(sim.conservation()[0] - m0) <= 1e-12 * m0
 
