@@ -53,7 +53,7 @@ __global__ void __launch_bounds__(kCols, 8) k_mass_sweep_x(const StepArgs<R> a,
   tile_mass_sweep_x<R, kFirst>(a, s, blockIdx.x, blockIdx.y);
 }
 template <typename R, bool kFirst>
-__global__ void __launch_bounds__(kCols, 8) k_mass_sweep_y(const StepArgs<R> a,
+__global__ void __launch_bounds__(kCols, 7) k_mass_sweep_y(const StepArgs<R> a,
                                                         const SweepArgs<R> s) {
   tile_mass_sweep_y<R, kFirst>(a, s, blockIdx.x, blockIdx.y);
 }

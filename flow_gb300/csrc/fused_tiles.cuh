@@ -148,6 +148,19 @@ __device__ __forceinline__ bool block_mesh_pow2(const StepArgs<R>& a, int col0, 
     CALL_FALSE;                                                             \
   } while (0)
 
+// Volume-weighted face value a*wa + b*wb, rounded once after the product
+// b*wb (the reference's a*wa + b*wb contracted as in the fused kernels).  On
+// power-of-two meshes both weights are powers of two, both products exact
+// exponent adds, and the single rounding is that of the sum.
+template <typename R, bool kP2>
+__device__ __forceinline__ R face_average(R a, R wa, R b, R wb) {
+  if constexpr (kP2 && !Prec<R>::kMixed) {
+    return Prec<R>::template mulp<true>(a, wa) + Prec<R>::template mulp<true>(b, wb);
+  } else {
+    return fma(a, wa, b * wb);
+  }
+}
+
 // ===========================================================================
 // Lagrangian phase.
 
@@ -221,7 +234,7 @@ __device__ __forceinline__ void tile_lag_pressure_impl(const StepArgs<R>& a, int
     if (ii >= pad && ii < ny - pad && jj >= pad && jj < nx + 1 - pad) {
       const size_t f = fidx(nx, ii, jj);
       const R mom = Pr::template dsub<kP2>(a.rho_u[f], dt * (Pc - sP[t]), exr, iex);
-      const R rbar = fma(rc, wx0, sR[t] * wx1);
+      const R rbar = face_average<R, kP2>(rc, wx0, sR[t], wx1);
       const bool z = Pr::is_zero(rbar);
       const R inv = z ? R(0) : Pr::rcp(rbar);
       const R vel = z ? R(0) : Pr::qdiv(mom, rbar, inv);
@@ -234,7 +247,7 @@ __device__ __forceinline__ void tile_lag_pressure_impl(const StepArgs<R>& a, int
     if (ii >= pad && ii < ny + 1 - pad && jj >= pad && jj < nx - pad) {
       const size_t c = cidx(nx, ii, jj);
       const R mom = Pr::template dsub<kP2>(a.rho_v[c], dt * (Pc - P_dn), s_ey[k], s_iey[k]);
-      const R rbar = fma(rc, s_wy0[k], r_dn * s_wy1[k]);
+      const R rbar = face_average<R, kP2>(rc, s_wy0[k], r_dn, s_wy1[k]);
       const bool z = Pr::is_zero(rbar);
       const R inv = z ? R(0) : Pr::rcp(rbar);
       const R vel = z ? R(0) : Pr::qdiv(mom, rbar, inv);
@@ -272,23 +285,32 @@ __device__ __forceinline__ void tile_lag_viscosity(const StepArgs<R>& a, int bx,
   const int jj = pad + bx * kCols + threadIdx.x;
   const int i0 = pad + by * a.rows;
   if (jj >= nx - pad) return;
+  using Pr = Prec<R>;
   const int i1 = min(i0 + a.rows, ny - pad);
-  R vm = a.v[cidx(nx, i0 - 1, jj)];
-  R v0 = a.v[cidx(nx, i0, jj)];
+  // The y stress of row ii uses the limited jumps m0, m1, m2 of v around the
+  // cell and |m1 - m0|, |m2 - m1|; the next row reuses three of those, so
+  // they are carried down the column (same operands, same values).
+  const R vm = a.v[cidx(nx, i0 - 1, jj)];
+  const R v0 = a.v[cidx(nx, i0, jj)];
   R vp = a.v[cidx(nx, i0 + 1, jj)];
+  R m0 = Pr::min0(v0 - vm), m1 = Pr::min0(vp - v0);
+  R g01 = Pr::abs(m1 - m0);
   for (int ii = i0; ii < i1; ++ii) {
     const R vp2 = a.v[cidx(nx, ii + 2, jj)];
     const size_t f = fidx(nx, ii, jj);
     const size_t c = cidx(nx, ii, jj);
     const R crho = R(-kCQ) * a.rho_r[c];
     const R qx = visc_stress(crho, a.u[f - 1], a.u[f], a.u[f + 1], a.u[f + 2]);
-    const R qy = visc_stress(crho, vm, v0, vp, vp2);
+    const R m2 = Pr::min0(vp2 - vp);
+    const R g12 = Pr::abs(m2 - m1);
+    const R qy = crho * m1 * Pr::half(g12 + g01);
     a.Qxx[c] = qx;
     a.Qyy[c] = qy;
     mirror(a.Qxx, nx, ny, pad, ii, jj, qx, false, false);
     mirror(a.Qyy, nx, ny, pad, ii, jj, qy, false, false);
-    vm = v0;
-    v0 = vp;
+    m0 = m1;
+    m1 = m2;
+    g01 = g12;
     vp = vp2;
   }
 }
@@ -494,52 +516,103 @@ __device__ __forceinline__ void finish_dt(const StepArgs<R>& a) {
 // Second-order upwind interpolation with the MC-limited slope from the four
 // values straddling the point (m2, m1 | p0, p1), for the branch chosen by
 // the wind sign: pos reconstructs from the left, base m1 + 0.5*m*(h - w*dt_h)
-// with differences (p0-m2, m1-m2, p0-m1); otherwise from the right, base
-// p0 - 0.5*m*(h + w*dt_h) with (p1-m1, p0-m1, p1-p0).  The operands are
-// selected before subtracting, so each difference is one FP64 instruction.
+// from the differences (da, db, dc) = (p0-m2, m1-m2, p0-m1); otherwise from
+// the right, base p0 - 0.5*m*(h + w*dt_h) from (p1-m1, p0-m1, p1-p0).
 // The slope minmod(0.5 da/h', 2 db/h', 2 dc/h') is formed as
 // minmod(0.5 da, 2 db, 2 dc) times inv_h = 1/h' > 0: scaling by a positive
 // factor keeps the selection (rounding is monotonic, and arguments that round
 // to a tie give the same value), so the result is the same number with one
 // multiplication instead of three; halving, doubling and negation are exact
-// integer operations.
+// integer operations.  A zero slope (flat or extremal data) leaves the base
+// value, and the reconstruction arithmetic is skipped.
 template <typename R, bool kP2>
-__device__ __forceinline__ R mc_face(bool pos, R m2, R m1, R p0, R p1, R inv_h, R h, R wdt) {
+__device__ __forceinline__ R mc_reconstruct(bool pos, R da, R db, R dc, R base, R inv_h, R h,
+                                            R wdt) {
   using Pr = Prec<R>;
-  const R a0 = pos ? p0 : p1;
-  const R a1 = pos ? m2 : m1;
-  const R base = pos ? m1 : p0;
-  const R mm = Pr::template mulp<kP2>(
-      Pr::minmod(Pr::minmod(Pr::half(a0 - a1), Pr::twice(base - a1)), Pr::twice(a0 - base)),
-      inv_h);
+  const R m0 = Pr::minmod(Pr::minmod(Pr::half(da), Pr::twice(db)), Pr::twice(dc));
+  if (Pr::is_zero(m0)) return base;
+  const R mm = Pr::template mulp<kP2>(m0, inv_h);
   const R w = h + (pos ? Pr::neg(wdt) : wdt);
   const R hm = Pr::half(pos ? mm : Pr::neg(mm));
   return Pr::madd(hm, w, base);
 }
 
-// Mass and energy flux through one face.  The four cells straddle the face
-// (m2, m1 | p0, p1), vm/v0/vp are the face velocities around it, h_m/h_p the
-// cell widths on each side, area the face length, inv_h the reciprocal of the
-// face spacing and icd the reciprocal of the downstream cell width.  kSideV0:
-// take the Van Leer smoothness side from v0 (the y sweep, omp3/flow.c:477)
-// instead of the half-step velocity.
-template <typename R, bool kSideV0, bool kP2>
-__device__ __forceinline__ void mass_energy_flux(R vm, R v0, R vp, R rm2,
-                                                 R rm1, R r0, R rp1, R em2,
-                                                 R em1, R e0, R ep1, R inv_h,
-                                                 R h_m, R h_p, R icd, R area,
-                                                 R dt, R dt_h, R* F_out,
-                                                 R* eF_out) {
+// The same from the four values themselves, selecting the operands before
+// subtracting so that each difference is one FP64 instruction.
+template <typename R, bool kP2>
+__device__ __forceinline__ R mc_face(bool pos, R m2, R m1, R p0, R p1, R inv_h, R h, R wdt) {
+  const R a0 = pos ? p0 : p1;
+  const R a1 = pos ? m2 : m1;
+  const R base = pos ? m1 : p0;
+  return mc_reconstruct<R, kP2>(pos, a0 - a1, base - a1, a0 - base, base, inv_h, h, wdt);
+}
+
+// Four consecutive values of a column (m2, m1, p0, p1) with their one-step
+// differences d1 = m1-m2, d2 = p0-m1, d3 = p1-p0 and two-step differences
+// D1 = p0-m2, D2 = p1-m1.  A tile marching down the column shifts the window
+// by one value per row and forms only the two new differences (the others
+// are the same operands as before, so the same values).
+template <typename R>
+struct ColWindow {
+  R m1, p0, p1, d1, d2, d3, D1, D2;
+  __device__ __forceinline__ void init(R m2_, R m1_, R p0_, R p1_) {
+    m1 = m1_; p0 = p0_; p1 = p1_;
+    d1 = m1_ - m2_; d2 = p0_ - m1_; d3 = p1_ - p0_;
+    D1 = p0_ - m2_; D2 = p1_ - m1_;
+  }
+  __device__ __forceinline__ void shift(R next) {
+    const R D2n = next - p0, d3n = next - p1;
+    m1 = p0; p0 = p1; p1 = next;
+    d1 = d2; d2 = d3; d3 = d3n;
+    D1 = D2; D2 = D2n;
+  }
+  // mc_face of the window's face (between m1 and p0).
+  template <bool kP2>
+  __device__ __forceinline__ R face(bool pos, R inv_h, R h, R wdt) const {
+    return mc_reconstruct<R, kP2>(pos, pos ? D1 : D2, pos ? d1 : d2, pos ? d2 : d3,
+                                  pos ? m1 : p0, inv_h, h, wdt);
+  }
+};
+
+// The one-step differences only (d1, d2, d3) of a marching column window.
+template <typename R>
+struct ColSteps {
+  R m1, p0, p1, d1, d2, d3;
+  __device__ __forceinline__ void init(R m2_, R m1_, R p0_, R p1_) {
+    m1 = m1_; p0 = p0_; p1 = p1_;
+    d1 = m1_ - m2_; d2 = p0_ - m1_; d3 = p1_ - p0_;
+  }
+  __device__ __forceinline__ void shift(R next) {
+    const R d3n = next - p1;
+    m1 = p0; p0 = p1; p1 = next;
+    d1 = d2; d2 = d3; d3 = d3n;
+  }
+};
+
+// Mass and energy flux through one face (omp3/flow.c:340-404, 455-517), from
+// the face velocity v0 and the differences of the face velocities around it
+// (dv2 = vp-vm, dvm = v0-vm, dvp = vp-v0), the densities rm1 | r0 either side
+// with jump = r0-rm1, the Van Leer smoothness numerator num_of(up) (upwind
+// side: rm1-rm2, else rp1-r0), and the energy reconstruction e_face_of(pos,
+// w dt_h).  inv_h is the reciprocal of the face spacing, icd of the
+// downstream cell width, area the face length.  kSideV0: take the Van Leer
+// side from v0 (the y sweep, omp3/flow.c:477) instead of the half-step
+// velocity.  A zero limiter (flat or extremal density) leaves the upwind
+// flux, and the second-order term is skipped.
+template <typename R, bool kSideV0, bool kP2, typename NumFn, typename EFaceFn>
+__device__ __forceinline__ void mass_energy_flux_core(R v0, R dv2, R dvm, R dvp, R rm1, R r0,
+                                                      R jump, NumFn num_of, EFaceFn e_face_of,
+                                                      R inv_h, R icd, R area, R dt, R dt_h,
+                                                      R* F_out, R* eF_out) {
   using Pr = Prec<R>;
-  // minmod(0.5 (vp-vm)/h, 2 (v0-vm)/h, 2 (vp-v0)/h), scaled once (mc_face).
+  // minmod(0.5 (vp-vm)/h, 2 (v0-vm)/h, 2 (vp-v0)/h), scaled once (mc_reconstruct).
   const R mm = Pr::template mulp<kP2>(
-      Pr::minmod(Pr::half(vp - vm), Pr::minmod(Pr::twice(v0 - vm), Pr::twice(vp - v0))), inv_h);
+      Pr::minmod(Pr::half(dv2), Pr::minmod(Pr::twice(dvm), Pr::twice(dvp))), inv_h);
   const R w_tc = Pr::msub(v0, Pr::half(v0) * dt, mm);
-  const R jump = r0 - rm1;
   R lim = R(0);
   if (!Pr::is_zero(jump)) {
     const bool up = kSideV0 ? Pr::ge0(v0) : Pr::ge0(w_tc);
-    const R num = (up ? rm1 : rp1) - (up ? rm2 : r0);
+    const R num = num_of(up);
     // Van Leer: (s+|s|)/(1+|s|) with s = num/jump, i.e. 2 num/(jump+num)
     // when num and jump share a sign, else 0.
     if (Pr::same_sign_nz(num, jump)) {
@@ -548,12 +621,36 @@ __device__ __forceinline__ void mass_energy_flux(R vm, R v0, R vp, R rm2,
   }
   const R rho_up = Pr::ge0(w_tc) ? rm1 : r0;
   const R wdt = w_tc * dt_h;
-  const R flux = Pr::madd(w_tc, rho_up,
-                          Pr::half(Pr::abs(w_tc)) * (R(1) - Pr::abs(Pr::template mulp<kP2>(wdt, icd))) * lim * jump);
-  const bool pos = Pr::gt0(w_tc);
-  const R e_face = mc_face<R, kP2>(pos, em2, em1, e0, ep1, inv_h, pos ? h_m : h_p, wdt);
+  R flux;
+  if (Pr::is_zero(lim)) {
+    flux = w_tc * rho_up;
+  } else {
+    flux = Pr::madd(w_tc, rho_up,
+                    Pr::half(Pr::abs(w_tc)) *
+                        (R(1) - Pr::abs(Pr::template mulp<kP2>(wdt, icd))) * lim * jump);
+  }
+  const R e_face = e_face_of(Pr::gt0(w_tc), wdt);
   *F_out = flux;
-  *eF_out = area * e_face * flux;
+  *eF_out = Pr::template mulp<kP2>(e_face, area) * flux;
+}
+
+// The flux from the four cells straddling the face (m2, m1 | p0, p1) and
+// the face velocities vm, v0, vp (the x sweep); h_m/h_p are the cell widths
+// either side.
+template <typename R, bool kSideV0, bool kP2>
+__device__ __forceinline__ void mass_energy_flux(R vm, R v0, R vp, R rm2,
+                                                 R rm1, R r0, R rp1, R em2,
+                                                 R em1, R e0, R ep1, R inv_h,
+                                                 R h_m, R h_p, R icd, R area,
+                                                 R dt, R dt_h, R* F_out,
+                                                 R* eF_out) {
+  mass_energy_flux_core<R, kSideV0, kP2>(
+      v0, vp - vm, v0 - vm, vp - v0, rm1, r0, r0 - rm1,
+      [&](bool up) { return (up ? rm1 : rp1) - (up ? rm2 : r0); },
+      [&](bool pos, R wdt) {
+        return mc_face<R, kP2>(pos, em2, em1, e0, ep1, inv_h, pos ? h_m : h_p, wdt);
+      },
+      inv_h, icd, area, dt, dt_h, F_out, eF_out);
 }
 
 // Conservative FP64 update of one cell from its two face fluxes (given in
@@ -577,7 +674,7 @@ __device__ __forceinline__ void mass_energy_update(double r_in, double e_in,
     r_new = fma(-coef, fma(a1, f1, -(a0 * f0)), r_in);
     rho_e = fma(-coef, de, r_old * e_in);
   } else {
-    const double net = __dadd_rn(__dmul_rn(a1, f1), -__dmul_rn(a0, f0));
+    const double net = __dadd_rn(Prec<double>::mulp<kP2>(f1, a1), -Prec<double>::mulp<kP2>(f0, a0));
     r_new = Prec<double>::dsub<kP2>(r_in, __dmul_rn(dt_h, net), vol, ivol);
     rho_e = Prec<double>::dsub<kP2>(__dmul_rn(r_old, e_in), __dmul_rn(dt_h, de), vol, ivol);
   }
@@ -722,18 +819,37 @@ __device__ __forceinline__ void tile_mass_sweep_y_impl(const StepArgs<R>& a,
   const R ex0_r = R(ex0), dt_r = R(dt), dt_h_r = R(dt_h);
   const int i1 = min(i0 + a.rows, ny - pad);
   const int last_face = ny - pad;  // the north boundary face row
-  // Windows at face row f: cells f-2..f+1, velocities f-1..f+1.
-  R r[4], e[4], w[3];
-  for (int q = 0; q < 4; ++q) {
-    const size_t c = cidx(nx, i0 - 2 + q, jj);
-    r[q] = s.r_in_r[c];
-    e[q] = s.e_in_r[c];
+  // Windows at face row f: cells f-2..f+1 (densities and energies with their
+  // differences), face velocities f-1..f+1 with theirs; each row shifts them
+  // by one and forms only the new differences.
+  ColSteps<R> rw;
+  ColWindow<R> ew;
+  {
+    R r[4], e[4];
+    for (int q = 0; q < 4; ++q) {
+      const size_t c = cidx(nx, i0 - 2 + q, jj);
+      r[q] = s.r_in_r[c];
+      e[q] = s.e_in_r[c];
+    }
+    rw.init(r[0], r[1], r[2], r[3]);
+    ew.init(e[0], e[1], e[2], e[3]);
   }
-  for (int q = 0; q < 3; ++q) w[q] = a.v[cidx(nx, i0 - 1 + q, jj)];
+  R vm = a.v[cidx(nx, i0 - 1, jj)];
+  R v0 = a.v[cidx(nx, i0, jj)];
+  R vp = a.v[cidx(nx, i0 + 1, jj)];
+  R dvm = v0 - vm, dvp = vp - v0, dv2 = vp - vm;
+  // Face row f = i0 + k: inverse spacing s_iey[k], cell widths s_cy[k] below
+  // and s_cy[k + 1] above, downstream inverse width s_icy[k].
+  auto flux_at = [&](int k, R* F, R* eF) {
+    mass_energy_flux_core<R, true, kP2>(
+        v0, dv2, dvm, dvp, rw.m1, rw.p0, rw.d2, [&](bool up) { return up ? rw.d1 : rw.d3; },
+        [&](bool pos, R wdt) {
+          return ew.template face<kP2>(pos, s_iey[k], pos ? s_cy[k] : s_cy[k + 1], wdt);
+        },
+        s_iey[k], s_icy[k], ex0_r, dt_r, dt_h_r, F, eF);
+  };
   R F0, eF0;
-  mass_energy_flux<R, true, kP2>(w[0], w[1], w[2], r[0], r[1], r[2], r[3], e[0], e[1],
-                            e[2], e[3], s_iey[0], s_cy[0], s_cy[1], s_icy[0],
-                            ex0_r, dt_r, dt_h_r, &F0, &eF0);
+  flux_at(0, &F0, &eF0);
   {
     const size_t c = cidx(nx, i0, jj);
     a.F_y[c] = F0;
@@ -741,21 +857,21 @@ __device__ __forceinline__ void tile_mass_sweep_y_impl(const StepArgs<R>& a,
   }
   for (int ii = i0; ii < i1; ++ii) {
     const int k = ii - i0;
-    for (int q = 0; q < 3; ++q) {
-      r[q] = r[q + 1];
-      e[q] = e[q + 1];
-    }
     const size_t c_next = cidx(nx, ii + 2, jj);
-    r[3] = s.r_in_r[c_next];
-    e[3] = s.e_in_r[c_next];
-    w[0] = w[1];
-    w[1] = w[2];
-    w[2] = a.v[cidx(nx, ii + 2, jj)];
+    rw.shift(s.r_in_r[c_next]);
+    ew.shift(s.e_in_r[c_next]);
+    {
+      const R vn = a.v[c_next];
+      const R dv2n = vn - v0, dvpn = vn - vp;
+      dvm = dvp;
+      dvp = dvpn;
+      dv2 = dv2n;
+      vm = v0;
+      v0 = vp;
+      vp = vn;
+    }
     R F1, eF1;
-    mass_energy_flux<R, true, kP2>(w[0], w[1], w[2], r[0], r[1], r[2], r[3], e[0],
-                              e[1], e[2], e[3], s_iey[k + 1], s_cy[k + 1],
-                              s_cy[k + 2], s_icy[k + 1], ex0_r, dt_r, dt_h_r, &F1,
-                              &eF1);
+    flux_at(k + 1, &F1, &eF1);
     if (ii + 1 < i1 || ii + 1 == last_face) {
       const size_t c = cidx(nx, ii + 1, jj);
       a.F_y[c] = F1;
@@ -815,7 +931,7 @@ __device__ __forceinline__ void tile_flux_uFx_impl(const StepArgs<R>& a, int bx,
   for (int ii = i0; ii < i1; ++ii) {
     const size_t f = fidx(nx, ii, jj);
     const R u0 = a.u[f], u1 = a.u[f + 1];
-    const R mass = s_hey[ii - i0] * (a.F_x[f] + a.F_x[f + 1]);
+    const R mass = Prec<R>::template mulp<kP2>(a.F_x[f] + a.F_x[f + 1], s_hey[ii - i0]);
     const R wind = Prec<R>::half(u0 + u1);
     const R val = mass * momentum_upwind<R, kP2>(wind, a.u[f - 1], u0, u1, a.u[f + 2], iex,
                                          cxl, cxr, dt_h);
@@ -841,22 +957,21 @@ __device__ __forceinline__ void tile_flux_uFy_impl(const StepArgs<R>& a, int bx,
   const R dt_h = R(a.dt_slot[1]);
   const R hex = Prec<R>::half(R(a.edgedx[jj]));  // edgedx * 0.5
   const int i1 = min(i0 + a.rows, ny + 1 - pad);
-  R um2 = a.u[fidx(nx, i0 - 2, jj)];
-  R um1 = a.u[fidx(nx, i0 - 1, jj)];
-  R u0 = a.u[fidx(nx, i0, jj)];
+  // u of rows ii-2 .. ii+1 around corner row ii, shifted down the column.
+  ColWindow<R> uw;
+  uw.init(a.u[fidx(nx, i0 - 2, jj)], a.u[fidx(nx, i0 - 1, jj)], a.u[fidx(nx, i0, jj)],
+          a.u[fidx(nx, i0 + 1, jj)]);
   for (int ii = i0; ii < i1; ++ii) {
     const int k = ii - i0;
-    const R up = a.u[fidx(nx, ii + 1, jj)];
     const size_t c = cidx(nx, ii, jj);
-    const R mass = hex * (a.F_y[c] + a.F_y[c - 1]);
+    const R mass = Prec<R>::template mulp<kP2>(a.F_y[c] + a.F_y[c - 1], hex);
     const R wind = Prec<R>::half(a.v[c - 1] + a.v[c]);
-    const R val = mass * momentum_upwind<R, kP2>(wind, um2, um1, u0, up, s_iey[k], s_cy[k],
-                                         s_cy[k + 1], dt_h);
+    const bool pos = Prec<R>::gt0(wind);
+    const R val = mass * uw.template face<kP2>(pos, s_iey[k], pos ? s_cy[k] : s_cy[k + 1],
+                                               wind * dt_h);
     a.uF_y[fidx(nx, ii, jj)] = val;
     mirror(a.uF_y, nx + 1, ny + 1, pad, ii, jj, val, false, false);
-    um2 = um1;
-    um1 = u0;
-    u0 = up;
+    if (ii + 1 < i1) uw.shift(a.u[fidx(nx, ii + 2, jj)]);
   }
 }
 
@@ -881,7 +996,7 @@ __device__ __forceinline__ void tile_flux_vFx_impl(const StepArgs<R>& a, int bx,
     const size_t f = fidx(nx, ii, jj);
     const size_t c = cidx(nx, ii, jj);
     const R u0 = a.u[f], F0 = a.F_x[f];
-    const R mass = s_hcy[ii - i0] * (F0 + F_dn);
+    const R mass = Prec<R>::template mulp<kP2>(F0 + F_dn, s_hcy[ii - i0]);
     const R wind = Prec<R>::half(u0 + u_dn);
     const R val = mass * momentum_upwind<R, kP2>(wind, a.v[c - 2], a.v[c - 1], a.v[c],
                                          a.v[c + 1], iex, cxl, cxr, dt_h);
@@ -909,23 +1024,22 @@ __device__ __forceinline__ void tile_flux_vFy_impl(const StepArgs<R>& a, int bx,
   const R dt_h = R(a.dt_slot[1]);
   const R hcx = Prec<R>::half(R(a.celldx[jj]));  // celldx * 0.5
   const int i1 = min(i0 + a.rows, ny - pad);
-  R vm = a.v[cidx(nx, i0 - 1, jj)];
-  R v0 = a.v[cidx(nx, i0, jj)];
-  R vp = a.v[cidx(nx, i0 + 1, jj)];
+  // v of face rows ii-1 .. ii+2 around cell row ii, shifted down the column.
+  ColWindow<R> vw;
+  vw.init(a.v[cidx(nx, i0 - 1, jj)], a.v[cidx(nx, i0, jj)], a.v[cidx(nx, i0 + 1, jj)],
+          a.v[cidx(nx, i0 + 2, jj)]);
   R F0 = a.F_y[cidx(nx, i0, jj)];
   for (int ii = i0; ii < i1; ++ii) {
     const int k = ii - i0;
-    const R vp2 = a.v[cidx(nx, ii + 2, jj)];
     const R F1 = a.F_y[cidx(nx, ii + 1, jj)];
-    const R mass = hcx * (F0 + F1);
-    const R wind = Prec<R>::half(v0 + vp);
-    const R val = mass * momentum_upwind<R, kP2>(wind, vm, v0, vp, vp2, s_iey[k], s_cy[k],
-                                         s_cy[k + 1], dt_h);
+    const R mass = Prec<R>::template mulp<kP2>(F0 + F1, hcx);
+    const R wind = Prec<R>::half(vw.m1 + vw.p0);
+    const bool pos = Prec<R>::gt0(wind);
+    const R val = mass * vw.template face<kP2>(pos, s_iey[k], pos ? s_cy[k] : s_cy[k + 1],
+                                               wind * dt_h);
     a.vF_y[cidx(nx, ii, jj)] = val;
     mirror(a.vF_y, nx, ny, pad, ii, jj, val, false, false);
-    vm = v0;
-    v0 = vp;
-    vp = vp2;
+    if (ii + 1 < i1) vw.shift(a.v[cidx(nx, ii + 3, jj)]);
     F0 = F1;
   }
 }
@@ -1014,8 +1128,8 @@ __device__ __forceinline__ void tile_momentum_update_impl(const StepArgs<R>& a, 
     *mom = m;
     if (kVel) {
       R rbar;
-      if (kU) rbar = fma(a.rho_r[c], wx0, a.rho_r[c - 1] * wx1);
-      else rbar = fma(a.rho_r[c], s_wy0[k], a.rho_r[c - nx] * s_wy1[k]);
+      if (kU) rbar = face_average<R, kP2>(a.rho_r[c], wx0, a.rho_r[c - 1], wx1);
+      else rbar = face_average<R, kP2>(a.rho_r[c], s_wy0[k], a.rho_r[c - nx], s_wy1[k]);
       const R vel = Pr::is_zero(rbar) ? R(0) : Pr::div(m, rbar);
       if (kU) {
         a.u[f] = vel;
