@@ -321,6 +321,31 @@ def run_sequential_ensemble(fg, torch, device, probs, precision, warmup, steps):
             "what": "per-instance single-problem steps, host-timed (each step reads dt back)"}
 
 
+def run_fp64_smooth(fg, problems, torch, device, n, steps, warmup):
+    """The FP64 step on a field with structure everywhere (density and energy
+    1 + a 16-mode smooth random field, seed 20261205): no flat regions, so
+    every slope and limiter is live -- the general-case rate next to the
+    blast problem, most of whose mesh is still at rest."""
+    import numpy as np
+    sim = fg.DeviceSim(problems.smooth_random(n, np.random.default_rng(20261205)), device)
+    sim.initial_timestep()
+    for _ in range(warmup):
+        sim.step()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        sim.step()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    del sim
+    torch.cuda.empty_cache()
+    return {"workload": f"smooth_{n}_fp64", "value": n * n * steps / (ms * 1e-3), "unit": UNIT,
+            "ms_per_step": ms / steps, "steps": steps, "warmup": warmup}
+
+
 def run_mixed_form(fg, problems, torch, device, n, steps, warmup, ref_state=None, workload="sedov"):
     """Times the mixed form on the same workload; returns its result dict and
     the final simulation object."""
@@ -448,6 +473,8 @@ def run_gpu(args):
     if not args.fp64_only:
         del sim, sim2
         torch.cuda.empty_cache()
+        forms["fp64_smooth"] = run_fp64_smooth(fg, problems, torch, device, n,
+                                               min(args.steps, 100), args.warmup)
         # The mixed form on the FP64 workload, then on the 8192^2 Sod tube.
         for workload, size in (("sedov", n), ("sod", args.sod_size)):
             if size <= 0:

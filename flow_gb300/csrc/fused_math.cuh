@@ -137,6 +137,14 @@ __device__ __forceinline__ double d_rcp(double x) {
   e = fma(-x, r, 1.0);
   return fma(r, e, r);
 }
+// 1/x to ~2^-40 (one Newton step on the MUFU seed) for a reciprocal that is
+// only ever used through a residual-corrected quotient (qdiv), which is then
+// still correctly rounded: the correction squares the error.
+__device__ __forceinline__ double d_rcp_for_qdiv(double x) {
+  double r;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
+  return fma(r, fma(-x, r, 1.0), r);
+}
 // n/d for finite normal non-zero d when 1/d itself is not needed: one Newton
 // step on the MUFU seed (relative error ~2^-20 measured -> ~2^-40), the
 // quotient from it, and one residual correction q + r (n - d q) (-> ~2^-80):

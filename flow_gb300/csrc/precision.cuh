@@ -35,6 +35,8 @@ struct Prec<double> {
   __device__ static __forceinline__ double min0(double x) { return d_min0(x); }
   __device__ static __forceinline__ double minmod(double a, double b) { return d_minmod(a, b); }
   __device__ static __forceinline__ double rcp(double x) { return d_rcp(x); }
+  // A reciprocal used only through qdiv (which corrects the quotient).
+  __device__ static __forceinline__ double rcp_q(double x) { return d_rcp_for_qdiv(x); }
   __device__ static __forceinline__ double rsqrt(double x) { return d_rsqrt(x); }
   __device__ static __forceinline__ double to_d(double x) { return x; }
   __device__ static __forceinline__ double from_d(double x) { return x; }
@@ -125,6 +127,7 @@ struct Prec<float> {
   __device__ static __forceinline__ float msub(float m, float t, float s) { return fmaf(-t, s, m); }
   __device__ static __forceinline__ float madd(float h, float w, float b) { return fmaf(h, w, b); }
   __device__ static __forceinline__ float qdiv(float n, float, float inv) { return n * inv; }
+  __device__ static __forceinline__ float rcp_q(float x) { return rcp(x); }
   __device__ static __forceinline__ float div(float n, float d) { return n * rcp(d); }
   template <bool kPow2 = false>
   __device__ static __forceinline__ float dsub(float m, float t, float, float inv) {

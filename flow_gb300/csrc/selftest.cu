@@ -33,7 +33,7 @@ __device__ __forceinline__ long long ulp_gap(double a, double b) {
 }
 
 // counts[0] d_half != x*0.5, [1] d_twice != x*2 (all bit patterns, NaN = NaN),
-// [2] d_is_pow2 wrong, [3] d_div != IEEE n/d, [4] d_rcp + one correction
+// [2] d_is_pow2 wrong, [3] d_div != IEEE n/d, [4] d_rcp_for_qdiv + qdiv
 // != IEEE n/d, [5] d_mul_pow2(x, 2^k) != x*2^k (all bit patterns of x, k in
 // [-1022, 1023]); ulp[0], ulp[1] the largest gaps of [3], [4]; seed_err the
 // largest |rcp.approx(d) d - 1| as FP64 bits.
@@ -66,7 +66,7 @@ __global__ void k_check(long long n, unsigned long long seed, unsigned long long
     const double nn = normal_from(mix64(h + 1)), dd = normal_from(mix64(h + 2));
     const double q = __ddiv_rn(nn, dd);
     const double qa = d_div(nn, dd);
-    const double r = d_rcp(dd);
+    const double r = d_rcp_for_qdiv(dd);
     const double qb = fma(r, fma(-dd, nn * r, nn), nn * r);
     if (dbits(qa) != dbits(q)) {
       ++c[3];

@@ -299,7 +299,7 @@ int gb300_measure_fp64_fma_rate(double* fma_per_s);
  *   counts[1]  x*2 on the integer pipes != IEEE x*2
  *   counts[2]  power-of-two test wrong
  *   counts[3]  one-Newton-step quotient with one correction != IEEE n/d
- *   counts[4]  Newton reciprocal + one correction quotient != IEEE n/d
+ *   counts[4]  one-Newton-step reciprocal, then a corrected quotient != IEEE n/d
  *   counts[5]  x times a power of two on the integer pipes != IEEE product
  * max_ulp[0..1]: the largest gaps of counts[3..4] in units in the last
  * place; max_seed_rel_err: the largest |rcp.approx(d) * d - 1|. */

@@ -6,7 +6,7 @@ on the GPU against the IEEE operations (gb300_check_fp64_helpers):
 * the power-of-two test that selects the exact-spacing fast path, and the
   product by a power of two as an exponent add: exact;
 * quotients: one Newton step on the MUFU seed with one residual correction
-  (d_div) and the two-step Newton reciprocal with one correction (qdiv) both
+  (d_div) and the one-step Newton reciprocal with a corrected quotient (qdiv) both
   return the IEEE quotient except in vanishingly rare near-ties, and then
   differ by one unit in the last place.
 """
