@@ -79,8 +79,8 @@ def parse_args():
 
 
 def dist_env():
-    return (int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)),
-            int(os.environ.get("LOCAL_RANK", 0)))
+    from flow_gb300.replicas import dist_env as env
+    return env()
 
 
 def measured_peaks():
@@ -250,7 +250,13 @@ def run_batched_form(fg, problems, torch, device, kind, precision, steps, warmup
     """Times one batched ensemble (autotuned, graph-replayed) and measures its
     error on two sampled instances against the single-problem FP64 step."""
     import numpy as np
+    from flow_gb300.replicas import max_over_ranks, shard_instances, sum_over_ranks
+    rank, world, _ = dist_env()
     probs = batch_problems(problems, kind)
+    if world > 1:
+        # Under torchrun the ensemble is split across the GPUs by instance.
+        mine = shard_instances([p.gnx * p.gny for p in probs], rank, world)
+        probs = [probs[i] for i in mine]
     b = fg.Batch(probs, precision=precision, device=device)
     tune = b.autotune(steps=2)
     b.step(warmup)
@@ -262,8 +268,8 @@ def run_batched_form(fg, problems, torch, device, kind, precision, steps, warmup
     e1.record()
     torch.cuda.synchronize()
     b.status()
-    ms = e0.elapsed_time(e1)
-    cells = b.cells
+    ms = max_over_ranks(e0.elapsed_time(e1), device)
+    cells = int(sum_over_ranks(b.cells, device))
     value = cells * steps / (ms * 1e-3)
     total_steps = b.steps_done
     samples = [0, len(probs) // 2]
@@ -385,10 +391,7 @@ def run_gpu(args):
     fg.set_mode(fg.MODE_FUSED)
     n = args.size
 
-    def barrier():
-        if world > 1:
-            import torch.distributed as dist
-            dist.barrier()
+    from flow_gb300.replicas import barrier, job_throughput, max_over_ranks
 
     prob = problems.sedov(n)
     sim = fg.DeviceSim(prob, device)
@@ -422,14 +425,10 @@ def run_gpu(args):
         torch.cuda.synchronize()
         barrier()
     L.gb300_profile_enable(0)
-    ms = e0.elapsed_time(e1)
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms], device=device)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    # The job's time is its slowest replica's.
+    ms = max_over_ranks(e0.elapsed_time(e1), device)
     ms_per_step = ms / args.steps
-    value = world * n * n * args.steps / (ms * 1e-3)
+    value = job_throughput(n * n * args.steps, world, ms * 1e-3)
     mass, energy = out2[0], out2[1]
 
     kernels = []
@@ -461,11 +460,11 @@ def run_gpu(args):
     for f in fields:
         host_out[f].copy_(sim2.a[f], non_blocking=True)
     torch.cuda.synchronize()
-    e2e_s = time.perf_counter() - t0
+    e2e_s = max_over_ranks(time.perf_counter() - t0, device)
     barrier()
     h2d = sum(host_in[f].numel() * 8 for f in fields)
     d2h = sum(host_out[f].numel() * 8 for f in fields)
-    e2e_value = world * n * n * args.steps / e2e_s
+    e2e_value = job_throughput(n * n * args.steps, world, e2e_s)
     del host_in, host_out
 
     # ---- the mixed-precision form on the same workload ----
