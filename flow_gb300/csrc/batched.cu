@@ -167,9 +167,15 @@ __device__ __forceinline__ int phase_list(int tt, int* ph) {
   return n;
 }
 
+// Resident CTAs per SM the register budget is sized for: the mixed form is
+// bound by latency and keeps 8 (64 registers); the FP64 form by its FP64 pipe,
+// and 5 (up to 102 registers) leaves it without spills.
 template <typename R>
-__global__ void __launch_bounds__(kCols) k_batch_step(const BatchDev<R> b, int tt,
-                                                      int first_step) {
+constexpr int kBatchMinCtas = Prec<R>::kMixed ? 8 : 5;
+
+template <typename R>
+__global__ void __launch_bounds__(kCols, kBatchMinCtas<R>) k_batch_step(const BatchDev<R> b,
+                                                                         int tt, int first_step) {
   __shared__ Instance<R> s_inst;
   __shared__ int s_cur;
   int ph[20];

@@ -345,22 +345,30 @@ __device__ __forceinline__ void tile_lag_viscous_accel_impl(const StepArgs<R>& a
     if (ii < ny - pad) {
       const size_t f = fidx(nx, ii, jj);
       const size_t c = cidx(nx, ii, jj);
-      const R mom = Pr::template dsub<kP2>(a.rho_u[f], dt * (a.Qxx[c] - a.Qxx[c - 1]), cx, icx);
-      const R inv = a.F_x[f];
-      const R vel = Pr::is_zero(inv) ? R(0) : Pr::qdiv(mom, a.uF_x[f], inv);
-      a.rho_u[f] = mom;
-      a.u[f] = vel;
-      mirror(a.u, nx + 1, ny, pad, ii, jj, vel, true, false);
+      // No stress gradient: the momentum and the velocity from the pressure
+      // phase stand as they are.
+      const R dqx = a.Qxx[c] - a.Qxx[c - 1];
+      if (!Pr::is_zero(dqx)) {
+        const R mom = Pr::template dsub<kP2>(a.rho_u[f], dt * dqx, cx, icx);
+        const R inv = a.F_x[f];
+        const R vel = Pr::is_zero(inv) ? R(0) : Pr::qdiv(mom, a.uF_x[f], inv);
+        a.rho_u[f] = mom;
+        a.u[f] = vel;
+        mirror(a.u, nx + 1, ny, pad, ii, jj, vel, true, false);
+      }
     }
     if (jj < nx - pad) {
       const size_t c = cidx(nx, ii, jj);
       const R qy = a.Qyy[c];
-      const R mom = Pr::template dsub<kP2>(a.rho_v[c], dt * (qy - qy_dn), s_cy[k], s_icy[k]);
-      const R inv = a.F_y[c];
-      const R vel = Pr::is_zero(inv) ? R(0) : Pr::qdiv(mom, a.vF_y[c], inv);
-      a.rho_v[c] = mom;
-      a.v[c] = vel;
-      mirror(a.v, nx, ny + 1, pad, ii, jj, vel, false, true);
+      const R dqy = qy - qy_dn;
+      if (!Pr::is_zero(dqy)) {
+        const R mom = Pr::template dsub<kP2>(a.rho_v[c], dt * dqy, s_cy[k], s_icy[k]);
+        const R inv = a.F_y[c];
+        const R vel = Pr::is_zero(inv) ? R(0) : Pr::qdiv(mom, a.vF_y[c], inv);
+        a.rho_v[c] = mom;
+        a.v[c] = vel;
+        mirror(a.v, nx, ny + 1, pad, ii, jj, vel, false, true);
+      }
       qy_dn = qy;
     }
   }
@@ -426,21 +434,30 @@ __device__ __forceinline__ void tile_lag_energy_dt_impl(const StepArgs<R>& a, in
       const R p = Pr::kMixed ? R(kG1) * r * er : R(a.P[c]);
       const R qx = a.Qxx[c], qy = a.Qyy[c];
       const bool rz = Pr::is_zero(r);
-      const R inv_r = rz ? R(0) : Pr::rcp(r);
       const R dudx = Pr::template mulp<kP2>(a.u[f + 1] - a.u[f], icx);
       const R dvdy = Pr::template mulp<kP2>(v1 - v0, s_icy[k]);
-      const R div_dt = (dudx + dvdy) * dt_h;
-      // e_q = e - dt_h (Qxx dudx + Qyy dvdy) / rho, kept as an increment.
-      const R dq = -(dt_h * fma(qx, dudx, qy * dvdy)) * inv_r;
-      const R e_q = er + dq;
-      const R rho_c = r * Pr::rcp(R(1) + div_dt);
-      const R e_c = fma(-(p * div_dt), inv_r, e_q);
-      const R work = Pr::half(div_dt) * fma(R(kG1) * e_c, rho_c, p) * inv_r;
+      // A cell whose faces do not move relative to each other does no work
+      // and takes no shock heating: every increment below is a zero, so e is
+      // left as it is (a cell at rest, or in uniform translation).
+      const bool still = Pr::is_zero(dudx) && Pr::is_zero(dvdy);
+      R inv_r = R(0);
       double e_new;
-      if (Pr::kMixed) {
-        e_new = rz ? 0.0 : a.e[c] + Pr::to_d(dq - work);
+      if (still) {
+        e_new = rz ? 0.0 : (Pr::kMixed ? a.e[c] : double(er));
       } else {
-        e_new = rz ? 0.0 : double(e_q - work);
+        inv_r = rz ? R(0) : Pr::rcp(r);
+        const R div_dt = (dudx + dvdy) * dt_h;
+        // e_q = e - dt_h (Qxx dudx + Qyy dvdy) / rho, kept as an increment.
+        const R dq = -(dt_h * fma(qx, dudx, qy * dvdy)) * inv_r;
+        const R e_q = er + dq;
+        const R rho_c = r * Pr::rcp(R(1) + div_dt);
+        const R e_c = fma(-(p * div_dt), inv_r, e_q);
+        const R work = Pr::half(div_dt) * fma(R(kG1) * e_c, rho_c, p) * inv_r;
+        if (Pr::kMixed) {
+          e_new = rz ? 0.0 : a.e[c] + Pr::to_d(dq - work);
+        } else {
+          e_new = rz ? 0.0 : double(e_q - work);
+        }
       }
       store_cell(a.e, a.e_r, nx, ny, pad, ii, jj, e_new);
       // CFL: celldx / sqrt(c_s^2 + 2 Q / rho) with c_s^2 = gamma (gamma-1) e.
@@ -451,9 +468,13 @@ __device__ __forceinline__ void tile_lag_energy_dt_impl(const StepArgs<R>& a, in
       // Skip such cells rather than use gamma (gamma-1) e + 2Q/rho directly.
       const R e_nr = Pr::from_d(e_new);
       const R s2 = R(kGam * (kGam - 1.0)) * e_nr;
-      const R two_inv_r = Pr::twice(inv_r);
-      const R sx = fma(qx, two_inv_r, s2);
-      const R sy = fma(qy, two_inv_r, s2);
+      R sx = s2, sy = s2;  // + 2 Q / rho, zero without viscous stress
+      if (!Pr::is_zero(qx) || !Pr::is_zero(qy)) {
+        if (still) inv_r = rz ? R(0) : Pr::rcp(r);
+        const R two_inv_r = Pr::twice(inv_r);
+        sx = fma(qx, two_inv_r, s2);
+        sy = fma(qy, two_inv_r, s2);
+      }
       const bool e_neg = Pr::kMixed ? (e_nr < R(0)) : d_lt0(e_new);
       if constexpr (Pr::kMixed) {
         const unsigned long long mx = (unsigned long long)dbits(Pr::to_d(cx * Pr::rsqrt(sx)));
