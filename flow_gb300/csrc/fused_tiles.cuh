@@ -150,6 +150,16 @@ __device__ __forceinline__ bool block_mesh_pow2(const StepArgs<R>& a, int col0, 
     CALL_FALSE;                                                             \
   } while (0)
 
+// Face velocity momentum / face density (0 where the face density is 0, as
+// the reference sets it); a face without momentum keeps it (0 / rho = 0).
+template <typename R>
+__device__ __forceinline__ R face_velocity(R mom, R rbar) {
+  using Pr = Prec<R>;
+  if (Pr::is_zero(rbar)) return R(0);
+  if (Pr::is_zero(mom)) return mom;
+  return Pr::div(mom, rbar);
+}
+
 // Volume-weighted face value a*wa + b*wb, rounded once after the product
 // b*wb (the reference's a*wa + b*wb contracted as in the fused kernels).  On
 // power-of-two meshes both weights are powers of two, both products exact
@@ -235,27 +245,29 @@ __device__ __forceinline__ void tile_lag_pressure_impl(const StepArgs<R>& a, int
     __syncthreads();
     if (ii >= pad && ii < ny - pad && jj >= pad && jj < nx + 1 - pad) {
       const size_t f = fidx(nx, ii, jj);
-      const R mom = Pr::template dsub<kP2>(a.rho_u[f], dt * (Pc - sP[t]), exr, iex);
+      const R dp = Pc - sP[t];
+      R mom = a.rho_u[f];
+      if (!Pr::is_zero(dp)) {
+        mom = Pr::template dsub<kP2>(mom, dt * dp, exr, iex);
+        a.rho_u[f] = mom;
+      }
       const R rbar = face_average<R, kP2>(rc, wx0, sR[t], wx1);
-      const bool z = Pr::is_zero(rbar);
-      const R inv = z ? R(0) : Pr::rcp_q(rbar);
-      const R vel = z ? R(0) : Pr::qdiv(mom, rbar, inv);
-      a.rho_u[f] = mom;
+      const R vel = face_velocity(mom, rbar);
       a.u[f] = vel;
-      a.F_x[f] = inv;
       a.uF_x[f] = rbar;
       mirror(a.u, nx + 1, ny, pad, ii, jj, vel, true, false);
     }
     if (ii >= pad && ii < ny + 1 - pad && jj >= pad && jj < nx - pad) {
       const size_t c = cidx(nx, ii, jj);
-      const R mom = Pr::template dsub<kP2>(a.rho_v[c], dt * (Pc - P_dn), s_ey[k], s_iey[k]);
+      const R dp = Pc - P_dn;
+      R mom = a.rho_v[c];
+      if (!Pr::is_zero(dp)) {
+        mom = Pr::template dsub<kP2>(mom, dt * dp, s_ey[k], s_iey[k]);
+        a.rho_v[c] = mom;
+      }
       const R rbar = face_average<R, kP2>(rc, s_wy0[k], r_dn, s_wy1[k]);
-      const bool z = Pr::is_zero(rbar);
-      const R inv = z ? R(0) : Pr::rcp_q(rbar);
-      const R vel = z ? R(0) : Pr::qdiv(mom, rbar, inv);
-      a.rho_v[c] = mom;
+      const R vel = face_velocity(mom, rbar);
       a.v[c] = vel;
-      a.F_y[c] = inv;
       a.vF_y[c] = rbar;
       mirror(a.v, nx, ny + 1, pad, ii, jj, vel, false, true);
     }
@@ -275,8 +287,9 @@ __device__ __forceinline__ void tile_lag_pressure(const StepArgs<R>& a, int bx, 
 template <typename R>
 __device__ __forceinline__ R visc_stress(R crho, R lo, R mid, R hi, R hi2) {
   using Pr = Prec<R>;
-  const R m0 = Pr::min0(mid - lo);
   const R m1 = Pr::min0(hi - mid);
+  if (Pr::is_zero(m1)) return R(0);  // no compression across the cell
+  const R m0 = Pr::min0(mid - lo);
   const R m2 = Pr::min0(hi2 - hi);
   return crho * m1 * Pr::half(Pr::abs(m2 - m1) + Pr::abs(m1 - m0));
 }
@@ -305,7 +318,7 @@ __device__ __forceinline__ void tile_lag_viscosity(const StepArgs<R>& a, int bx,
     const R qx = visc_stress(crho, a.u[f - 1], a.u[f], a.u[f + 1], a.u[f + 2]);
     const R m2 = Pr::min0(vp2 - vp);
     const R g12 = Pr::abs(m2 - m1);
-    const R qy = crho * m1 * Pr::half(g12 + g01);
+    const R qy = Pr::is_zero(m1) ? R(0) : crho * m1 * Pr::half(g12 + g01);
     a.Qxx[c] = qx;
     a.Qyy[c] = qy;
     mirror(a.Qxx, nx, ny, pad, ii, jj, qx, false, false);
@@ -350,8 +363,7 @@ __device__ __forceinline__ void tile_lag_viscous_accel_impl(const StepArgs<R>& a
       const R dqx = a.Qxx[c] - a.Qxx[c - 1];
       if (!Pr::is_zero(dqx)) {
         const R mom = Pr::template dsub<kP2>(a.rho_u[f], dt * dqx, cx, icx);
-        const R inv = a.F_x[f];
-        const R vel = Pr::is_zero(inv) ? R(0) : Pr::qdiv(mom, a.uF_x[f], inv);
+        const R vel = face_velocity(mom, a.uF_x[f]);
         a.rho_u[f] = mom;
         a.u[f] = vel;
         mirror(a.u, nx + 1, ny, pad, ii, jj, vel, true, false);
@@ -363,8 +375,7 @@ __device__ __forceinline__ void tile_lag_viscous_accel_impl(const StepArgs<R>& a
       const R dqy = qy - qy_dn;
       if (!Pr::is_zero(dqy)) {
         const R mom = Pr::template dsub<kP2>(a.rho_v[c], dt * dqy, s_cy[k], s_icy[k]);
-        const R inv = a.F_y[c];
-        const R vel = Pr::is_zero(inv) ? R(0) : Pr::qdiv(mom, a.vF_y[c], inv);
+        const R vel = face_velocity(mom, a.vF_y[c]);
         a.rho_v[c] = mom;
         a.v[c] = vel;
         mirror(a.v, nx, ny + 1, pad, ii, jj, vel, false, true);
@@ -628,6 +639,11 @@ __device__ __forceinline__ void mass_energy_flux_core(R v0, R dv2, R dvm, R dvp,
                                                       R inv_h, R icd, R area, R dt, R dt_h,
                                                       R* F_out, R* eF_out) {
   using Pr = Prec<R>;
+  if (Pr::is_zero(v0)) {  // a face at rest carries no mass and no energy
+    *F_out = R(0);
+    *eF_out = R(0);
+    return;
+  }
   // minmod(0.5 (vp-vm)/h, 2 (v0-vm)/h, 2 (vp-v0)/h), scaled once (mc_reconstruct).
   const R mm = Pr::template mulp<kP2>(
       Pr::minmod(Pr::half(dv2), Pr::minmod(Pr::twice(dvm), Pr::twice(dvp))), inv_h);
@@ -955,9 +971,11 @@ __device__ __forceinline__ void tile_flux_uFx_impl(const StepArgs<R>& a, int bx,
     const size_t f = fidx(nx, ii, jj);
     const R u0 = a.u[f], u1 = a.u[f + 1];
     const R mass = Prec<R>::template mulp<kP2>(a.F_x[f] + a.F_x[f + 1], s_hey[ii - i0]);
-    const R wind = Prec<R>::half(u0 + u1);
-    const R val = mass * momentum_upwind<R, kP2>(wind, a.u[f - 1], u0, u1, a.u[f + 2], iex,
-                                         cxl, cxr, dt_h);
+    // No mass through the cell, no momentum flux (the upwind value is skipped).
+    const R val = Prec<R>::is_zero(mass)
+                      ? mass
+                      : mass * momentum_upwind<R, kP2>(Prec<R>::half(u0 + u1), a.u[f - 1], u0, u1,
+                                                       a.u[f + 2], iex, cxl, cxr, dt_h);
     a.uF_x[cidx(nx, ii, jj)] = val;
     mirror(a.uF_x, nx, ny, pad, ii, jj, val, false, false);
   }
@@ -988,10 +1006,12 @@ __device__ __forceinline__ void tile_flux_uFy_impl(const StepArgs<R>& a, int bx,
     const int k = ii - i0;
     const size_t c = cidx(nx, ii, jj);
     const R mass = Prec<R>::template mulp<kP2>(a.F_y[c] + a.F_y[c - 1], hex);
-    const R wind = Prec<R>::half(a.v[c - 1] + a.v[c]);
-    const bool pos = Prec<R>::gt0(wind);
-    const R val = mass * uw.template face<kP2>(pos, s_iey[k], pos ? s_cy[k] : s_cy[k + 1],
-                                               wind * dt_h);
+    R val = mass;
+    if (!Prec<R>::is_zero(mass)) {
+      const R wind = Prec<R>::half(a.v[c - 1] + a.v[c]);
+      const bool pos = Prec<R>::gt0(wind);
+      val = mass * uw.template face<kP2>(pos, s_iey[k], pos ? s_cy[k] : s_cy[k + 1], wind * dt_h);
+    }
     a.uF_y[fidx(nx, ii, jj)] = val;
     mirror(a.uF_y, nx + 1, ny + 1, pad, ii, jj, val, false, false);
     if (ii + 1 < i1) uw.shift(a.u[fidx(nx, ii + 2, jj)]);
@@ -1020,9 +1040,11 @@ __device__ __forceinline__ void tile_flux_vFx_impl(const StepArgs<R>& a, int bx,
     const size_t c = cidx(nx, ii, jj);
     const R u0 = a.u[f], F0 = a.F_x[f];
     const R mass = Prec<R>::template mulp<kP2>(F0 + F_dn, s_hcy[ii - i0]);
-    const R wind = Prec<R>::half(u0 + u_dn);
-    const R val = mass * momentum_upwind<R, kP2>(wind, a.v[c - 2], a.v[c - 1], a.v[c],
-                                         a.v[c + 1], iex, cxl, cxr, dt_h);
+    const R val = Prec<R>::is_zero(mass)
+                      ? mass
+                      : mass * momentum_upwind<R, kP2>(Prec<R>::half(u0 + u_dn), a.v[c - 2],
+                                                       a.v[c - 1], a.v[c], a.v[c + 1], iex, cxl,
+                                                       cxr, dt_h);
     a.vF_x[f] = val;
     mirror(a.vF_x, nx + 1, ny + 1, pad, ii, jj, val, false, false);
     u_dn = u0;
@@ -1056,10 +1078,12 @@ __device__ __forceinline__ void tile_flux_vFy_impl(const StepArgs<R>& a, int bx,
     const int k = ii - i0;
     const R F1 = a.F_y[cidx(nx, ii + 1, jj)];
     const R mass = Prec<R>::template mulp<kP2>(F0 + F1, hcx);
-    const R wind = Prec<R>::half(vw.m1 + vw.p0);
-    const bool pos = Prec<R>::gt0(wind);
-    const R val = mass * vw.template face<kP2>(pos, s_iey[k], pos ? s_cy[k] : s_cy[k + 1],
-                                               wind * dt_h);
+    R val = mass;
+    if (!Prec<R>::is_zero(mass)) {
+      const R wind = Prec<R>::half(vw.m1 + vw.p0);
+      const bool pos = Prec<R>::gt0(wind);
+      val = mass * vw.template face<kP2>(pos, s_iey[k], pos ? s_cy[k] : s_cy[k + 1], wind * dt_h);
+    }
     a.vF_y[cidx(nx, ii, jj)] = val;
     mirror(a.vF_y, nx, ny, pad, ii, jj, val, false, false);
     if (ii + 1 < i1) vw.shift(a.v[cidx(nx, ii + 3, jj)]);
@@ -1145,15 +1169,18 @@ __device__ __forceinline__ void tile_momentum_update_impl(const StepArgs<R>& a, 
     else diff = a.vF_y[c] - a.vF_y[c - nx];
     R* mom = kU ? a.rho_u + f : a.rho_v + c;
     // mom - dt_h * diff / (hx * hy), the divisor rounded as the reference
-    // forms it (omp3/flow.c:581-584).
-    const R m = Pr::template dsub<kP2>(*mom, dt_h_r * diff, hx_r * s_h[k],
-                                       Pr::template mulp<kP2>(s_row[k], ihx));
-    *mom = m;
+    // forms it (omp3/flow.c:581-584); no flux difference, no change.
+    R m = *mom;
+    if (!Pr::is_zero(diff)) {
+      m = Pr::template dsub<kP2>(m, dt_h_r * diff, hx_r * s_h[k],
+                                 Pr::template mulp<kP2>(s_row[k], ihx));
+      *mom = m;
+    }
     if (kVel) {
       R rbar;
       if (kU) rbar = face_average<R, kP2>(a.rho_r[c], wx0, a.rho_r[c - 1], wx1);
       else rbar = face_average<R, kP2>(a.rho_r[c], s_wy0[k], a.rho_r[c - nx], s_wy1[k]);
-      const R vel = Pr::is_zero(rbar) ? R(0) : Pr::div(m, rbar);
+      const R vel = face_velocity(m, rbar);
       if (kU) {
         a.u[f] = vel;
         mirror(a.u, nx + 1, ny, pad, ii, jj, vel, true, false);
