@@ -156,7 +156,7 @@ template <typename R>
 __device__ __forceinline__ R face_velocity(R mom, R rbar) {
   using Pr = Prec<R>;
   if (Pr::is_zero(rbar)) return R(0);
-  if (Pr::is_zero(mom)) return mom;
+  if (Pr::zero_skip(mom)) return mom;
   return Pr::div(mom, rbar);
 }
 
@@ -247,7 +247,7 @@ __device__ __forceinline__ void tile_lag_pressure_impl(const StepArgs<R>& a, int
       const size_t f = fidx(nx, ii, jj);
       const R dp = Pc - sP[t];
       R mom = a.rho_u[f];
-      if (!Pr::is_zero(dp)) {
+      if (!Pr::zero_skip(dp)) {
         mom = Pr::template dsub<kP2>(mom, dt * dp, exr, iex);
         a.rho_u[f] = mom;
       }
@@ -261,7 +261,7 @@ __device__ __forceinline__ void tile_lag_pressure_impl(const StepArgs<R>& a, int
       const size_t c = cidx(nx, ii, jj);
       const R dp = Pc - P_dn;
       R mom = a.rho_v[c];
-      if (!Pr::is_zero(dp)) {
+      if (!Pr::zero_skip(dp)) {
         mom = Pr::template dsub<kP2>(mom, dt * dp, s_ey[k], s_iey[k]);
         a.rho_v[c] = mom;
       }
@@ -288,7 +288,7 @@ template <typename R>
 __device__ __forceinline__ R visc_stress(R crho, R lo, R mid, R hi, R hi2) {
   using Pr = Prec<R>;
   const R m1 = Pr::min0(hi - mid);
-  if (Pr::is_zero(m1)) return R(0);  // no compression across the cell
+  if (Pr::zero_skip(m1)) return R(0);  // no compression across the cell
   const R m0 = Pr::min0(mid - lo);
   const R m2 = Pr::min0(hi2 - hi);
   return crho * m1 * Pr::half(Pr::abs(m2 - m1) + Pr::abs(m1 - m0));
@@ -318,7 +318,7 @@ __device__ __forceinline__ void tile_lag_viscosity(const StepArgs<R>& a, int bx,
     const R qx = visc_stress(crho, a.u[f - 1], a.u[f], a.u[f + 1], a.u[f + 2]);
     const R m2 = Pr::min0(vp2 - vp);
     const R g12 = Pr::abs(m2 - m1);
-    const R qy = Pr::is_zero(m1) ? R(0) : crho * m1 * Pr::half(g12 + g01);
+    const R qy = Pr::zero_skip(m1) ? R(0) : crho * m1 * Pr::half(g12 + g01);
     a.Qxx[c] = qx;
     a.Qyy[c] = qy;
     mirror(a.Qxx, nx, ny, pad, ii, jj, qx, false, false);
@@ -361,7 +361,7 @@ __device__ __forceinline__ void tile_lag_viscous_accel_impl(const StepArgs<R>& a
       // No stress gradient: the momentum and the velocity from the pressure
       // phase stand as they are.
       const R dqx = a.Qxx[c] - a.Qxx[c - 1];
-      if (!Pr::is_zero(dqx)) {
+      if (!Pr::zero_skip(dqx)) {
         const R mom = Pr::template dsub<kP2>(a.rho_u[f], dt * dqx, cx, icx);
         const R vel = face_velocity(mom, a.uF_x[f]);
         a.rho_u[f] = mom;
@@ -373,7 +373,7 @@ __device__ __forceinline__ void tile_lag_viscous_accel_impl(const StepArgs<R>& a
       const size_t c = cidx(nx, ii, jj);
       const R qy = a.Qyy[c];
       const R dqy = qy - qy_dn;
-      if (!Pr::is_zero(dqy)) {
+      if (!Pr::zero_skip(dqy)) {
         const R mom = Pr::template dsub<kP2>(a.rho_v[c], dt * dqy, s_cy[k], s_icy[k]);
         const R vel = face_velocity(mom, a.vF_y[c]);
         a.rho_v[c] = mom;
@@ -450,7 +450,7 @@ __device__ __forceinline__ void tile_lag_energy_dt_impl(const StepArgs<R>& a, in
       // A cell whose faces do not move relative to each other does no work
       // and takes no shock heating: every increment below is a zero, so e is
       // left as it is (a cell at rest, or in uniform translation).
-      const bool still = Pr::is_zero(dudx) && Pr::is_zero(dvdy);
+      const bool still = Pr::zero_skip_coarse(dudx) && Pr::zero_skip_coarse(dvdy);
       R inv_r = R(0);
       double e_new;
       if (still) {
@@ -480,7 +480,7 @@ __device__ __forceinline__ void tile_lag_energy_dt_impl(const StepArgs<R>& a, in
       const R e_nr = Pr::from_d(e_new);
       const R s2 = R(kGam * (kGam - 1.0)) * e_nr;
       R sx = s2, sy = s2;  // + 2 Q / rho, zero without viscous stress
-      if (!Pr::is_zero(qx) || !Pr::is_zero(qy)) {
+      if (!Pr::zero_skip_coarse(qx) || !Pr::zero_skip_coarse(qy)) {
         if (still) inv_r = rz ? R(0) : Pr::rcp(r);
         const R two_inv_r = Pr::twice(inv_r);
         sx = fma(qx, two_inv_r, s2);
@@ -564,7 +564,7 @@ __device__ __forceinline__ R mc_reconstruct(bool pos, R da, R db, R dc, R base, 
                                             R wdt) {
   using Pr = Prec<R>;
   const R m0 = Pr::minmod(Pr::minmod(Pr::half(da), Pr::twice(db)), Pr::twice(dc));
-  if (Pr::is_zero(m0)) return base;
+  if (Pr::zero_skip(m0)) return base;
   const R mm = Pr::template mulp<kP2>(m0, inv_h);
   const R w = h + (pos ? Pr::neg(wdt) : wdt);
   const R hm = Pr::half(pos ? mm : Pr::neg(mm));
@@ -639,7 +639,7 @@ __device__ __forceinline__ void mass_energy_flux_core(R v0, R dv2, R dvm, R dvp,
                                                       R inv_h, R icd, R area, R dt, R dt_h,
                                                       R* F_out, R* eF_out) {
   using Pr = Prec<R>;
-  if (Pr::is_zero(v0)) {  // a face at rest carries no mass and no energy
+  if (Pr::zero_skip_coarse(v0)) {  // a face at rest carries no mass and no energy
     *F_out = R(0);
     *eF_out = R(0);
     return;
@@ -661,7 +661,7 @@ __device__ __forceinline__ void mass_energy_flux_core(R v0, R dv2, R dvm, R dvp,
   const R rho_up = Pr::ge0(w_tc) ? rm1 : r0;
   const R wdt = w_tc * dt_h;
   R flux;
-  if (Pr::is_zero(lim)) {
+  if (Pr::zero_skip(lim)) {
     flux = w_tc * rho_up;
   } else {
     flux = Pr::madd(w_tc, rho_up,
@@ -972,7 +972,7 @@ __device__ __forceinline__ void tile_flux_uFx_impl(const StepArgs<R>& a, int bx,
     const R u0 = a.u[f], u1 = a.u[f + 1];
     const R mass = Prec<R>::template mulp<kP2>(a.F_x[f] + a.F_x[f + 1], s_hey[ii - i0]);
     // No mass through the cell, no momentum flux (the upwind value is skipped).
-    const R val = Prec<R>::is_zero(mass)
+    const R val = Prec<R>::zero_skip_coarse(mass)
                       ? mass
                       : mass * momentum_upwind<R, kP2>(Prec<R>::half(u0 + u1), a.u[f - 1], u0, u1,
                                                        a.u[f + 2], iex, cxl, cxr, dt_h);
@@ -1007,7 +1007,7 @@ __device__ __forceinline__ void tile_flux_uFy_impl(const StepArgs<R>& a, int bx,
     const size_t c = cidx(nx, ii, jj);
     const R mass = Prec<R>::template mulp<kP2>(a.F_y[c] + a.F_y[c - 1], hex);
     R val = mass;
-    if (!Prec<R>::is_zero(mass)) {
+    if (!Prec<R>::zero_skip_coarse(mass)) {
       const R wind = Prec<R>::half(a.v[c - 1] + a.v[c]);
       const bool pos = Prec<R>::gt0(wind);
       val = mass * uw.template face<kP2>(pos, s_iey[k], pos ? s_cy[k] : s_cy[k + 1], wind * dt_h);
@@ -1040,7 +1040,7 @@ __device__ __forceinline__ void tile_flux_vFx_impl(const StepArgs<R>& a, int bx,
     const size_t c = cidx(nx, ii, jj);
     const R u0 = a.u[f], F0 = a.F_x[f];
     const R mass = Prec<R>::template mulp<kP2>(F0 + F_dn, s_hcy[ii - i0]);
-    const R val = Prec<R>::is_zero(mass)
+    const R val = Prec<R>::zero_skip_coarse(mass)
                       ? mass
                       : mass * momentum_upwind<R, kP2>(Prec<R>::half(u0 + u_dn), a.v[c - 2],
                                                        a.v[c - 1], a.v[c], a.v[c + 1], iex, cxl,
@@ -1079,7 +1079,7 @@ __device__ __forceinline__ void tile_flux_vFy_impl(const StepArgs<R>& a, int bx,
     const R F1 = a.F_y[cidx(nx, ii + 1, jj)];
     const R mass = Prec<R>::template mulp<kP2>(F0 + F1, hcx);
     R val = mass;
-    if (!Prec<R>::is_zero(mass)) {
+    if (!Prec<R>::zero_skip_coarse(mass)) {
       const R wind = Prec<R>::half(vw.m1 + vw.p0);
       const bool pos = Prec<R>::gt0(wind);
       val = mass * vw.template face<kP2>(pos, s_iey[k], pos ? s_cy[k] : s_cy[k + 1], wind * dt_h);
@@ -1171,7 +1171,7 @@ __device__ __forceinline__ void tile_momentum_update_impl(const StepArgs<R>& a, 
     // mom - dt_h * diff / (hx * hy), the divisor rounded as the reference
     // forms it (omp3/flow.c:581-584); no flux difference, no change.
     R m = *mom;
-    if (!Pr::is_zero(diff)) {
+    if (!Pr::zero_skip(diff)) {
       m = Pr::template dsub<kP2>(m, dt_h_r * diff, hx_r * s_h[k],
                                  Pr::template mulp<kP2>(s_row[k], ihx));
       *mom = m;

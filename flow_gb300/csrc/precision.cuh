@@ -25,6 +25,12 @@ struct Prec;
 template <>
 struct Prec<double> {
   static constexpr bool kMixed = false;
+  // x is an exact zero whose arithmetic a tile may skip (the result is the
+  // same number).  Worth it where FP64 instructions are the bound: every
+  // such test, per lane.  zero_skip_coarse marks the few skips that remove
+  // a whole flux or cell update.
+  __device__ static __forceinline__ bool zero_skip(double x) { return d_is_zero(x); }
+  __device__ static __forceinline__ bool zero_skip_coarse(double x) { return d_is_zero(x); }
   __device__ static __forceinline__ bool is_zero(double x) { return d_is_zero(x); }
   __device__ static __forceinline__ bool gt0(double x) { return d_gt0(x); }
   __device__ static __forceinline__ bool ge0(double x) { return d_ge0(x); }
@@ -102,6 +108,15 @@ __device__ __forceinline__ float f64_to_f32(double x) {
 template <>
 struct Prec<float> {
   static constexpr bool kMixed = true;
+  // The FP32 bulk is cheap and bound by issue latency, where branches cost
+  // more than most skips save (measured: ~10% slower on fields in motion
+  // everywhere).  Only the coarse skips remain, taken when every active lane
+  // of the warp has the zero (a warp-uniform branch; each lane's own value
+  // is zero then, so the skip is exact for each).
+  __device__ static __forceinline__ constexpr bool zero_skip(float) { return false; }
+  __device__ static __forceinline__ bool zero_skip_coarse(float x) {
+    return __all_sync(__activemask(), x == 0.0f) != 0;
+  }
   __device__ static __forceinline__ bool is_zero(float x) { return x == 0.0f; }
   __device__ static __forceinline__ bool gt0(float x) { return x > 0.0f; }
   __device__ static __forceinline__ bool ge0(float x) { return x >= 0.0f; }
