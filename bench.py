@@ -69,6 +69,9 @@ def parse_args():
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--size", type=int, default=N_CELLS_SIDE)
+    p.add_argument("--workload", default="sedov", choices=["sedov", "smooth"],
+                   help="the FP64 line's problem: the blast (default) or a field in "
+                        "motion everywhere")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--fp64-only", action="store_true", help="skip the mixed/batched forms")
     p.add_argument("--sod-size", type=int, default=8192,
@@ -156,13 +159,22 @@ def _omp_env():
     return int(os.environ["OMP_NUM_THREADS"])
 
 
-def cpu_run(n: int, steps: int, warmup: int, budget_s: float):
+def main_problem(problems, workload: str, n: int):
+    """The FP64 line's problem: the Sedov-type blast, or density and energy
+    1 + a 16-mode smooth random field (seed 20261205)."""
+    if workload == "smooth":
+        import numpy as np
+        return problems.smooth_random(n, np.random.default_rng(20261205))
+    return problems.sedov(n)
+
+
+def cpu_run(n: int, steps: int, warmup: int, budget_s: float, workload: str = "sedov"):
     """Times the oracle on the same workload; returns (cell-steps/s, steps
     timed, threads).  Times at most ~budget_s seconds of steps."""
     threads = _omp_env()
     from flow_gb300 import problems
     from oracle import oracle as O
-    prob = problems.sedov(n)
+    prob = main_problem(problems, workload, n)
     hm = O.HostMesh(n, n, dt=prob.dt_param)
     st = O.HostState(hm)
     O.fill_fields(hm, st, prob.interior(prob.rho), prob.interior(prob.e))
@@ -194,15 +206,16 @@ def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    value, timed, threads = cpu_run(args.size, args.steps, args.warmup, budget_s=150.0)
-    sample = (f"Sedov {args.size}^2 FP64 timesteps on {threads} host threads: "
+    value, timed, threads = cpu_run(args.size, args.steps, args.warmup, budget_s=150.0,
+                                    workload=args.workload)
+    sample = (f"{args.workload} {args.size}^2 FP64 timesteps on {threads} host threads: "
               f"{timed} of {args.steps} requested steps timed after {args.warmup} warm-up")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": args.size * args.size / value * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"sedov_{args.size}_fp64", "nx": args.size, "ny": args.size,
+        "config": {"workload": f"{args.workload}_{args.size}_fp64", "nx": args.size, "ny": args.size,
                    "form": "fp64", "parallelism": "host OpenMP"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": sample},
@@ -393,7 +406,7 @@ def run_gpu(args):
 
     from flow_gb300.replicas import barrier, job_throughput, max_over_ranks
 
-    prob = problems.sedov(n)
+    prob = main_problem(problems, args.workload, n)
     sim = fg.DeviceSim(prob, device)
     sim.initial_timestep()
     out2 = (fg.ctypes.c_double * 2)()
@@ -442,7 +455,7 @@ def run_gpu(args):
 
     # ---- end to end through the C ABI with host buffers ----
     fields = ("rho", "e", "rho_u", "rho_v", "u", "v")
-    prob2 = problems.sedov(n)
+    prob2 = main_problem(problems, args.workload, n)
     sim2 = fg.DeviceSim(prob2, device)
     host_in = {f: sim2.a[f].cpu().pin_memory() for f in fields}
     host_out = {f: torch.empty_like(host_in[f]).pin_memory() for f in fields}
@@ -472,8 +485,9 @@ def run_gpu(args):
     if not args.fp64_only:
         del sim, sim2
         torch.cuda.empty_cache()
-        forms["fp64_smooth"] = run_fp64_smooth(fg, problems, torch, device, n,
-                                               min(args.steps, 100), args.warmup)
+        if args.workload != "smooth":
+            forms["fp64_smooth"] = run_fp64_smooth(fg, problems, torch, device, n,
+                                                   min(args.steps, 100), args.warmup)
         # The mixed form on the FP64 workload, then on the 8192^2 Sod tube.
         for workload, size in (("sedov", n), ("sod", args.sod_size)):
             if size <= 0:
@@ -525,9 +539,9 @@ def run_gpu(args):
 
     cpu = None
     if not args.no_cpu_baseline:
-        cv, timed, threads = cpu_run(n, 64, 1, budget_s=20.0)
+        cv, timed, threads = cpu_run(n, 64, 1, budget_s=20.0, workload=args.workload)
         cpu = {"value": cv, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": f"Sedov {n}^2 FP64, {timed} timesteps on {threads} host threads "
+               "sample": f"{args.workload} {n}^2 FP64, {timed} timesteps on {threads} host threads "
                          "(C restatement of the reference omp3 set, OpenMP)"}
 
     line = {
@@ -535,7 +549,7 @@ def run_gpu(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"sedov_{n}_fp64", "nx": n, "ny": n, "form": "fp64",
+        "config": {"workload": f"{args.workload}_{n}_fp64", "nx": n, "ny": n, "form": "fp64",
                    "iterations_timed": args.steps, "l2": "inputs larger than L2 (2.3 GB state)",
                    "parallelism": "replicas" if world > 1 else "single GPU",
                    "hbm_fraction_of_step": value / world * B_ALG_FP64 / (peak * 1e9)},

@@ -150,6 +150,11 @@ __device__ __forceinline__ bool block_mesh_pow2(const StepArgs<R>& a, int col0, 
     CALL_FALSE;                                                             \
   } while (0)
 
+// The FP64 quotient as a called function: a branch around five inline FP64
+// instructions is turned into predicated code, which occupies the FP64 pipe
+// even in lanes (and whole warps) that skip it; a call is a real branch.
+static __device__ __noinline__ double face_quotient(double n, double d) { return d_div(n, d); }
+
 // Face velocity momentum / face density (0 where the face density is 0, as
 // the reference sets it); a face without momentum keeps it (0 / rho = 0).
 template <typename R>
@@ -157,7 +162,11 @@ __device__ __forceinline__ R face_velocity(R mom, R rbar) {
   using Pr = Prec<R>;
   if (Pr::is_zero(rbar)) return R(0);
   if (Pr::zero_skip(mom)) return mom;
-  return Pr::div(mom, rbar);
+  if constexpr (Pr::kMixed) {
+    return Pr::div(mom, rbar);
+  } else {
+    return face_quotient(mom, rbar);
+  }
 }
 
 // Volume-weighted face value a*wa + b*wb, rounded once after the product
