@@ -721,6 +721,11 @@ __device__ __forceinline__ void mass_energy_update(double r_in, double e_in,
     const double coef = dt_h * ivol;
     r_new = fma(-coef, fma(a1, f1, -(a0 * f0)), r_in);
     rho_e = fma(-coef, de, r_old * e_in);
+  } else if (Pr::zero_skip(f0) && Pr::zero_skip(f1) && Pr::zero_skip(de)) {
+    // Nothing crosses the cell's faces: the updates subtract zeros.  (The
+    // energy still takes the reference's rho_old*e/den round trip below.)
+    r_new = r_in;
+    rho_e = __dmul_rn(r_old, e_in);
   } else {
     const double net = __dadd_rn(Prec<double>::mulp<kP2>(f1, a1), -Prec<double>::mulp<kP2>(f0, a0));
     r_new = Prec<double>::dsub<kP2>(r_in, __dmul_rn(dt_h, net), vol, ivol);
