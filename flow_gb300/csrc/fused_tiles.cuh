@@ -718,9 +718,15 @@ __device__ __forceinline__ void mass_energy_update(double r_in, double e_in,
   const double de = Pr::to_d(eF1) - Pr::to_d(eF0);
   double r_new, rho_e;
   if (Pr::kMixed) {
-    const double coef = dt_h * ivol;
-    r_new = fma(-coef, fma(a1, f1, -(a0 * f0)), r_in);
-    rho_e = fma(-coef, de, r_old * e_in);
+    if (Pr::zero_skip_coarse(F0) && Pr::zero_skip_coarse(F1)) {
+      // No flux through any cell of the warp: the updates subtract zeros.
+      r_new = r_in;
+      rho_e = r_old * e_in;
+    } else {
+      const double coef = dt_h * ivol;
+      r_new = fma(-coef, fma(a1, f1, -(a0 * f0)), r_in);
+      rho_e = fma(-coef, de, r_old * e_in);
+    }
   } else if (Pr::zero_skip(f0) && Pr::zero_skip(f1) && Pr::zero_skip(de)) {
     // Nothing crosses the cell's faces: the updates subtract zeros.  (The
     // energy still takes the reference's rho_old*e/den round trip below.)

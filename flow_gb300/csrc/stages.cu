@@ -198,19 +198,20 @@ __global__ void __launch_bounds__(kRedThreads)
   }
 }
 
+// Each block sums whole interior rows (threads stride along the row), so the
+// traversal needs no division of a flat index.
 __global__ void __launch_bounds__(kRedThreads)
     k_conservation(int nx, int ny, int pad, const double* rho, const double* e,
                    double* ra) {
-  const int w = nx - 2 * pad;
-  const long long n = (long long)w * (ny - 2 * pad);
   double ms = 0.0, es = 0.0;
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
-       t += (long long)gridDim.x * blockDim.x) {
-    const int ii = pad + (int)(t / w);
-    const int jj = pad + (int)(t % w);
-    const size_t c = cidx(nx, ii, jj);
-    ms += rho[c];
-    es += rho[c] * e[c];
+  for (int ii = pad + blockIdx.x; ii < ny - pad; ii += gridDim.x) {
+    const double* rr = rho + (size_t)ii * nx;
+    const double* er = e + (size_t)ii * nx;
+    for (int jj = pad + threadIdx.x; jj < nx - pad; jj += blockDim.x) {
+      const double d = rr[jj];
+      ms += d;
+      es += d * er[jj];
+    }
   }
   __shared__ double s_m[kRedThreads / 32], s_e[kRedThreads / 32];
   __shared__ bool s_last;
