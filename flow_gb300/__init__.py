@@ -104,6 +104,7 @@ def _declare(L: ctypes.CDLL) -> None:
         "gb300_solve_hydro_2d": [M, I] + [P] * 17,
         "gb300_conservation": [I, I, I, P, P, P, P, I],
         "gb300_conservation_noalloc": [I, I, I, P, P, P],
+        "gb300_fill_boxes": [I, I, P, P, P, I, P, P],
         "gb300_profile_enable": [I],
         "gb300_profile_reset": [],
         "gb300_profile_count": [],
@@ -130,6 +131,7 @@ def _declare(L: ctypes.CDLL) -> None:
         "gb300_batch_create": [I, IP, IP, P, P, I, ctypes.POINTER(V)],
         "gb300_batch_bind": [V, V, ctypes.c_size_t],
         "gb300_batch_set_state": [V, I, P, P, D],
+        "gb300_batch_fill_boxes": [V, I, P, I, D],
         "gb300_batch_set_tuning": [V, I, I, I],
         "gb300_batch_get_tuning": [V, IP, IP, IP, IP],
         "gb300_batch_step": [V, I, I],
@@ -164,6 +166,12 @@ def set_stream(stream) -> None:
 def set_mode(mode: int) -> None:
     if lib().gb300_set_mode(mode) != GB300_OK:
         check()
+
+
+def boxes_array(boxes) -> "ctypes.Array":
+    """(density, energy, xpos, ypos, width, height) boxes as a flat C array."""
+    flat = [float(v) for b in boxes for v in b]
+    return (ctypes.c_double * max(1, len(flat)))(*flat)
 
 
 def dptr(t) -> "ctypes._Pointer":

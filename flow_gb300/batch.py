@@ -41,12 +41,20 @@ class Batch:
         self.pool = torch.empty(self.bytes, dtype=torch.uint8, device=device)
         if L.gb300_batch_bind(handle, ctypes.c_void_p(self.pool.data_ptr()), self.bytes) != GB300_OK:
             check()
+        from . import boxes_array
         for i, p in enumerate(problems):
-            rho = np.ascontiguousarray(p.interior(p.rho), dtype=np.float64)
-            e = np.ascontiguousarray(p.interior(p.e), dtype=np.float64)
-            if L.gb300_batch_set_state(handle, i, rho.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
-                                       e.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
-                                       p.dt_param) != GB300_OK:
+            if p.box_list is not None:
+                # Problem boxes are rasterised on the device: no host fields.
+                st = L.gb300_batch_fill_boxes(handle, i, boxes_array(p.box_list),
+                                              len(p.box_list), p.dt_param)
+            else:
+                rho = np.ascontiguousarray(p.interior(p.rho), dtype=np.float64)
+                e = np.ascontiguousarray(p.interior(p.e), dtype=np.float64)
+                st = L.gb300_batch_set_state(handle, i,
+                                             rho.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                             e.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                             p.dt_param)
+            if st != GB300_OK:
                 check()
         torch.cuda.synchronize()
         self.steps_done = 0

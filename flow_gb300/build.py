@@ -33,7 +33,7 @@ UNIT_FLAGS = {
 }
 
 SOURCES = ["stages.cu", "interface.cu", "fused.cu", "batched.cu", "profile.cu", "peaks.cu",
-           "noalloc.cu", "selftest.cu"]
+           "noalloc.cu", "selftest.cu", "init.cu"]
 
 
 def _nvcc() -> str:
@@ -96,9 +96,11 @@ def _build_driver(verbose: bool) -> None:
     cuda_lib = os.path.join(_cuda_home(), "lib64")
     link_cuda = ["-L" + cuda_lib, "-Wl,-rpath," + cuda_lib, "-lcudart"]
     arch_src = os.path.join(PKG, "host", "arch_gb300.c")
-    if _stale(ARCH_LIB, [arch_src] + _headers()):
+    if _stale(ARCH_LIB, [arch_src, LIB] + _headers()):
+        # The arch layer's problem set-up calls the kernel set's device
+        # rasteriser (gb300_fill_boxes).
         cmd = ["gcc", "-O2", "-std=gnu99", "-fPIC", "-shared", *inc, arch_src, "-o", ARCH_LIB,
-               *link_cuda]
+               "-L" + PKG, "-lflow_gb300", "-Wl,-rpath,$ORIGIN", *link_cuda]
         if verbose:
             print(" ".join(cmd), flush=True)
         subprocess.run(cmd, check=True)

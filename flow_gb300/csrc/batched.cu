@@ -21,6 +21,7 @@
 #include "../../include/flow_gb300.h"
 #include "fused.h"
 #include "fused_tiles.cuh"
+#include "init.h"
 #include "stages.h"
 
 namespace flow {
@@ -526,7 +527,8 @@ int gb300_batch_bind(GB300Batch* b, void* pool, size_t bytes) {
   o += 256;
   B.d_inst = B.pool + o;
   cudaStreamSynchronize(current_stream());
-  // Uniform meshes: spacing width/gnx on every face and cell.
+  // Uniform meshes: spacing width/gnx on every face and cell, and the face
+  // positions (for device-side problem set-up) after the four spacing arrays.
   for (int i = 0; i < B.n; ++i) {
     const int nx = B.gnx[i] + 4, ny = B.gny[i] + 4;
     const InstLayout L = inst_layout(nx, ny, B.precision);
@@ -537,30 +539,28 @@ int gb300_batch_bind(GB300Batch* b, void* pool, size_t bytes) {
     k_fill<<<8, 256, 0, current_stream()>>>(mesh + m, m, dy);
     k_fill<<<8, 256, 0, current_stream()>>>(mesh + 2 * m, m, dx);
     k_fill<<<8, 256, 0, current_stream()>>>(mesh + 3 * m, m, dy);
+    launch_uniform_edges(current_stream(), mesh + 4 * m, nx + 1, 2, B.width[i], B.gnx[i]);
+    launch_uniform_edges(current_stream(), mesh + 5 * m, ny + 1, 2, B.height[i], B.gny[i]);
   }
   const int st = check_launch("gb300_batch_bind");
   if (st != GB300_OK) return st;
   return retune(B);
 }
 
-int gb300_batch_set_state(GB300Batch* b, int i, const double* rho, const double* e,
-                          double dt_param) {
+namespace {
+
+// Ghost fill, FP32 shadows and the driver's first set_timestep of instance i
+// once its interior density and energy are in place.
+int finish_state(flow::BatchImpl& B, int i, double dt_param, const char* where) {
   using namespace flow;
-  if (!b || i < 0 || i >= b->impl.n || !rho || !e || !b->impl.pool) {
-    return record_error(GB300_ERR_ARG, "gb300_batch_set_state: bad arguments");
-  }
-  BatchImpl& B = b->impl;
   const int gx = B.gnx[i], gy = B.gny[i], nx = gx + 4, ny = gy + 4;
+  (void)gx;
+  (void)gy;
   const InstLayout L = inst_layout(nx, ny, B.precision);
   char* base = B.pool + B.off[i];
   double* d_rho = reinterpret_cast<double*>(base + L.rho);
   double* d_e = reinterpret_cast<double*>(base + L.e);
   cudaStream_t s = current_stream();
-  // Interior rows (host arrays are gy x gx, row-major) into the padded mesh.
-  cudaMemcpy2DAsync(d_rho + 2 * (size_t)nx + 2, nx * sizeof(double), rho, gx * sizeof(double),
-                    gx * sizeof(double), gy, cudaMemcpyHostToDevice, s);
-  cudaMemcpy2DAsync(d_e + 2 * (size_t)nx + 2, nx * sizeof(double), e, gx * sizeof(double),
-                    gx * sizeof(double), gy, cudaMemcpyHostToDevice, s);
   launch_boundary(s, nx, ny, 2, d_rho, kNoInvert);
   launch_boundary(s, nx, ny, 2, d_e, kNoInvert);
   if (B.precision == 1) {
@@ -581,7 +581,49 @@ int gb300_batch_set_state(GB300Batch* b, int i, const double* rho, const double*
   launch_min_timestep(s, nx, ny, 2, 10.0, dt0, 0, zeros, zeros, d_rho, d_e, mv, ra);
   // The fused CFL minimum starts from "no candidate yet".
   cudaMemsetAsync(ra + kRaMinSlot, 0xff, sizeof(double), s);
-  return check_launch("gb300_batch_set_state");
+  return check_launch(where);
+}
+
+}  // namespace
+
+int gb300_batch_set_state(GB300Batch* b, int i, const double* rho, const double* e,
+                          double dt_param) {
+  using namespace flow;
+  if (!b || i < 0 || i >= b->impl.n || !rho || !e || !b->impl.pool) {
+    return record_error(GB300_ERR_ARG, "gb300_batch_set_state: bad arguments");
+  }
+  BatchImpl& B = b->impl;
+  const int gx = B.gnx[i], gy = B.gny[i], nx = gx + 4;
+  const InstLayout L = inst_layout(nx, gy + 4, B.precision);
+  char* base = B.pool + B.off[i];
+  double* d_rho = reinterpret_cast<double*>(base + L.rho);
+  double* d_e = reinterpret_cast<double*>(base + L.e);
+  cudaStream_t s = current_stream();
+  // Interior rows (host arrays are gy x gx, row-major) into the padded mesh.
+  cudaMemcpy2DAsync(d_rho + 2 * (size_t)nx + 2, nx * sizeof(double), rho, gx * sizeof(double),
+                    gx * sizeof(double), gy, cudaMemcpyHostToDevice, s);
+  cudaMemcpy2DAsync(d_e + 2 * (size_t)nx + 2, nx * sizeof(double), e, gx * sizeof(double),
+                    gx * sizeof(double), gy, cudaMemcpyHostToDevice, s);
+  return finish_state(B, i, dt_param, "gb300_batch_set_state");
+}
+
+int gb300_batch_fill_boxes(GB300Batch* b, int i, const double* boxes, int nboxes,
+                           double dt_param) {
+  using namespace flow;
+  if (!b || i < 0 || i >= b->impl.n || !b->impl.pool) {
+    return record_error(GB300_ERR_ARG, "gb300_batch_fill_boxes: bad arguments");
+  }
+  BatchImpl& B = b->impl;
+  const int nx = B.gnx[i] + 4, ny = B.gny[i] + 4;
+  const InstLayout L = inst_layout(nx, ny, B.precision);
+  char* base = B.pool + B.off[i];
+  const size_t m = (size_t)std::max(nx, ny) + 1;
+  const double* mesh = reinterpret_cast<const double*>(base + L.mesh);
+  const int st = launch_fill_boxes(current_stream(), nx, ny, mesh + 4 * m, mesh + 5 * m, boxes,
+                                   nboxes, reinterpret_cast<double*>(base + L.rho),
+                                   reinterpret_cast<double*>(base + L.e));
+  if (st != GB300_OK) return st;
+  return finish_state(B, i, dt_param, "gb300_batch_fill_boxes");
 }
 
 int gb300_batch_set_tuning(GB300Batch* b, int rows, int ctas_per_sm, int order) {

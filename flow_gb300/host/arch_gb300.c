@@ -1,8 +1,9 @@
 /*
  * arch_gb300.c -- single-rank GPU arch layer of the flow host driver
  * (include/flow_arch.h): params parsing, device allocation, uniform mesh
- * set-up, problem rasterisation and the VisIt dump.  Compiled into
- * libflow_gb300_arch.so.
+ * set-up, problem set-up (the params boxes, rasterised on the device by the
+ * kernel set's gb300_fill_boxes) and the VisIt dump.  Compiled into
+ * libflow_gb300_arch.so, which links libflow_gb300.so.
  */
 #include <cuda_runtime.h>
 #include <stdio.h>
@@ -10,6 +11,7 @@
 #include <string.h>
 
 #include "../../include/flow_arch.h"
+#include "../../include/flow_gb300.h"
 
 struct Profile compute_profile;
 struct Profile comms_profile;
@@ -144,10 +146,6 @@ static double* upload(const double* h, size_t n) {
   return d;
 }
 
-/* Host copies of the face positions, kept for the problem rasteriser. */
-static double* g_host_edgex = NULL;
-static double* g_host_edgey = NULL;
-
 void initialise_mesh_2d(Mesh* mesh) {
   const int nx = mesh->local_nx, ny = mesh->local_ny;
   double* ex = (double*)malloc(sizeof(double) * (nx + 1));
@@ -170,10 +168,8 @@ void initialise_mesh_2d(Mesh* mesh) {
   mesh->celldx = upload(dxs, nx + 1);
   mesh->edgedy = upload(dys, ny + 1);
   mesh->celldy = upload(dys, ny + 1);
-  free(g_host_edgex);
-  free(g_host_edgey);
-  g_host_edgex = ex;
-  g_host_edgey = ey;
+  free(ex);
+  free(ey);
   free(dxs);
   free(dys);
 }
@@ -187,40 +183,34 @@ void finalise_mesh(Mesh* mesh) {
   cudaFree(mesh->celldy);
 }
 
-/* Problem boxes: a cell takes a box's density/energy when its left/bottom
- * edge coordinate lies in [pos, pos + extent); later boxes win. */
-static void rasterise(int nx, int ny, const char* params, const double* ex,
-                      const double* ey, double* rho, double* e) {
+/* The problem boxes of the params file (problem_0, problem_1, ...: density,
+ * energy, xpos, ypos, width, height) as rows of 6 doubles; returns the count. */
+static int parse_boxes(const char* params, double* boxes, int max_boxes) {
   char* keys = (char*)malloc(MAX_KEYS * (MAX_STR_LEN + 1));
   double values[MAX_KEYS];
+  int nb = 0;
   for (int pp = 0;; ++pp) {
     char spec[64];
     snprintf(spec, sizeof(spec), "problem_%d", pp);
     int n = 0;
     if (!get_key_value_parameter(spec, params, keys, values, &n)) break;
-    double d = 0, en = 0, x0 = 0, y0 = 0, w = 0, h = 0;
+    if (nb == max_boxes) TERMINATE("more than %d problem boxes\n", max_boxes);
+    double* b = boxes + 6 * nb;
     int have = 0;
     for (int k = 0; k < n; ++k) {
       const char* key = &keys[k * (MAX_STR_LEN + 1)];
-      if (strmatch(key, "density")) { d = values[k]; have |= 1; }
-      else if (strmatch(key, "energy")) { en = values[k]; have |= 2; }
-      else if (strmatch(key, "xpos")) { x0 = values[k]; have |= 4; }
-      else if (strmatch(key, "ypos")) { y0 = values[k]; have |= 8; }
-      else if (strmatch(key, "width")) { w = values[k]; have |= 16; }
-      else if (strmatch(key, "height")) { h = values[k]; have |= 32; }
+      if (strmatch(key, "density")) { b[0] = values[k]; have |= 1; }
+      else if (strmatch(key, "energy")) { b[1] = values[k]; have |= 2; }
+      else if (strmatch(key, "xpos")) { b[2] = values[k]; have |= 4; }
+      else if (strmatch(key, "ypos")) { b[3] = values[k]; have |= 8; }
+      else if (strmatch(key, "width")) { b[4] = values[k]; have |= 16; }
+      else if (strmatch(key, "height")) { b[5] = values[k]; have |= 32; }
     }
     if (have != 63) TERMINATE("%s needs density energy xpos ypos width height\n", spec);
-    for (int ii = 0; ii < ny; ++ii) {
-      if (!(ey[ii] >= y0 && ey[ii] < y0 + h)) continue;
-      for (int jj = 0; jj < nx; ++jj) {
-        if (ex[jj] >= x0 && ex[jj] < x0 + w) {
-          rho[(size_t)ii * nx + jj] = d;
-          e[(size_t)ii * nx + jj] = en;
-        }
-      }
-    }
+    ++nb;
   }
   free(keys);
+  return nb;
 }
 
 void initialise_shared_data_2d(const int local_nx, const int local_ny,
@@ -231,8 +221,6 @@ void initialise_shared_data_2d(const int local_nx, const int local_ny,
   (void)pad;
   (void)width;
   (void)height;
-  (void)edgex;
-  (void)edgey;
   const size_t nc = (size_t)local_nx * local_ny;
   const size_t nf = (size_t)(local_nx + 1) * (local_ny + 1);
   allocate_data(&sd->pressure, nc);
@@ -245,14 +233,16 @@ void initialise_shared_data_2d(const int local_nx, const int local_ny,
   allocate_data(&sd->Qyy, nc);
   allocate_data(&sd->reduce_array0, nc);
   allocate_data(&sd->reduce_array1, nc);
-  if (!g_host_edgex) TERMINATE("initialise_mesh_2d must run first\n");
-  double* rho = (double*)calloc(nc, sizeof(double));
-  double* e = (double*)calloc(nc, sizeof(double));
-  rasterise(local_nx, local_ny, params_filename, g_host_edgex, g_host_edgey, rho, e);
-  cuda_or_die(cudaMemcpy(sd->density, rho, nc * sizeof(double), cudaMemcpyHostToDevice), "upload");
-  cuda_or_die(cudaMemcpy(sd->energy, e, nc * sizeof(double), cudaMemcpyHostToDevice), "upload");
-  free(rho);
-  free(e);
+  if (!edgex || !edgey) TERMINATE("initialise_mesh_2d must run first\n");
+  /* The boxes are rasterised on the device (gb300_fill_boxes): no host
+   * arrays and no copies of the fields. */
+  double boxes[6 * GB300_MAX_BOXES];
+  const int nb = parse_boxes(params_filename, boxes, GB300_MAX_BOXES);
+  if (gb300_fill_boxes(local_nx, local_ny, edgex, edgey, boxes, nb, sd->density,
+                       sd->energy) != GB300_OK) {
+    TERMINATE("problem set-up: %s\n", gb300_last_error_message());
+  }
+  cuda_or_die(cudaDeviceSynchronize(), "problem set-up");
 }
 
 void finalise_shared_data(SharedData* sd) {

@@ -44,6 +44,10 @@ class Problem:
     sim_end: float = 10.0
     rho: np.ndarray = field(default=None, repr=False)
     e: np.ndarray = field(default=None, repr=False)
+    # The boxes the fields were built from, when they were built from boxes
+    # alone (None once fields() sets them): the device can rasterise those
+    # itself (gb300_fill_boxes) instead of receiving host arrays.
+    box_list: list = field(default=None, repr=False)
 
     def __post_init__(self):
         if self.gnx < 2 or self.gny < 2:
@@ -52,6 +56,7 @@ class Problem:
         if self.rho is None:
             self.rho = np.zeros((self.ny, self.nx))
             self.e = np.zeros((self.ny, self.nx))
+            self.box_list = []
 
     # -- mesh arrays (local_n + 1 entries each) ------------------------------
     @property
@@ -85,6 +90,8 @@ class Problem:
             sel = ((ey >= y0) & (ey < y0 + h))[:, None] & ((ex >= x0) & (ex < x0 + w))[None, :]
             self.rho[sel] = d
             self.e[sel] = en
+        if self.box_list is not None:
+            self.box_list = self.box_list + [tuple(float(v) for v in b) for b in boxes]
         return self
 
     def fields(self, rho_int: np.ndarray, e_int: np.ndarray) -> "Problem":
@@ -92,6 +99,7 @@ class Problem:
         p = PAD
         self.rho[p:self.ny - p, p:self.nx - p] = rho_int
         self.e[p:self.ny - p, p:self.nx - p] = e_int
+        self.box_list = None
         return self
 
     def interior(self, a: np.ndarray) -> np.ndarray:
@@ -170,17 +178,13 @@ def two_region(n: int, rng: np.random.Generator) -> Problem:
     e_hi, e_lo = rng.uniform(0.5, 5.0, size=2)
     axis = int(rng.integers(0, 2))
     high_first = bool(rng.integers(0, 2))
-    rho = np.empty((n, n))
-    e = np.empty((n, n))
+    # As boxes: the low side everywhere, then the high half (cells 0..n/2-1
+    # or n/2..n-1 along the axis; the left/bottom-edge rule at k/n is exact).
     half = n // 2
-    a, b = (slice(0, half), slice(half, n)) if high_first else (slice(half, n), slice(0, half))
-    if axis == 0:
-        rho[:, a], e[:, a] = 1.0, e_hi
-        rho[:, b], e[:, b] = 1.0 / ratio, e_lo
-    else:
-        rho[a, :], e[a, :] = 1.0, e_hi
-        rho[b, :], e[b, :] = 1.0 / ratio, e_lo
-    return Problem(n, n).fields(rho, e).with_cfl_dt()
+    lo, extent = (0.0, half / n) if high_first else (half / n, 1.0)
+    high = (lo, 0.0, extent, 1.0) if axis == 0 else (0.0, lo, 1.0, extent)
+    return Problem(n, n).boxes([(1.0 / ratio, e_lo, 0.0, 0.0, 1.0, 1.0),
+                                (1.0, e_hi) + high]).with_cfl_dt()
 
 
 def fourier_field(n: int, rng: np.random.Generator, modes: int = 16,

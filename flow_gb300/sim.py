@@ -61,7 +61,10 @@ class DeviceSim:
             setattr(m, k, dptr(t))
         self.mesh = m
         self.tt = 0
-        self.upload(prob.rho, prob.e)
+        if prob.box_list is not None:
+            self.fill_boxes(prob.box_list)
+        else:
+            self.upload(prob.rho, prob.e)
 
     # -- state transfer -----------------------------------------------------
     def upload(self, rho: np.ndarray, e: np.ndarray) -> None:
@@ -72,6 +75,19 @@ class DeviceSim:
         self.a["rho"].copy_(torch.from_numpy(np.ascontiguousarray(rho, dtype=np.float64).reshape(n)))
         self.a["e"].copy_(torch.from_numpy(np.ascontiguousarray(e, dtype=np.float64).reshape(n)))
         L = lib()
+        for f in ("rho", "e"):
+            L.handle_boundary_2d(self.nx, self.ny, ctypes.byref(self.mesh), dptr(self.a[f]), 0, 1)
+        check()
+
+    def fill_boxes(self, boxes) -> None:
+        """Rasterises problem boxes on the device (gb300_fill_boxes) and fills
+        the ghosts (main.c:52-59)."""
+        from . import boxes_array
+        L = lib()
+        if L.gb300_fill_boxes(self.nx, self.ny, self.mesh.edgex, self.mesh.edgey,
+                              boxes_array(boxes), len(boxes), dptr(self.a["rho"]),
+                              dptr(self.a["e"])) != GB300_OK:
+            check()
         for f in ("rho", "e"):
             L.handle_boundary_2d(self.nx, self.ny, ctypes.byref(self.mesh), dptr(self.a[f]), 0, 1)
         check()

@@ -208,6 +208,19 @@ int gb300_conservation(int nx, int ny, int pad, const double* rho,
 int gb300_conservation_noalloc(int nx, int ny, int pad, const double* rho,
                                const double* e, double* out);
 
+/* Device-side problem set-up (the arch layer's initialise_shared_data_2d
+ * step, main.c:52-54): nboxes problem boxes from the params file (host array
+ * of nboxes x 6: density, energy, xpos, ypos, width, height; at most
+ * GB300_MAX_BOXES) rasterised onto every cell of an nx x ny mesh whose face
+ * positions are the device arrays edgex (nx+1) and edgey (ny+1).  A cell
+ * takes the last box whose [pos, pos + extent) holds its left / bottom edge
+ * coordinate, 0 where none does.  Ghost cells follow the same rule; the
+ * caller applies the reflective fill afterwards, as main.c:56-59 does.
+ * Asynchronous on the current stream. */
+#define GB300_MAX_BOXES 32
+int gb300_fill_boxes(int nx, int ny, const double* edgex, const double* edgey,
+                     const double* boxes, int nboxes, double* rho, double* e);
+
 /* Per-kernel CUDA-event timing of the fused timestep: enable, run steps,
  * then read one (name, launches, total milliseconds) entry per kernel. */
 int gb300_profile_enable(int on);
@@ -270,6 +283,11 @@ int gb300_batch_bind(GB300Batch* batch, void* pool, size_t bytes);
  * params dt dt_param (main.c:30, 64-66). */
 int gb300_batch_set_state(GB300Batch* batch, int i, const double* rho,
                           const double* e, double dt_param);
+/* The same from problem boxes rasterised on the device (gb300_fill_boxes
+ * rule, on the instance's uniform mesh over width x height): no host arrays
+ * and no copies. */
+int gb300_batch_fill_boxes(GB300Batch* batch, int i, const double* boxes, int nboxes,
+                           double dt_param);
 /* Tile height (1..32 rows), CTAs per SM of the persistent launch (0 = as many
  * as fit) and work order (0 largest instance first, 1 input order). */
 int gb300_batch_set_tuning(GB300Batch* batch, int rows, int ctas_per_sm,
