@@ -128,6 +128,38 @@ __device__ __forceinline__ bool d_is_pow2(double x) {
   return (b & 0x000fffffffffffffLL) == 0 && ex - 1u < 0x7feu;
 }
 
+// Quotients of powers of two, for the spacing factors of power-of-two
+// meshes: 1/y, x/(2y) and 1/(y*y) with x, y positive normal powers of two.
+// The quotient is a power of two itself, so when it is a normal number it
+// is formed exactly from the exponent fields on the integer pipes (the IEEE
+// quotient is that same number); otherwise the IEEE expression is evaluated
+// in a called function.
+static __device__ __noinline__ double d_pow2_quot_slow(double x, double y, int form) {
+  if (form == 1) return x / (2.0 * y);
+  if (form == 2) return 1.0 / (y * y);
+  return 1.0 / y;
+}
+__device__ __forceinline__ int d_exp_field(double x) { return (dhi(x) >> 20) & 0x7ff; }
+// 1/y
+__device__ __forceinline__ double d_pow2_rcp(double y) {
+  const int f = 2046 - d_exp_field(y);
+  if ((unsigned)(f - 1) < 2046u) return dfrom2(f << 20, 0);
+  return d_pow2_quot_slow(1.0, y, 0);
+}
+// x / (2 y)  (2 y must not overflow, as it is formed first)
+__device__ __forceinline__ double d_pow2_half_ratio(double x, double y) {
+  const int ey = d_exp_field(y);
+  const int f = d_exp_field(x) - ey + 1022;
+  if ((unsigned)(f - 1) < 2046u && ey < 2046) return dfrom2(f << 20, 0);
+  return d_pow2_quot_slow(x, y, 1);
+}
+// 1 / (y * y)
+__device__ __forceinline__ double d_pow2_rcp_sq(double y) {
+  const int f = 3069 - 2 * d_exp_field(y);
+  if ((unsigned)(f - 1) < 2046u) return dfrom2(f << 20, 0);
+  return d_pow2_quot_slow(1.0, y, 2);
+}
+
 // 1/x for finite normal non-zero x: MUFU seed, two Newton-Raphson steps.
 __device__ __forceinline__ double d_rcp(double x) {
   double r;

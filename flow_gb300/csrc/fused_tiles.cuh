@@ -150,6 +150,53 @@ __device__ __forceinline__ bool block_mesh_pow2(const StepArgs<R>& a, int col0, 
     CALL_FALSE;                                                             \
   } while (0)
 
+// Spacing factors of a tile (mesh spacings, their reciprocals and ratios),
+// formed once per tile from the FP64 mesh arrays:
+//   FP64 form on a power-of-two tile (kP2): exact exponent arithmetic on the
+//     integer pipes (d_pow2_*), the same numbers as the IEEE expressions;
+//   FP64 form otherwise: the IEEE expressions 1/h, c/(2e), 1/(h*h);
+//   mixed form: FP32 arithmetic (IEEE division) on the spacings rounded to
+//     FP32 on the integer pipes -- an FP64->FP32 conversion instruction, like
+//     an FP64 division, occupies the FP64 pipe, and per tile these cost more
+//     than the arithmetic of a still cell.
+template <typename R>
+__device__ __forceinline__ R geo_v(double h) { return Prec<R>::from_d(h); }
+template <typename R, bool kP2>
+__device__ __forceinline__ R geo_rcp(double h) {
+  if constexpr (Prec<R>::kMixed) {
+    return __frcp_rn(f64_to_f32(h));
+  } else {
+    return kP2 ? d_pow2_rcp(h) : 1.0 / h;
+  }
+}
+template <typename R, bool kP2>
+__device__ __forceinline__ R geo_half_ratio(double c, double e) {
+  if constexpr (Prec<R>::kMixed) {
+    return __fdiv_rn(f64_to_f32(c), 2.0f * f64_to_f32(e));
+  } else {
+    return kP2 ? d_pow2_half_ratio(c, e) : c / (2.0 * e);
+  }
+}
+// h/2 in bulk precision (exact).
+template <typename R>
+__device__ __forceinline__ R geo_half(double h) { return Prec<R>::from_d(d_half(h)); }
+// FP64 1/h for the coefficients of the FP64 conservative update: as geo_rcp
+// in the FP64 form; the MUFU reciprocal with two Newton steps in the mixed
+// form (whose fluxes are FP32).
+template <typename R, bool kP2>
+__device__ __forceinline__ double geo_rcp_d(double h) {
+  if constexpr (Prec<R>::kMixed) {
+    return d_rcp(h);
+  } else {
+    return kP2 ? d_pow2_rcp(h) : 1.0 / h;
+  }
+}
+// 1/(h*h), FP64 form only (CFL keys).
+template <bool kP2>
+__device__ __forceinline__ double geo_rcp_sq(double h) {
+  return kP2 ? d_pow2_rcp_sq(h) : 1.0 / (h * h);
+}
+
 // The FP64 quotient as a called function: a branch around five inline FP64
 // instructions is turned into predicated code, which occupies the FP64 pipe
 // even in lanes (and whole warps) that skip it; a call is a real branch.
@@ -204,21 +251,21 @@ __device__ __forceinline__ void tile_lag_pressure_impl(const StepArgs<R>& a, int
     const int ii = i0 + t;
     if (ii >= 1 && ii < ny) {
       const double ey = a.edgedy[ii];
-      s_ey[t] = R(ey);
-      s_iey[t] = R(1.0 / ey);
-      s_wy0[t] = R(a.celldy[ii] / (2.0 * ey));
-      s_wy1[t] = R(a.celldy[ii - 1] / (2.0 * ey));
+      s_ey[t] = geo_v<R>(ey);
+      s_iey[t] = geo_rcp<R, kP2>(ey);
+      s_wy0[t] = geo_half_ratio<R, kP2>(a.celldy[ii], ey);
+      s_wy1[t] = geo_half_ratio<R, kP2>(a.celldy[ii - 1], ey);
     }
   }
   R exr = R(0), iex = R(0), wx0 = R(0), wx1 = R(0);
   if (jj >= 1 && jj < nx) {
     const double ex = a.edgedx[jj];
-    exr = R(ex);
-    iex = R(1.0 / ex);
-    wx0 = R(a.celldx[jj] / (2.0 * ex));
-    wx1 = R(a.celldx[jj - 1] / (2.0 * ex));
+    exr = geo_v<R>(ex);
+    iex = geo_rcp<R, kP2>(ex);
+    wx0 = geo_half_ratio<R, kP2>(a.celldx[jj], ex);
+    wx1 = geo_half_ratio<R, kP2>(a.celldx[jj - 1], ex);
   }
-  const R dt = R(a.dt);
+  const R dt = Pr::from_d(a.dt);
   R P_dn = R(0), r_dn = R(0);  // cell (ii-1, jj)
   if (i0 >= 1 && jj < nx) {
     const size_t c = cidx(nx, i0 - 1, jj);
@@ -351,15 +398,15 @@ __device__ __forceinline__ void tile_lag_viscous_accel_impl(const StepArgs<R>& a
   if (threadIdx.x < a.rows) {
     const int ii = i0 + threadIdx.x;
     if (ii < ny) {
-      s_cy[threadIdx.x] = R(a.celldy[ii]);
-      s_icy[threadIdx.x] = R(1.0 / a.celldy[ii]);
+      s_cy[threadIdx.x] = geo_v<R>(a.celldy[ii]);
+      s_icy[threadIdx.x] = geo_rcp<R, kP2>(a.celldy[ii]);
     }
   }
   __syncthreads();
   if (jj >= nx + 1 - pad) return;
-  const R cx = R(a.celldx[jj]);
-  const R icx = R(1.0 / a.celldx[jj]);
-  const R dt = R(a.dt);
+  const R cx = geo_v<R>(a.celldx[jj]);
+  const R icx = geo_rcp<R, kP2>(a.celldx[jj]);
+  const R dt = Pr::from_d(a.dt);
   const int i1 = min(i0 + a.rows, ny + 1 - pad);
   R qy_dn = (jj < nx - pad) ? a.Qyy[cidx(nx, i0 - 1, jj)] : R(0);
   for (int ii = i0; ii < i1; ++ii) {
@@ -427,9 +474,9 @@ __device__ __forceinline__ void tile_lag_energy_dt_impl(const StepArgs<R>& a, in
   if (threadIdx.x < a.rows) {
     const int ii = i0 + threadIdx.x;
     if (ii < ny) {
-      s_cy[threadIdx.x] = R(a.celldy[ii]);
-      s_icy[threadIdx.x] = R(1.0 / a.celldy[ii]);
-      s_icy2[threadIdx.x] = 1.0 / (a.celldy[ii] * a.celldy[ii]);
+      s_cy[threadIdx.x] = geo_v<R>(a.celldy[ii]);
+      s_icy[threadIdx.x] = geo_rcp<R, kP2>(a.celldy[ii]);
+      if constexpr (!Pr::kMixed) s_icy2[threadIdx.x] = geo_rcp_sq<kP2>(a.celldy[ii]);
     }
   }
   __syncthreads();
@@ -438,10 +485,10 @@ __device__ __forceinline__ void tile_lag_energy_dt_impl(const StepArgs<R>& a, in
   long long kbest = -1;
   double s_best = 0.0, c_best = 0.0;
   if (jj < nx - pad) {
-    const R cx = R(a.celldx[jj]);
-    const R icx = R(1.0 / a.celldx[jj]);
-    const double icx2 = 1.0 / (a.celldx[jj] * a.celldx[jj]);
-    const R dt_h = R(a.dt_h);
+    const R cx = geo_v<R>(a.celldx[jj]);
+    const R icx = geo_rcp<R, kP2>(a.celldx[jj]);
+    const double icx2 = Pr::kMixed ? 0.0 : geo_rcp_sq<kP2>(a.celldx[jj]);
+    const R dt_h = Pr::from_d(a.dt_h);
     const int i1 = min(i0 + a.rows, ny - pad);
     R v0 = a.v[cidx(nx, i0, jj)];
     for (int ii = i0; ii < i1; ++ii) {
@@ -770,7 +817,8 @@ struct SweepArgs {
 template <typename R, bool kFirst, bool kP2>
 __device__ __forceinline__ void tile_mass_sweep_x_impl(const StepArgs<R>& a,
                                                        const SweepArgs<R>& s, int bx, int by) {
-  __shared__ R sF[kCols], seF[kCols];
+  using Pr = Prec<R>;
+  __shared__ R sF[kCols], seF[kCols], s_ey0r[kMaxRows];
   __shared__ double s_coef[kMaxRows], s_cyd[kMaxRows], s_ey0[kMaxRows], s_ey1[kMaxRows];
   const int nx = a.nx, ny = a.ny, pad = a.pad;
   const int t = threadIdx.x;
@@ -780,9 +828,10 @@ __device__ __forceinline__ void tile_mass_sweep_x_impl(const StepArgs<R>& a,
   if (t < a.rows) {
     const int ii = i0 + t;
     if (ii < ny - pad) {
-      s_coef[t] = 1.0 / a.celldy[ii];
+      s_coef[t] = geo_rcp_d<R, kP2>(a.celldy[ii]);
       s_cyd[t] = a.celldy[ii];
       s_ey0[t] = a.edgedy[ii];
+      s_ey0r[t] = geo_v<R>(a.edgedy[ii]);
       s_ey1[t] = a.edgedy[ii + 1];
     }
   }
@@ -792,13 +841,13 @@ __device__ __forceinline__ void tile_mass_sweep_x_impl(const StepArgs<R>& a,
   R iex = R(0), cxm = R(0), cx0 = R(0), icx_r = R(0);
   double icx = 0.0;
   if (face_ok) {
-    iex = R(1.0 / a.edgedx[jj]);
-    cxm = R(a.celldx[jj - 1]);
-    cx0 = R(a.celldx[jj]);
-    icx = 1.0 / a.celldx[jj];
-    icx_r = R(icx);
+    iex = geo_rcp<R, kP2>(a.edgedx[jj]);
+    cxm = geo_v<R>(a.celldx[jj - 1]);
+    cx0 = geo_v<R>(a.celldx[jj]);
+    icx = geo_rcp_d<R, kP2>(a.celldx[jj]);
+    icx_r = Pr::from_d(icx);
   }
-  const R dt_r = R(dt), dt_h_r = R(dt_h);
+  const R dt_r = Pr::from_d(dt), dt_h_r = Pr::from_d(dt_h);
   __syncthreads();
   const int i1 = min(i0 + a.rows, ny - pad);
   for (int ii = i0; ii < i1; ++ii) {
@@ -811,7 +860,7 @@ __device__ __forceinline__ void tile_mass_sweep_x_impl(const StepArgs<R>& a,
                                  s.r_in_r[c - 1], s.r_in_r[c], s.r_in_r[c + 1],
                                  s.e_in_r[c - 2], s.e_in_r[c - 1], s.e_in_r[c],
                                  s.e_in_r[c + 1], iex, cxm, cx0, icx_r,
-                                 R(s_ey0[k]), dt_r, dt_h_r, &F, &eF);
+                                 s_ey0r[k], dt_r, dt_h_r, &F, &eF);
       if (face_owner) {
         a.F_x[f] = F;
         mirror(a.F_x, nx + 1, ny, pad, ii, jj, F, true, false);
@@ -849,6 +898,7 @@ __device__ __forceinline__ void tile_mass_sweep_x(const StepArgs<R>& a, const Sw
 template <typename R, bool kFirst, bool kP2>
 __device__ __forceinline__ void tile_mass_sweep_y_impl(const StepArgs<R>& a,
                                                        const SweepArgs<R>& s, int bx, int by) {
+  using Pr = Prec<R>;
   __shared__ R s_iey[kMaxRows + 1], s_cy[kMaxRows + 2], s_icy[kMaxRows + 1];
   __shared__ double s_coef[kMaxRows], s_cyd[kMaxRows];
   const int nx = a.nx, ny = a.ny, pad = a.pad;
@@ -858,24 +908,24 @@ __device__ __forceinline__ void tile_mass_sweep_y_impl(const StepArgs<R>& a,
   // Face rows i0 .. i0+a.rows, cell rows i0-1 .. i0+a.rows.
   if (threadIdx.x < a.rows + 2) {
     const int ii = i0 - 1 + threadIdx.x;
-    if (ii < ny) s_cy[threadIdx.x] = R(a.celldy[ii]);
+    if (ii < ny) s_cy[threadIdx.x] = geo_v<R>(a.celldy[ii]);
   }
   if (threadIdx.x < a.rows + 1) {
     const int ii = i0 + threadIdx.x;
     if (ii < ny) {
-      s_iey[threadIdx.x] = R(1.0 / a.edgedy[ii]);
-      s_icy[threadIdx.x] = R(1.0 / a.celldy[ii]);
+      s_iey[threadIdx.x] = geo_rcp<R, kP2>(a.edgedy[ii]);
+      s_icy[threadIdx.x] = geo_rcp<R, kP2>(a.celldy[ii]);
       if (threadIdx.x < a.rows) {
-        s_coef[threadIdx.x] = 1.0 / a.celldy[ii];
+        s_coef[threadIdx.x] = geo_rcp_d<R, kP2>(a.celldy[ii]);
         s_cyd[threadIdx.x] = a.celldy[ii];
       }
     }
   }
   __syncthreads();
   if (jj >= nx - pad) return;
-  const double icx = 1.0 / a.celldx[jj];
+  const double icx = geo_rcp_d<R, kP2>(a.celldx[jj]);
   const double ex0 = a.edgedx[jj], ex1 = a.edgedx[jj + 1];
-  const R ex0_r = R(ex0), dt_r = R(dt), dt_h_r = R(dt_h);
+  const R ex0_r = geo_v<R>(ex0), dt_r = Pr::from_d(dt), dt_h_r = Pr::from_d(dt_h);
   const int i1 = min(i0 + a.rows, ny - pad);
   const int last_face = ny - pad;  // the north boundary face row
   // Windows at face row f: cells f-2..f+1 (densities and energies with their
@@ -979,13 +1029,13 @@ __device__ __forceinline__ void tile_flux_uFx_impl(const StepArgs<R>& a, int bx,
   const int jj = pad + bx * kCols + threadIdx.x;
   const int i0 = pad + by * a.rows;
   if (threadIdx.x < a.rows && i0 + (int)threadIdx.x < ny) {
-    s_hey[threadIdx.x] = R(a.edgedy[i0 + threadIdx.x] * 0.5);
+    s_hey[threadIdx.x] = geo_half<R>(a.edgedy[i0 + threadIdx.x]);
   }
   __syncthreads();
   if (jj >= nx - pad) return;
-  const R dt_h = R(a.dt_slot[1]);
-  const R iex = R(1.0 / a.edgedx[jj]);
-  const R cxl = R(a.celldx[jj - 1]), cxr = R(a.celldx[jj]);
+  const R dt_h = Prec<R>::from_d(a.dt_slot[1]);
+  const R iex = geo_rcp<R, kP2>(a.edgedx[jj]);
+  const R cxl = geo_v<R>(a.celldx[jj - 1]), cxr = geo_v<R>(a.celldx[jj]);
   const int i1 = min(i0 + a.rows, ny - pad);
   for (int ii = i0; ii < i1; ++ii) {
     const size_t f = fidx(nx, ii, jj);
@@ -1010,13 +1060,13 @@ __device__ __forceinline__ void tile_flux_uFy_impl(const StepArgs<R>& a, int bx,
   const int i0 = pad + by * a.rows;
   if (threadIdx.x < a.rows + 1) {
     const int ii = i0 - 1 + threadIdx.x;
-    if (ii < ny) s_cy[threadIdx.x] = R(a.celldy[ii]);
-    if (threadIdx.x >= 1 && ii < ny) s_iey[threadIdx.x - 1] = R(1.0 / a.edgedy[ii]);
+    if (ii < ny) s_cy[threadIdx.x] = geo_v<R>(a.celldy[ii]);
+    if (threadIdx.x >= 1 && ii < ny) s_iey[threadIdx.x - 1] = geo_rcp<R, kP2>(a.edgedy[ii]);
   }
   __syncthreads();
   if (jj >= nx + 1 - pad) return;
-  const R dt_h = R(a.dt_slot[1]);
-  const R hex = Prec<R>::half(R(a.edgedx[jj]));  // edgedx * 0.5
+  const R dt_h = Prec<R>::from_d(a.dt_slot[1]);
+  const R hex = geo_half<R>(a.edgedx[jj]);  // edgedx * 0.5
   const int i1 = min(i0 + a.rows, ny + 1 - pad);
   // u of rows ii-2 .. ii+1 around corner row ii, shifted down the column.
   ColWindow<R> uw;
@@ -1046,13 +1096,13 @@ __device__ __forceinline__ void tile_flux_vFx_impl(const StepArgs<R>& a, int bx,
   const int jj = pad + bx * kCols + threadIdx.x;
   const int i0 = pad + by * a.rows;
   if (threadIdx.x < a.rows && i0 + (int)threadIdx.x < ny) {
-    s_hcy[threadIdx.x] = R(a.celldy[i0 + threadIdx.x] * 0.5);
+    s_hcy[threadIdx.x] = geo_half<R>(a.celldy[i0 + threadIdx.x]);
   }
   __syncthreads();
   if (jj >= nx + 1 - pad) return;
-  const R dt_h = R(a.dt_slot[1]);
-  const R iex = R(1.0 / a.edgedx[jj]);
-  const R cxl = R(a.celldx[jj - 1]), cxr = R(a.celldx[jj]);
+  const R dt_h = Prec<R>::from_d(a.dt_slot[1]);
+  const R iex = geo_rcp<R, kP2>(a.edgedx[jj]);
+  const R cxl = geo_v<R>(a.celldx[jj - 1]), cxr = geo_v<R>(a.celldx[jj]);
   const int i1 = min(i0 + a.rows, ny + 1 - pad);
   R u_dn = a.u[fidx(nx, i0 - 1, jj)], F_dn = a.F_x[fidx(nx, i0 - 1, jj)];
   for (int ii = i0; ii < i1; ++ii) {
@@ -1081,13 +1131,13 @@ __device__ __forceinline__ void tile_flux_vFy_impl(const StepArgs<R>& a, int bx,
   const int i0 = pad + by * a.rows;
   if (threadIdx.x < a.rows + 1) {
     const int ii = i0 - 1 + threadIdx.x;
-    if (ii < ny) s_cy[threadIdx.x] = R(a.celldy[ii]);
-    if (threadIdx.x >= 1 && ii < ny) s_iey[threadIdx.x - 1] = R(1.0 / a.edgedy[ii]);
+    if (ii < ny) s_cy[threadIdx.x] = geo_v<R>(a.celldy[ii]);
+    if (threadIdx.x >= 1 && ii < ny) s_iey[threadIdx.x - 1] = geo_rcp<R, kP2>(a.edgedy[ii]);
   }
   __syncthreads();
   if (jj >= nx - pad) return;
-  const R dt_h = R(a.dt_slot[1]);
-  const R hcx = Prec<R>::half(R(a.celldx[jj]));  // celldx * 0.5
+  const R dt_h = Prec<R>::from_d(a.dt_slot[1]);
+  const R hcx = geo_half<R>(a.celldx[jj]);  // celldx * 0.5
   const int i1 = min(i0 + a.rows, ny - pad);
   // v of face rows ii-1 .. ii+2 around cell row ii, shifted down the column.
   ColWindow<R> vw;
@@ -1154,12 +1204,12 @@ __device__ __forceinline__ void tile_momentum_update_impl(const StepArgs<R>& a, 
       // Row factor of the flux divergence: 1/celldy for x fluxes of rho_u
       // and rho_v, 1/edgedy for the y fluxes.
       const double h = (kWhich == 0 || kWhich == 2) ? a.celldy[ii] : a.edgedy[ii];
-      s_h[threadIdx.x] = R(h);
-      s_row[threadIdx.x] = R(1.0 / h);
+      s_h[threadIdx.x] = geo_v<R>(h);
+      s_row[threadIdx.x] = geo_rcp<R, kP2>(h);
       if (!kU && kVel) {
         const double ey = a.edgedy[ii];
-        s_wy0[threadIdx.x] = R(a.celldy[ii] / (2.0 * ey));
-        s_wy1[threadIdx.x] = R(a.celldy[ii - 1] / (2.0 * ey));
+        s_wy0[threadIdx.x] = geo_half_ratio<R, kP2>(a.celldy[ii], ey);
+        s_wy1[threadIdx.x] = geo_half_ratio<R, kP2>(a.celldy[ii - 1], ey);
       }
     }
   }
@@ -1168,14 +1218,14 @@ __device__ __forceinline__ void tile_momentum_update_impl(const StepArgs<R>& a, 
   const int row_end = kU ? ny - pad : ny + 1 - pad;
   if (jj >= col_end) return;
   const double hx = (kWhich == 0 || kWhich == 2) ? a.edgedx[jj] : a.celldx[jj];
-  const R hx_r = R(hx);
-  const R ihx = R(1.0 / hx);
-  const R dt_h_r = R(dt_h);
+  const R hx_r = geo_v<R>(hx);
+  const R ihx = geo_rcp<R, kP2>(hx);
+  const R dt_h_r = Pr::from_d(dt_h);
   R wx0 = R(0), wx1 = R(0);
   if (kU && kVel) {
     const double ex = a.edgedx[jj];
-    wx0 = R(a.celldx[jj] / (2.0 * ex));
-    wx1 = R(a.celldx[jj - 1] / (2.0 * ex));
+    wx0 = geo_half_ratio<R, kP2>(a.celldx[jj], ex);
+    wx1 = geo_half_ratio<R, kP2>(a.celldx[jj - 1], ex);
   }
   const int i1 = min(i0 + a.rows, row_end);
   for (int ii = i0; ii < i1; ++ii) {

@@ -35,11 +35,12 @@ __device__ __forceinline__ long long ulp_gap(double a, double b) {
 // counts[0] d_half != x*0.5, [1] d_twice != x*2 (all bit patterns, NaN = NaN),
 // [2] d_is_pow2 wrong, [3] d_div != IEEE n/d, [4] d_rcp_for_qdiv + qdiv
 // != IEEE n/d, [5] d_mul_pow2(x, 2^k) != x*2^k (all bit patterns of x, k in
-// [-1022, 1023]); ulp[0], ulp[1] the largest gaps of [3], [4]; seed_err the
+// [-1022, 1023]); [6] the power-of-two quotients d_pow2_rcp, d_pow2_half_ratio,
+// d_pow2_rcp_sq != 1/p, x/(2p), 1/(p*p) (exponents over the whole range); ulp[0], ulp[1] the largest gaps of [3], [4]; seed_err the
 // largest |rcp.approx(d) d - 1| as FP64 bits.
 __global__ void k_check(long long n, unsigned long long seed, unsigned long long* counts,
                         unsigned long long* ulp, unsigned long long* seed_err) {
-  unsigned long long c[6] = {0, 0, 0, 0, 0, 0}, u0 = 0, u1 = 0, se = 0;
+  unsigned long long c[7] = {0, 0, 0, 0, 0, 0, 0}, u0 = 0, u1 = 0, se = 0;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x) {
     const unsigned long long h = mix64(seed ^ mix64((unsigned long long)i));
@@ -63,6 +64,13 @@ __global__ void k_check(long long n, unsigned long long seed, unsigned long long
                                    : (long long)((hp >> 3) % 2046) - 1022;
     const double pw = dfrom((kp + 1023) << 52);
     if (!same_value(d_mul_pow2(x, pw), __dmul_rn(x, pw))) ++c[5];
+    const unsigned long long hq = mix64(h + 4);
+    const long long kq = (hq & 7u) ? (long long)((hq >> 3) % 121) - 60
+                                   : (long long)((hq >> 3) % 2046) - 1022;
+    const double pq = dfrom((kq + 1023) << 52);
+    if (!same_value(d_pow2_rcp(pw), __ddiv_rn(1.0, pw))) ++c[6];
+    if (!same_value(d_pow2_half_ratio(pq, pw), __ddiv_rn(pq, __dmul_rn(2.0, pw)))) ++c[6];
+    if (!same_value(d_pow2_rcp_sq(pw), __ddiv_rn(1.0, __dmul_rn(pw, pw)))) ++c[6];
     const double nn = normal_from(mix64(h + 1)), dd = normal_from(mix64(h + 2));
     const double q = __ddiv_rn(nn, dd);
     const double qa = d_div(nn, dd);
@@ -84,7 +92,7 @@ __global__ void k_check(long long n, unsigned long long seed, unsigned long long
     const unsigned long long eb = (unsigned long long)dbits(err);
     se = eb > se ? eb : se;
   }
-  for (int k = 0; k < 6; ++k) {
+  for (int k = 0; k < 7; ++k) {
     if (c[k]) atomicAdd(&counts[k], c[k]);
   }
   atomicMax(&ulp[0], u0);
@@ -100,22 +108,22 @@ extern "C" int gb300_check_fp64_helpers(long long n, unsigned long long seed,
                                         double* max_seed_rel_err) {
   if (n <= 0 || !counts || !max_ulp || !max_seed_rel_err) return GB300_ERR_ARG;
   unsigned long long* d = nullptr;
-  if (cudaMalloc(&d, 9 * sizeof(unsigned long long)) != cudaSuccess) return GB300_ERR_CUDA;
-  cudaMemset(d, 0, 9 * sizeof(unsigned long long));
+  if (cudaMalloc(&d, 10 * sizeof(unsigned long long)) != cudaSuccess) return GB300_ERR_CUDA;
+  cudaMemset(d, 0, 10 * sizeof(unsigned long long));
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  flow::k_check<<<sms * 8, 256>>>(n, seed, d, d + 6, d + 8);
-  unsigned long long h[9];
+  flow::k_check<<<sms * 8, 256>>>(n, seed, d, d + 7, d + 9);
+  unsigned long long h[10];
   cudaError_t err = cudaMemcpy(h, d, sizeof(h), cudaMemcpyDeviceToHost);
   cudaFree(d);
   if (err == cudaSuccess) err = cudaGetLastError();
   if (err != cudaSuccess) return GB300_ERR_CUDA;
-  for (int k = 0; k < 6; ++k) counts[k] = (long long)h[k];
-  max_ulp[0] = (long long)h[6];
-  max_ulp[1] = (long long)h[7];
+  for (int k = 0; k < 7; ++k) counts[k] = (long long)h[k];
+  max_ulp[0] = (long long)h[7];
+  max_ulp[1] = (long long)h[8];
   double e;
-  memcpy(&e, &h[8], sizeof(e));
+  memcpy(&e, &h[9], sizeof(e));
   *max_seed_rel_err = e;
   return GB300_OK;
 }

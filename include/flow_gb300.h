@@ -319,6 +319,8 @@ int gb300_measure_fp64_fma_rate(double* fma_per_s);
  *   counts[3]  one-Newton-step quotient with one correction != IEEE n/d
  *   counts[4]  one-Newton-step reciprocal, then a corrected quotient != IEEE n/d
  *   counts[5]  x times a power of two on the integer pipes != IEEE product
+ *   counts[6]  1/p, x/(2p), 1/(p*p) of powers of two x, p from their
+ *              exponent fields != the IEEE expressions
  * max_ulp[0..1]: the largest gaps of counts[3..4] in units in the last
  * place; max_seed_rel_err: the largest |rcp.approx(d) * d - 1|. */
 int gb300_check_fp64_helpers(long long n, unsigned long long seed, long long* counts,
