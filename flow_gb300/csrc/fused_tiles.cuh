@@ -83,9 +83,12 @@ struct StepArgs {
 // its ghost mirror images (pad layers per side): column images negated when
 // flip_x, row images when flip_y, corner images by both.  This reproduces the
 // reflective fill of every ghost point whose mirror source is (ii, jj).
+// edge: the tile may hold such points (tile_near_edge); a tile away from the
+// walls skips the tests with one uniform branch.
 template <typename T>
-__device__ __forceinline__ void mirror(T* a, int w, int h, int pad, int ii,
+__device__ __forceinline__ void mirror(bool edge, T* a, int w, int h, int pad, int ii,
                                        int jj, T val, bool flip_x, bool flip_y) {
+  if (!edge) return;
   int mc[2], mr[2];
   int nc = 0, nr = 0;
   if (jj < 2 * pad) mc[nc++] = 2 * pad - 1 - jj;
@@ -106,16 +109,26 @@ __device__ __forceinline__ void mirror(T* a, int w, int h, int pad, int ii,
 // Stores an FP64 cell value, and its bulk-precision shadow in the mixed form,
 // with ghost mirrors.
 template <typename R>
-__device__ __forceinline__ void store_cell(double* a64, R* ar, int nx, int ny,
+__device__ __forceinline__ void store_cell(bool edge, double* a64, R* ar, int nx, int ny,
                                            int pad, int ii, int jj, double val) {
   const size_t c = cidx(nx, ii, jj);
   a64[c] = val;
-  mirror(a64, nx, ny, pad, ii, jj, val, false, false);
+  mirror(edge, a64, nx, ny, pad, ii, jj, val, false, false);
   if (Prec<R>::kMixed) {
     const R vr = Prec<R>::from_d(val);
     ar[c] = vr;
-    mirror(ar, nx, ny, pad, ii, jj, vr, false, false);
+    mirror(edge, ar, nx, ny, pad, ii, jj, vr, false, false);
   }
+}
+
+// True when a tile whose columns start at col0 and rows at row0 may write a
+// point within 2*pad of a wall of any array (so that mirror has images to
+// write): the tile's points lie in [col0, col0 + kCols) x [row0 - 1,
+// row0 + rows] (face rows included), tested with a margin.  Block-uniform.
+__device__ __forceinline__ bool tile_near_edge(int nx, int ny, int pad, int col0, int row0,
+                                               int rows) {
+  return !(col0 - 2 >= 2 * pad && col0 + kCols + 2 <= nx - 2 * pad && row0 - 2 >= 2 * pad &&
+           row0 + rows + 2 <= ny - 2 * pad);
 }
 
 // True when every mesh spacing (celldx, edgedx, celldy, edgedy) within two
@@ -246,6 +259,7 @@ __device__ __forceinline__ void tile_lag_pressure_impl(const StepArgs<R>& a, int
   const int t = threadIdx.x;
   const int jj = bx * kCols + t;
   const int i0 = by * a.rows;
+  const bool edge = tile_near_edge(nx, ny, pad, bx * kCols, i0, a.rows);
   const R g1 = R(kG1);
   if (t < a.rows) {
     const int ii = i0 + t;
@@ -311,7 +325,7 @@ __device__ __forceinline__ void tile_lag_pressure_impl(const StepArgs<R>& a, int
       const R vel = face_velocity(mom, rbar);
       a.u[f] = vel;
       a.uF_x[f] = rbar;
-      mirror(a.u, nx + 1, ny, pad, ii, jj, vel, true, false);
+      mirror(edge, a.u, nx + 1, ny, pad, ii, jj, vel, true, false);
     }
     if (ii >= pad && ii < ny + 1 - pad && jj >= pad && jj < nx - pad) {
       const size_t c = cidx(nx, ii, jj);
@@ -325,7 +339,7 @@ __device__ __forceinline__ void tile_lag_pressure_impl(const StepArgs<R>& a, int
       const R vel = face_velocity(mom, rbar);
       a.v[c] = vel;
       a.vF_y[c] = rbar;
-      mirror(a.v, nx, ny + 1, pad, ii, jj, vel, false, true);
+      mirror(edge, a.v, nx, ny + 1, pad, ii, jj, vel, false, true);
     }
     P_dn = Pc;
     r_dn = rc;
@@ -355,6 +369,7 @@ __device__ __forceinline__ void tile_lag_viscosity(const StepArgs<R>& a, int bx,
   const int nx = a.nx, ny = a.ny, pad = a.pad;
   const int jj = pad + bx * kCols + threadIdx.x;
   const int i0 = pad + by * a.rows;
+  const bool edge = tile_near_edge(nx, ny, pad, pad + bx * kCols, i0, a.rows);
   if (jj >= nx - pad) return;
   using Pr = Prec<R>;
   const int i1 = min(i0 + a.rows, ny - pad);
@@ -377,8 +392,8 @@ __device__ __forceinline__ void tile_lag_viscosity(const StepArgs<R>& a, int bx,
     const R qy = Pr::zero_skip(m1) ? R(0) : crho * m1 * Pr::half(g12 + g01);
     a.Qxx[c] = qx;
     a.Qyy[c] = qy;
-    mirror(a.Qxx, nx, ny, pad, ii, jj, qx, false, false);
-    mirror(a.Qyy, nx, ny, pad, ii, jj, qy, false, false);
+    mirror(edge, a.Qxx, nx, ny, pad, ii, jj, qx, false, false);
+    mirror(edge, a.Qyy, nx, ny, pad, ii, jj, qy, false, false);
     m0 = m1;
     m1 = m2;
     g01 = g12;
@@ -395,6 +410,7 @@ __device__ __forceinline__ void tile_lag_viscous_accel_impl(const StepArgs<R>& a
   const int nx = a.nx, ny = a.ny, pad = a.pad;
   const int jj = pad + bx * kCols + threadIdx.x;
   const int i0 = pad + by * a.rows;
+  const bool edge = tile_near_edge(nx, ny, pad, pad + bx * kCols, i0, a.rows);
   if (threadIdx.x < a.rows) {
     const int ii = i0 + threadIdx.x;
     if (ii < ny) {
@@ -422,7 +438,7 @@ __device__ __forceinline__ void tile_lag_viscous_accel_impl(const StepArgs<R>& a
         const R vel = face_velocity(mom, a.uF_x[f]);
         a.rho_u[f] = mom;
         a.u[f] = vel;
-        mirror(a.u, nx + 1, ny, pad, ii, jj, vel, true, false);
+        mirror(edge, a.u, nx + 1, ny, pad, ii, jj, vel, true, false);
       }
     }
     if (jj < nx - pad) {
@@ -434,7 +450,7 @@ __device__ __forceinline__ void tile_lag_viscous_accel_impl(const StepArgs<R>& a
         const R vel = face_velocity(mom, a.vF_y[c]);
         a.rho_v[c] = mom;
         a.v[c] = vel;
-        mirror(a.v, nx, ny + 1, pad, ii, jj, vel, false, true);
+        mirror(edge, a.v, nx, ny + 1, pad, ii, jj, vel, false, true);
       }
       qy_dn = qy;
     }
@@ -471,6 +487,7 @@ __device__ __forceinline__ void tile_lag_energy_dt_impl(const StepArgs<R>& a, in
   const int nx = a.nx, ny = a.ny, pad = a.pad;
   const int jj = pad + bx * kCols + threadIdx.x;
   const int i0 = pad + by * a.rows;
+  const bool edge = tile_near_edge(nx, ny, pad, pad + bx * kCols, i0, a.rows);
   if (threadIdx.x < a.rows) {
     const int ii = i0 + threadIdx.x;
     if (ii < ny) {
@@ -526,7 +543,7 @@ __device__ __forceinline__ void tile_lag_energy_dt_impl(const StepArgs<R>& a, in
           e_new = rz ? 0.0 : double(e_q - work);
         }
       }
-      store_cell(a.e, a.e_r, nx, ny, pad, ii, jj, e_new);
+      store_cell(edge, a.e, a.e_r, nx, ny, pad, ii, jj, e_new);
       // CFL: celldx / sqrt(c_s^2 + 2 Q / rho) with c_s^2 = gamma (gamma-1) e.
       // The reference squares c_s = sqrt(gamma (gamma-1) e), so a cell whose
       // energy went negative gives a NaN candidate whatever Q is, and its dt
@@ -750,7 +767,8 @@ __device__ __forceinline__ void mass_energy_flux(R vm, R v0, R vp, R rm2,
 
 // Conservative FP64 update of one cell from its two face fluxes (given in
 // bulk precision, converted exactly): vol = celldx*celldy and ivol its
-// reciprocal, a0/a1 the face lengths.  den is rho_old in the first sweep of a step and the new
+// reciprocal (in the mixed form ivol is dt_h/vol: the sweeps fold dt_h into
+// their row factors), a0/a1 the face lengths.  den is rho_old in the first sweep of a step and the new
 // density in the second (omp3/flow.c:416-432).  The FP64 form keeps the
 // reference's evaluation order; the mixed form contracts into FMAs.
 template <typename R, bool kFirst, bool kP2>
@@ -770,7 +788,7 @@ __device__ __forceinline__ void mass_energy_update(double r_in, double e_in,
       r_new = r_in;
       rho_e = r_old * e_in;
     } else {
-      const double coef = dt_h * ivol;
+      const double coef = ivol;
       r_new = fma(-coef, fma(a1, f1, -(a0 * f0)), r_in);
       rho_e = fma(-coef, de, r_old * e_in);
     }
@@ -824,11 +842,14 @@ __device__ __forceinline__ void tile_mass_sweep_x_impl(const StepArgs<R>& a,
   const int t = threadIdx.x;
   const int jj = pad + bx * (kCols - 1) + t;  // face (and cell) column
   const int i0 = pad + by * a.rows;
+  const bool edge = tile_near_edge(nx, ny, pad, pad + bx * (kCols - 1), i0, a.rows);
   const double dt = a.dt_slot[0], dt_h = a.dt_slot[1];
   if (t < a.rows) {
     const int ii = i0 + t;
     if (ii < ny - pad) {
-      s_coef[t] = geo_rcp_d<R, kP2>(a.celldy[ii]);
+      // Row factor of the update: 1/celldy, times dt_h in the mixed form.
+      s_coef[t] = Pr::kMixed ? dt_h * geo_rcp_d<R, kP2>(a.celldy[ii])
+                             : geo_rcp_d<R, kP2>(a.celldy[ii]);
       s_cyd[t] = a.celldy[ii];
       s_ey0[t] = a.edgedy[ii];
       s_ey0r[t] = geo_v<R>(a.edgedy[ii]);
@@ -863,7 +884,7 @@ __device__ __forceinline__ void tile_mass_sweep_x_impl(const StepArgs<R>& a,
                                  s_ey0r[k], dt_r, dt_h_r, &F, &eF);
       if (face_owner) {
         a.F_x[f] = F;
-        mirror(a.F_x, nx + 1, ny, pad, ii, jj, F, true, false);
+        mirror(edge, a.F_x, nx + 1, ny, pad, ii, jj, F, true, false);
       }
     }
     sF[t] = F;
@@ -878,8 +899,8 @@ __device__ __forceinline__ void tile_mass_sweep_x_impl(const StepArgs<R>& a,
                                          Prec<double>::mulp<kP2>(s_coef[k], icx),
                                          s_ey0[k], s_ey1[k], sF[t],
                                          sF[t + 1], seF[t], seF[t + 1], &r_new, &e_new);
-      store_cell(s.r_out, s.r_out_r, nx, ny, pad, ii, jj, r_new);
-      store_cell(s.e_out, s.e_out_r, nx, ny, pad, ii, jj, e_new);
+      store_cell(edge, s.r_out, s.r_out_r, nx, ny, pad, ii, jj, r_new);
+      store_cell(edge, s.e_out, s.e_out_r, nx, ny, pad, ii, jj, e_new);
     }
     __syncthreads();
   }
@@ -904,6 +925,7 @@ __device__ __forceinline__ void tile_mass_sweep_y_impl(const StepArgs<R>& a,
   const int nx = a.nx, ny = a.ny, pad = a.pad;
   const int jj = pad + bx * kCols + threadIdx.x;
   const int i0 = pad + by * a.rows;
+  const bool edge = tile_near_edge(nx, ny, pad, pad + bx * kCols, i0, a.rows);
   const double dt = a.dt_slot[0], dt_h = a.dt_slot[1];
   // Face rows i0 .. i0+a.rows, cell rows i0-1 .. i0+a.rows.
   if (threadIdx.x < a.rows + 2) {
@@ -916,7 +938,8 @@ __device__ __forceinline__ void tile_mass_sweep_y_impl(const StepArgs<R>& a,
       s_iey[threadIdx.x] = geo_rcp<R, kP2>(a.edgedy[ii]);
       s_icy[threadIdx.x] = geo_rcp<R, kP2>(a.celldy[ii]);
       if (threadIdx.x < a.rows) {
-        s_coef[threadIdx.x] = geo_rcp_d<R, kP2>(a.celldy[ii]);
+        s_coef[threadIdx.x] = Pr::kMixed ? dt_h * geo_rcp_d<R, kP2>(a.celldy[ii])
+                                         : geo_rcp_d<R, kP2>(a.celldy[ii]);
         s_cyd[threadIdx.x] = a.celldy[ii];
       }
     }
@@ -962,7 +985,7 @@ __device__ __forceinline__ void tile_mass_sweep_y_impl(const StepArgs<R>& a,
   {
     const size_t c = cidx(nx, i0, jj);
     a.F_y[c] = F0;
-    mirror(a.F_y, nx, ny + 1, pad, i0, jj, F0, false, true);
+    mirror(edge, a.F_y, nx, ny + 1, pad, i0, jj, F0, false, true);
   }
   for (int ii = i0; ii < i1; ++ii) {
     const int k = ii - i0;
@@ -984,7 +1007,7 @@ __device__ __forceinline__ void tile_mass_sweep_y_impl(const StepArgs<R>& a,
     if (ii + 1 < i1 || ii + 1 == last_face) {
       const size_t c = cidx(nx, ii + 1, jj);
       a.F_y[c] = F1;
-      mirror(a.F_y, nx, ny + 1, pad, ii + 1, jj, F1, false, true);
+      mirror(edge, a.F_y, nx, ny + 1, pad, ii + 1, jj, F1, false, true);
     }
     const size_t c = cidx(nx, ii, jj);
     const double r_old = kFirst ? s.r_in[c] : a.rho[c];
@@ -993,8 +1016,8 @@ __device__ __forceinline__ void tile_mass_sweep_y_impl(const StepArgs<R>& a,
                                        a.celldx[jj] * s_cyd[k],
                                        Prec<double>::mulp<kP2>(s_coef[k], icx), ex0, ex1,
                                        F0, F1, eF0, eF1, &r_new, &e_new);
-    store_cell(s.r_out, s.r_out_r, nx, ny, pad, ii, jj, r_new);
-    store_cell(s.e_out, s.e_out_r, nx, ny, pad, ii, jj, e_new);
+    store_cell(edge, s.r_out, s.r_out_r, nx, ny, pad, ii, jj, r_new);
+    store_cell(edge, s.e_out, s.e_out_r, nx, ny, pad, ii, jj, e_new);
     F0 = F1;
     eF0 = eF1;
   }
@@ -1028,6 +1051,7 @@ __device__ __forceinline__ void tile_flux_uFx_impl(const StepArgs<R>& a, int bx,
   const int nx = a.nx, ny = a.ny, pad = a.pad;
   const int jj = pad + bx * kCols + threadIdx.x;
   const int i0 = pad + by * a.rows;
+  const bool edge = tile_near_edge(nx, ny, pad, pad + bx * kCols, i0, a.rows);
   if (threadIdx.x < a.rows && i0 + (int)threadIdx.x < ny) {
     s_hey[threadIdx.x] = geo_half<R>(a.edgedy[i0 + threadIdx.x]);
   }
@@ -1047,7 +1071,7 @@ __device__ __forceinline__ void tile_flux_uFx_impl(const StepArgs<R>& a, int bx,
                       : mass * momentum_upwind<R, kP2>(Prec<R>::half(u0 + u1), a.u[f - 1], u0, u1,
                                                        a.u[f + 2], iex, cxl, cxr, dt_h);
     a.uF_x[cidx(nx, ii, jj)] = val;
-    mirror(a.uF_x, nx, ny, pad, ii, jj, val, false, false);
+    mirror(edge, a.uF_x, nx, ny, pad, ii, jj, val, false, false);
   }
 }
 
@@ -1058,6 +1082,7 @@ __device__ __forceinline__ void tile_flux_uFy_impl(const StepArgs<R>& a, int bx,
   const int nx = a.nx, ny = a.ny, pad = a.pad;
   const int jj = pad + bx * kCols + threadIdx.x;
   const int i0 = pad + by * a.rows;
+  const bool edge = tile_near_edge(nx, ny, pad, pad + bx * kCols, i0, a.rows);
   if (threadIdx.x < a.rows + 1) {
     const int ii = i0 - 1 + threadIdx.x;
     if (ii < ny) s_cy[threadIdx.x] = geo_v<R>(a.celldy[ii]);
@@ -1083,7 +1108,7 @@ __device__ __forceinline__ void tile_flux_uFy_impl(const StepArgs<R>& a, int bx,
       val = mass * uw.template face<kP2>(pos, s_iey[k], pos ? s_cy[k] : s_cy[k + 1], wind * dt_h);
     }
     a.uF_y[fidx(nx, ii, jj)] = val;
-    mirror(a.uF_y, nx + 1, ny + 1, pad, ii, jj, val, false, false);
+    mirror(edge, a.uF_y, nx + 1, ny + 1, pad, ii, jj, val, false, false);
     if (ii + 1 < i1) uw.shift(a.u[fidx(nx, ii + 2, jj)]);
   }
 }
@@ -1095,6 +1120,7 @@ __device__ __forceinline__ void tile_flux_vFx_impl(const StepArgs<R>& a, int bx,
   const int nx = a.nx, ny = a.ny, pad = a.pad;
   const int jj = pad + bx * kCols + threadIdx.x;
   const int i0 = pad + by * a.rows;
+  const bool edge = tile_near_edge(nx, ny, pad, pad + bx * kCols, i0, a.rows);
   if (threadIdx.x < a.rows && i0 + (int)threadIdx.x < ny) {
     s_hcy[threadIdx.x] = geo_half<R>(a.celldy[i0 + threadIdx.x]);
   }
@@ -1116,7 +1142,7 @@ __device__ __forceinline__ void tile_flux_vFx_impl(const StepArgs<R>& a, int bx,
                                                        a.v[c - 1], a.v[c], a.v[c + 1], iex, cxl,
                                                        cxr, dt_h);
     a.vF_x[f] = val;
-    mirror(a.vF_x, nx + 1, ny + 1, pad, ii, jj, val, false, false);
+    mirror(edge, a.vF_x, nx + 1, ny + 1, pad, ii, jj, val, false, false);
     u_dn = u0;
     F_dn = F0;
   }
@@ -1129,6 +1155,7 @@ __device__ __forceinline__ void tile_flux_vFy_impl(const StepArgs<R>& a, int bx,
   const int nx = a.nx, ny = a.ny, pad = a.pad;
   const int jj = pad + bx * kCols + threadIdx.x;
   const int i0 = pad + by * a.rows;
+  const bool edge = tile_near_edge(nx, ny, pad, pad + bx * kCols, i0, a.rows);
   if (threadIdx.x < a.rows + 1) {
     const int ii = i0 - 1 + threadIdx.x;
     if (ii < ny) s_cy[threadIdx.x] = geo_v<R>(a.celldy[ii]);
@@ -1155,7 +1182,7 @@ __device__ __forceinline__ void tile_flux_vFy_impl(const StepArgs<R>& a, int bx,
       val = mass * vw.template face<kP2>(pos, s_iey[k], pos ? s_cy[k] : s_cy[k + 1], wind * dt_h);
     }
     a.vF_y[cidx(nx, ii, jj)] = val;
-    mirror(a.vF_y, nx, ny, pad, ii, jj, val, false, false);
+    mirror(edge, a.vF_y, nx, ny, pad, ii, jj, val, false, false);
     if (ii + 1 < i1) vw.shift(a.v[cidx(nx, ii + 3, jj)]);
     F0 = F1;
   }
@@ -1197,6 +1224,7 @@ __device__ __forceinline__ void tile_momentum_update_impl(const StepArgs<R>& a, 
   const int nx = a.nx, ny = a.ny, pad = a.pad;
   const int jj = pad + bx * kCols + threadIdx.x;
   const int i0 = pad + by * a.rows;
+  const bool edge = tile_near_edge(nx, ny, pad, pad + bx * kCols, i0, a.rows);
   const double dt_h = a.dt_slot[1];
   if (threadIdx.x < a.rows) {
     const int ii = i0 + threadIdx.x;
@@ -1253,10 +1281,10 @@ __device__ __forceinline__ void tile_momentum_update_impl(const StepArgs<R>& a, 
       const R vel = face_velocity(m, rbar);
       if (kU) {
         a.u[f] = vel;
-        mirror(a.u, nx + 1, ny, pad, ii, jj, vel, true, false);
+        mirror(edge, a.u, nx + 1, ny, pad, ii, jj, vel, true, false);
       } else {
         a.v[c] = vel;
-        mirror(a.v, nx, ny + 1, pad, ii, jj, vel, false, true);
+        mirror(edge, a.v, nx, ny + 1, pad, ii, jj, vel, false, true);
       }
     }
   }
