@@ -121,6 +121,12 @@ __device__ __forceinline__ void store_cell(bool edge, double* a64, R* ar, int nx
   }
 }
 
+// pred holds in every active lane of the warp (a warp-uniform branch
+// condition).
+__device__ __forceinline__ bool warp_all(bool pred) {
+  return __all_sync(__activemask(), pred) != 0;
+}
+
 // True when a tile whose columns start at col0 and rows at row0 may write a
 // point within 2*pad of a wall of any array (so that mirror has images to
 // write): the tile's points lie in [col0, col0 + kCols) x [row0 - 1,
@@ -659,17 +665,25 @@ __device__ __forceinline__ R mc_face(bool pos, R m2, R m1, R p0, R p1, R inv_h, 
 // D1 = p0-m2, D2 = p1-m1.  A tile marching down the column shifts the window
 // by one value per row and forms only the two new differences (the others
 // are the same operands as before, so the same values).
+// push/refresh: shift the values alone and form all the differences later
+// (a tile that skips the rows where nothing moves).
 template <typename R>
 struct ColWindow {
-  R m1, p0, p1, d1, d2, d3, D1, D2;
+  R m2, m1, p0, p1, d1, d2, d3, D1, D2;
   __device__ __forceinline__ void init(R m2_, R m1_, R p0_, R p1_) {
-    m1 = m1_; p0 = p0_; p1 = p1_;
-    d1 = m1_ - m2_; d2 = p0_ - m1_; d3 = p1_ - p0_;
-    D1 = p0_ - m2_; D2 = p1_ - m1_;
+    m2 = m2_; m1 = m1_; p0 = p0_; p1 = p1_;
+    refresh();
+  }
+  __device__ __forceinline__ void refresh() {
+    d1 = m1 - m2; d2 = p0 - m1; d3 = p1 - p0;
+    D1 = p0 - m2; D2 = p1 - m1;
+  }
+  __device__ __forceinline__ void push(R next) {
+    m2 = m1; m1 = p0; p0 = p1; p1 = next;
   }
   __device__ __forceinline__ void shift(R next) {
     const R D2n = next - p0, d3n = next - p1;
-    m1 = p0; p0 = p1; p1 = next;
+    m2 = m1; m1 = p0; p0 = p1; p1 = next;
     d1 = d2; d2 = d3; d3 = d3n;
     D1 = D2; D2 = D2n;
   }
@@ -684,14 +698,20 @@ struct ColWindow {
 // The one-step differences only (d1, d2, d3) of a marching column window.
 template <typename R>
 struct ColSteps {
-  R m1, p0, p1, d1, d2, d3;
+  R m2, m1, p0, p1, d1, d2, d3;
   __device__ __forceinline__ void init(R m2_, R m1_, R p0_, R p1_) {
-    m1 = m1_; p0 = p0_; p1 = p1_;
-    d1 = m1_ - m2_; d2 = p0_ - m1_; d3 = p1_ - p0_;
+    m2 = m2_; m1 = m1_; p0 = p0_; p1 = p1_;
+    refresh();
+  }
+  __device__ __forceinline__ void refresh() {
+    d1 = m1 - m2; d2 = p0 - m1; d3 = p1 - p0;
+  }
+  __device__ __forceinline__ void push(R next) {
+    m2 = m1; m1 = p0; p0 = p1; p1 = next;
   }
   __device__ __forceinline__ void shift(R next) {
     const R d3n = next - p1;
-    m1 = p0; p0 = p1; p1 = next;
+    m2 = m1; m1 = p0; p0 = p1; p1 = next;
     d1 = d2; d2 = d3; d3 = d3n;
   }
 };
@@ -771,6 +791,18 @@ __device__ __forceinline__ void mass_energy_flux(R vm, R v0, R vp, R rm2,
 // their row factors), a0/a1 the face lengths.  den is rho_old in the first sweep of a step and the new
 // density in the second (omp3/flow.c:416-432).  The FP64 form keeps the
 // reference's evaluation order; the mixed form contracts into FMAs.
+// The quotient rho_e / den of an update as a called function, for warps
+// whose cells take no flux but whose energies do not come back exactly: a
+// short FP64 sequence under a branch is turned into predicated code that
+// still occupies the FP64 pipe, while a call is a real branch.
+static __device__ __noinline__ double still_quotient(double n, double d) { return d_div(n, d); }
+template <typename R>
+static __device__ __noinline__ double still_quotient_mixed(double n, double d) {
+  const double r0 = Prec<R>::to_d(Prec<R>::rcp(Prec<R>::from_d(d)));
+  const double q = n * r0;
+  return fma(r0, fma(-d, q, n), q);
+}
+
 template <typename R, bool kFirst, bool kP2>
 __device__ __forceinline__ void mass_energy_update(double r_in, double e_in,
                                                    double r_old, double dt_h,
@@ -779,19 +811,34 @@ __device__ __forceinline__ void mass_energy_update(double r_in, double e_in,
                                                    R eF1, double* r_out,
                                                    double* e_out) {
   using Pr = Prec<R>;
+  // No mass or energy crosses any cell of the warp (a warp-uniform test): the
+  // updates subtract zeros, the density stays and the energy takes the
+  // reference's rho_old*e/den round trip -- which gives e itself when the
+  // product rho_old*e is exact and den is rho_old, as in the still background
+  // of a blast.  The FP64 form takes the per-lane skip below otherwise.
+  const bool none = warp_all(Pr::is_zero(F0) && Pr::is_zero(F1) &&
+                             (Pr::kMixed || (Pr::is_zero(eF0) && Pr::is_zero(eF1))));
+  if (none) {
+    const double rho_e = __dmul_rn(r_old, e_in);
+    const double den = kFirst ? r_old : r_in;
+    *r_out = r_in;
+    if (warp_all(d_is_zero(fma(r_old, e_in, -rho_e)) && dbits(den) == dbits(r_old) &&
+                 !d_is_zero(den))) {
+      *e_out = e_in;
+    } else if (d_is_zero(den)) {
+      *e_out = 0.0;
+    } else {
+      *e_out = Pr::kMixed ? still_quotient_mixed<R>(rho_e, den) : still_quotient(rho_e, den);
+    }
+    return;
+  }
   const double f0 = Pr::to_d(F0), f1 = Pr::to_d(F1);
   const double de = Pr::to_d(eF1) - Pr::to_d(eF0);
   double r_new, rho_e;
   if (Pr::kMixed) {
-    if (Pr::zero_skip_coarse(F0) && Pr::zero_skip_coarse(F1)) {
-      // No flux through any cell of the warp: the updates subtract zeros.
-      r_new = r_in;
-      rho_e = r_old * e_in;
-    } else {
-      const double coef = ivol;
-      r_new = fma(-coef, fma(a1, f1, -(a0 * f0)), r_in);
-      rho_e = fma(-coef, de, r_old * e_in);
-    }
+    const double coef = ivol;
+    r_new = fma(-coef, fma(a1, f1, -(a0 * f0)), r_in);
+    rho_e = fma(-coef, de, r_old * e_in);
   } else if (Pr::zero_skip(f0) && Pr::zero_skip(f1) && Pr::zero_skip(de)) {
     // Nothing crosses the cell's faces: the updates subtract zeros.  (The
     // energy still takes the reference's rho_old*e/den round trip below.)
@@ -953,9 +1000,17 @@ __device__ __forceinline__ void tile_mass_sweep_y_impl(const StepArgs<R>& a,
   const int last_face = ny - pad;  // the north boundary face row
   // Windows at face row f: cells f-2..f+1 (densities and energies with their
   // differences), face velocities f-1..f+1 with theirs; each row shifts them
-  // by one and forms only the new differences.
+  // by one and forms only the new differences.  In the FP64 form a face row
+  // at rest in the whole warp carries no flux, and its differences are not
+  // formed: the windows shift their values alone (stale differences) and
+  // form all the differences again at the next row that moves -- the same
+  // operands, so the same values.
   ColSteps<R> rw;
   ColWindow<R> ew;
+  R vm = a.v[cidx(nx, i0 - 1, jj)];
+  R v0 = a.v[cidx(nx, i0, jj)];
+  R vp = a.v[cidx(nx, i0 + 1, jj)];
+  R dvm, dvp, dv2;
   {
     R r[4], e[4];
     for (int q = 0; q < 4; ++q) {
@@ -963,13 +1018,21 @@ __device__ __forceinline__ void tile_mass_sweep_y_impl(const StepArgs<R>& a,
       r[q] = s.r_in_r[c];
       e[q] = s.e_in_r[c];
     }
-    rw.init(r[0], r[1], r[2], r[3]);
-    ew.init(e[0], e[1], e[2], e[3]);
+    rw.m2 = r[0]; rw.m1 = r[1]; rw.p0 = r[2]; rw.p1 = r[3];
+    ew.m2 = e[0]; ew.m1 = e[1]; ew.p0 = e[2]; ew.p1 = e[3];
   }
-  R vm = a.v[cidx(nx, i0 - 1, jj)];
-  R v0 = a.v[cidx(nx, i0, jj)];
-  R vp = a.v[cidx(nx, i0 + 1, jj)];
-  R dvm = v0 - vm, dvp = vp - v0, dv2 = vp - vm;
+  auto refresh = [&]() {
+    rw.refresh();
+    ew.refresh();
+    dvm = v0 - vm;
+    dvp = vp - v0;
+    dv2 = vp - vm;
+  };
+  // Whether face row f (velocity v0) moves somewhere in the warp; always in
+  // the mixed form, whose FP32 differences cost less than the test.
+  auto moves = [&]() { return Pr::kMixed || !warp_all(Pr::is_zero(v0)); };
+  bool fresh = moves();
+  if (fresh) refresh();
   // Face row f = i0 + k: inverse spacing s_iey[k], cell widths s_cy[k] below
   // and s_cy[k + 1] above, downstream inverse width s_icy[k].
   auto flux_at = [&](int k, R* F, R* eF) {
@@ -980,8 +1043,8 @@ __device__ __forceinline__ void tile_mass_sweep_y_impl(const StepArgs<R>& a,
         },
         s_iey[k], s_icy[k], ex0_r, dt_r, dt_h_r, F, eF);
   };
-  R F0, eF0;
-  flux_at(0, &F0, &eF0);
+  R F0 = R(0), eF0 = R(0);
+  if (fresh) flux_at(0, &F0, &eF0);
   {
     const size_t c = cidx(nx, i0, jj);
     a.F_y[c] = F0;
@@ -990,20 +1053,35 @@ __device__ __forceinline__ void tile_mass_sweep_y_impl(const StepArgs<R>& a,
   for (int ii = i0; ii < i1; ++ii) {
     const int k = ii - i0;
     const size_t c_next = cidx(nx, ii + 2, jj);
-    rw.shift(s.r_in_r[c_next]);
-    ew.shift(s.e_in_r[c_next]);
-    {
-      const R vn = a.v[c_next];
-      const R dv2n = vn - v0, dvpn = vn - vp;
-      dvm = dvp;
-      dvp = dvpn;
-      dv2 = dv2n;
-      vm = v0;
-      v0 = vp;
-      vp = vn;
+    const R rn = s.r_in_r[c_next], en = s.e_in_r[c_next], vn = a.v[c_next];
+    R F1 = R(0), eF1 = R(0);
+    const bool was_fresh = fresh;
+    // Shift the velocity window's values; face row k+1 has velocity vp.
+    const R v_prev0 = v0, v_prevp = vp;
+    vm = v0;
+    v0 = vp;
+    vp = vn;
+    fresh = moves();
+    if (fresh) {
+      if (was_fresh) {
+        rw.shift(rn);
+        ew.shift(en);
+        const R dv2n = vn - v_prev0, dvpn = vn - v_prevp;
+        dvm = dvp;
+        dvp = dvpn;
+        dv2 = dv2n;
+      } else {
+        rw.push(rn);
+        ew.push(en);
+        refresh();
+      }
+      flux_at(k + 1, &F1, &eF1);
+    } else {
+      // A face row at rest carries no mass and no energy (+0, as the flux
+      // core returns for a face at rest).
+      rw.push(rn);
+      ew.push(en);
     }
-    R F1, eF1;
-    flux_at(k + 1, &F1, &eF1);
     if (ii + 1 < i1 || ii + 1 == last_face) {
       const size_t c = cidx(nx, ii + 1, jj);
       a.F_y[c] = F1;
