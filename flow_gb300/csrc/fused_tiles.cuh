@@ -127,6 +127,46 @@ __device__ __forceinline__ bool warp_all(bool pred) {
   return __all_sync(__activemask(), pred) != 0;
 }
 
+// FP64 form: a and b are the same finite number, so that a - b is +0 and
+// a + b is exactly 2a (tests on the bit patterns).  The mixed form's FP32
+// differences cost less than the tests, so it never takes these paths.
+template <typename R>
+__device__ __forceinline__ bool lane_same(R a, R b) {
+  if constexpr (Prec<R>::kMixed) {
+    return false;
+  } else {
+    return dbits(a) == dbits(b) && (dhi(a) & 0x7ff00000) != 0x7ff00000;
+  }
+}
+// lane_same in every active lane of the warp.
+template <typename R>
+__device__ __forceinline__ bool warp_same(R a, R b) {
+  if constexpr (Prec<R>::kMixed) {
+    return false;
+  } else {
+    return warp_all(lane_same(a, b));
+  }
+}
+// FP64 form: a and b are zeros in every active lane of the warp (then a + b
+// is the zero sum_zeros gives).
+template <typename R>
+__device__ __forceinline__ bool warp_zeros(R a, R b) {
+  if constexpr (Prec<R>::kMixed) {
+    return false;
+  } else {
+    return warp_all(d_is_zero(a) && d_is_zero(b));
+  }
+}
+// The IEEE sum of two zeros: -0 only when both are -0.
+template <typename R>
+__device__ __forceinline__ R sum_zeros(R a, R b) {
+  if constexpr (Prec<R>::kMixed) {
+    return __uint_as_float(__float_as_uint(a) & __float_as_uint(b));
+  } else {
+    return dfrom(dbits(a) & dbits(b));
+  }
+}
+
 // True when a tile whose columns start at col0 and rows at row0 may write a
 // point within 2*pad of a wall of any array (so that mirror has images to
 // write): the tile's points lie in [col0, col0 + kCols) x [row0 - 1,
@@ -321,13 +361,24 @@ __device__ __forceinline__ void tile_lag_pressure_impl(const StepArgs<R>& a, int
     __syncthreads();
     if (ii >= pad && ii < ny - pad && jj >= pad && jj < nx + 1 - pad) {
       const size_t f = fidx(nx, ii, jj);
-      const R dp = Pc - sP[t];
+      const R Pl = sP[t], rl = sR[t];
       R mom = a.rho_u[f];
-      if (!Pr::zero_skip(dp)) {
-        mom = Pr::template dsub<kP2>(mom, dt * dp, exr, iex);
-        a.rho_u[f] = mom;
+      R rbar;
+      // FP64 form, power-of-two tile: a warp whose faces all have equal
+      // pressures, densities and weights either side keeps its momenta
+      // (dp = +0) and has the face density 2 (rc wx0) exactly, without FP64
+      // instructions.
+      if (kP2 && !Pr::kMixed &&
+          warp_all(lane_same(Pc, Pl) && lane_same(rc, rl) && lane_same(wx0, wx1))) {
+        rbar = Pr::twice(Pr::template mulp<true>(rc, wx0));
+      } else {
+        const R dp = Pc - Pl;
+        if (!Pr::zero_skip(dp)) {
+          mom = Pr::template dsub<kP2>(mom, dt * dp, exr, iex);
+          a.rho_u[f] = mom;
+        }
+        rbar = face_average<R, kP2>(rc, wx0, rl, wx1);
       }
-      const R rbar = face_average<R, kP2>(rc, wx0, sR[t], wx1);
       const R vel = face_velocity(mom, rbar);
       a.u[f] = vel;
       a.uF_x[f] = rbar;
@@ -335,13 +386,19 @@ __device__ __forceinline__ void tile_lag_pressure_impl(const StepArgs<R>& a, int
     }
     if (ii >= pad && ii < ny + 1 - pad && jj >= pad && jj < nx - pad) {
       const size_t c = cidx(nx, ii, jj);
-      const R dp = Pc - P_dn;
       R mom = a.rho_v[c];
-      if (!Pr::zero_skip(dp)) {
-        mom = Pr::template dsub<kP2>(mom, dt * dp, s_ey[k], s_iey[k]);
-        a.rho_v[c] = mom;
+      R rbar;
+      if (kP2 && !Pr::kMixed &&
+          warp_all(lane_same(Pc, P_dn) && lane_same(rc, r_dn) && lane_same(s_wy0[k], s_wy1[k]))) {
+        rbar = Pr::twice(Pr::template mulp<true>(rc, s_wy0[k]));
+      } else {
+        const R dp = Pc - P_dn;
+        if (!Pr::zero_skip(dp)) {
+          mom = Pr::template dsub<kP2>(mom, dt * dp, s_ey[k], s_iey[k]);
+          a.rho_v[c] = mom;
+        }
+        rbar = face_average<R, kP2>(rc, s_wy0[k], r_dn, s_wy1[k]);
       }
-      const R rbar = face_average<R, kP2>(rc, s_wy0[k], r_dn, s_wy1[k]);
       const R vel = face_velocity(mom, rbar);
       a.v[c] = vel;
       a.vF_y[c] = rbar;
@@ -361,13 +418,16 @@ __device__ __forceinline__ void tile_lag_pressure(const StepArgs<R>& a, int bx, 
 
 // Artificial viscous stresses on interior cells, omp3/flow.c:173-207.
 template <typename R>
-__device__ __forceinline__ R visc_stress(R crho, R lo, R mid, R hi, R hi2) {
+__device__ __forceinline__ R visc_stress(R rho, R lo, R mid, R hi, R hi2) {
   using Pr = Prec<R>;
+  // Equal velocities either side of every cell of the warp: hi - mid = +0,
+  // no compression (the result below, without the FP64 instructions).
+  if (warp_same(hi, mid)) return R(0);
   const R m1 = Pr::min0(hi - mid);
   if (Pr::zero_skip(m1)) return R(0);  // no compression across the cell
   const R m0 = Pr::min0(mid - lo);
   const R m2 = Pr::min0(hi2 - hi);
-  return crho * m1 * Pr::half(Pr::abs(m2 - m1) + Pr::abs(m1 - m0));
+  return R(-kCQ) * rho * m1 * Pr::half(Pr::abs(m2 - m1) + Pr::abs(m1 - m0));
 }
 
 template <typename R>
@@ -391,11 +451,20 @@ __device__ __forceinline__ void tile_lag_viscosity(const StepArgs<R>& a, int bx,
     const R vp2 = a.v[cidx(nx, ii + 2, jj)];
     const size_t f = fidx(nx, ii, jj);
     const size_t c = cidx(nx, ii, jj);
-    const R crho = R(-kCQ) * a.rho_r[c];
-    const R qx = visc_stress(crho, a.u[f - 1], a.u[f], a.u[f + 1], a.u[f + 2]);
-    const R m2 = Pr::min0(vp2 - vp);
-    const R g12 = Pr::abs(m2 - m1);
-    const R qy = Pr::zero_skip(m1) ? R(0) : crho * m1 * Pr::half(g12 + g01);
+    const R rho = a.rho_r[c];
+    const R qx = visc_stress(rho, a.u[f - 1], a.u[f], a.u[f + 1], a.u[f + 2]);
+    R m2, g12, qy;
+    if (!Pr::kMixed && warp_all(lane_same(vp2, vp) && Pr::is_zero(m1))) {
+      // No jump of v across the cell or above it anywhere in the warp:
+      // m2 = min0(+0) = +0, g12 = |+0 - m1| = +0, no stress.
+      m2 = R(0);
+      g12 = R(0);
+      qy = R(0);
+    } else {
+      m2 = Pr::min0(vp2 - vp);
+      g12 = Pr::abs(m2 - m1);
+      qy = Pr::zero_skip(m1) ? R(0) : R(-kCQ) * rho * m1 * Pr::half(g12 + g01);
+    }
     a.Qxx[c] = qx;
     a.Qyy[c] = qy;
     mirror(edge, a.Qxx, nx, ny, pad, ii, jj, qx, false, false);
@@ -438,25 +507,30 @@ __device__ __forceinline__ void tile_lag_viscous_accel_impl(const StepArgs<R>& a
       const size_t c = cidx(nx, ii, jj);
       // No stress gradient: the momentum and the velocity from the pressure
       // phase stand as they are.
-      const R dqx = a.Qxx[c] - a.Qxx[c - 1];
-      if (!Pr::zero_skip(dqx)) {
-        const R mom = Pr::template dsub<kP2>(a.rho_u[f], dt * dqx, cx, icx);
-        const R vel = face_velocity(mom, a.uF_x[f]);
-        a.rho_u[f] = mom;
-        a.u[f] = vel;
-        mirror(edge, a.u, nx + 1, ny, pad, ii, jj, vel, true, false);
+      const R q1 = a.Qxx[c], q0 = a.Qxx[c - 1];
+      if (!warp_same(q1, q0)) {  // equal stresses in the whole warp: dqx = +0
+        const R dqx = q1 - q0;
+        if (!Pr::zero_skip(dqx)) {
+          const R mom = Pr::template dsub<kP2>(a.rho_u[f], dt * dqx, cx, icx);
+          const R vel = face_velocity(mom, a.uF_x[f]);
+          a.rho_u[f] = mom;
+          a.u[f] = vel;
+          mirror(edge, a.u, nx + 1, ny, pad, ii, jj, vel, true, false);
+        }
       }
     }
     if (jj < nx - pad) {
       const size_t c = cidx(nx, ii, jj);
       const R qy = a.Qyy[c];
-      const R dqy = qy - qy_dn;
-      if (!Pr::zero_skip(dqy)) {
-        const R mom = Pr::template dsub<kP2>(a.rho_v[c], dt * dqy, s_cy[k], s_icy[k]);
-        const R vel = face_velocity(mom, a.vF_y[c]);
-        a.rho_v[c] = mom;
-        a.v[c] = vel;
-        mirror(edge, a.v, nx, ny + 1, pad, ii, jj, vel, false, true);
+      if (!warp_same(qy, qy_dn)) {
+        const R dqy = qy - qy_dn;
+        if (!Pr::zero_skip(dqy)) {
+          const R mom = Pr::template dsub<kP2>(a.rho_v[c], dt * dqy, s_cy[k], s_icy[k]);
+          const R vel = face_velocity(mom, a.vF_y[c]);
+          a.rho_v[c] = mom;
+          a.v[c] = vel;
+          mirror(edge, a.v, nx, ny + 1, pad, ii, jj, vel, false, true);
+        }
       }
       qy_dn = qy;
     }
@@ -524,29 +598,38 @@ __device__ __forceinline__ void tile_lag_energy_dt_impl(const StepArgs<R>& a, in
       const R p = Pr::kMixed ? R(kG1) * r * er : R(a.P[c]);
       const R qx = a.Qxx[c], qy = a.Qyy[c];
       const bool rz = Pr::is_zero(r);
-      const R dudx = Pr::template mulp<kP2>(a.u[f + 1] - a.u[f], icx);
-      const R dvdy = Pr::template mulp<kP2>(v1 - v0, s_icy[k]);
+      const R u0f = a.u[f], u1f = a.u[f + 1];
       // A cell whose faces do not move relative to each other does no work
       // and takes no shock heating: every increment below is a zero, so e is
-      // left as it is (a cell at rest, or in uniform translation).
-      const bool still = Pr::zero_skip_coarse(dudx) && Pr::zero_skip_coarse(dvdy);
+      // left as it is (a cell at rest, or in uniform translation).  In the
+      // FP64 form a warp whose cells all have equal opposite face velocities
+      // (dudx = dvdy = +0) takes this without forming the differences.
       R inv_r = R(0);
       double e_new;
-      if (still) {
-        e_new = rz ? 0.0 : (Pr::kMixed ? a.e[c] : double(er));
+      bool still;
+      if (!Pr::kMixed && warp_all(lane_same(u1f, u0f) && lane_same(v1, v0))) {
+        still = true;
+        e_new = rz ? 0.0 : double(er);
       } else {
-        inv_r = rz ? R(0) : Pr::rcp(r);
-        const R div_dt = (dudx + dvdy) * dt_h;
-        // e_q = e - dt_h (Qxx dudx + Qyy dvdy) / rho, kept as an increment.
-        const R dq = -(dt_h * fma(qx, dudx, qy * dvdy)) * inv_r;
-        const R e_q = er + dq;
-        const R rho_c = r * Pr::rcp(R(1) + div_dt);
-        const R e_c = fma(-(p * div_dt), inv_r, e_q);
-        const R work = Pr::half(div_dt) * fma(R(kG1) * e_c, rho_c, p) * inv_r;
-        if (Pr::kMixed) {
-          e_new = rz ? 0.0 : a.e[c] + Pr::to_d(dq - work);
+        const R dudx = Pr::template mulp<kP2>(u1f - u0f, icx);
+        const R dvdy = Pr::template mulp<kP2>(v1 - v0, s_icy[k]);
+        still = Pr::zero_skip_coarse(dudx) && Pr::zero_skip_coarse(dvdy);
+        if (still) {
+          e_new = rz ? 0.0 : (Pr::kMixed ? a.e[c] : double(er));
         } else {
-          e_new = rz ? 0.0 : double(e_q - work);
+          inv_r = rz ? R(0) : Pr::rcp(r);
+          const R div_dt = (dudx + dvdy) * dt_h;
+          // e_q = e - dt_h (Qxx dudx + Qyy dvdy) / rho, kept as an increment.
+          const R dq = -(dt_h * fma(qx, dudx, qy * dvdy)) * inv_r;
+          const R e_q = er + dq;
+          const R rho_c = r * Pr::rcp(R(1) + div_dt);
+          const R e_c = fma(-(p * div_dt), inv_r, e_q);
+          const R work = Pr::half(div_dt) * fma(R(kG1) * e_c, rho_c, p) * inv_r;
+          if (Pr::kMixed) {
+            e_new = rz ? 0.0 : a.e[c] + Pr::to_d(dq - work);
+          } else {
+            e_new = rz ? 0.0 : double(e_q - work);
+          }
         }
       }
       store_cell(edge, a.e, a.e_r, nx, ny, pad, ii, jj, e_new);
@@ -1141,13 +1224,21 @@ __device__ __forceinline__ void tile_flux_uFx_impl(const StepArgs<R>& a, int bx,
   const int i1 = min(i0 + a.rows, ny - pad);
   for (int ii = i0; ii < i1; ++ii) {
     const size_t f = fidx(nx, ii, jj);
-    const R u0 = a.u[f], u1 = a.u[f + 1];
-    const R mass = Prec<R>::template mulp<kP2>(a.F_x[f] + a.F_x[f + 1], s_hey[ii - i0]);
-    // No mass through the cell, no momentum flux (the upwind value is skipped).
-    const R val = Prec<R>::zero_skip_coarse(mass)
-                      ? mass
-                      : mass * momentum_upwind<R, kP2>(Prec<R>::half(u0 + u1), a.u[f - 1], u0, u1,
-                                                       a.u[f + 2], iex, cxl, cxr, dt_h);
+    const R Fa = a.F_x[f], Fb = a.F_x[f + 1];
+    R val;
+    if (warp_zeros(Fa, Fb)) {
+      // FP64 form: no mass through any cell of the warp; the flux is the
+      // zero mass (a zero sum scaled by a positive spacing).
+      val = sum_zeros(Fa, Fb);
+    } else {
+      const R u0 = a.u[f], u1 = a.u[f + 1];
+      const R mass = Prec<R>::template mulp<kP2>(Fa + Fb, s_hey[ii - i0]);
+      // No mass through the cell, no momentum flux (the upwind value is skipped).
+      val = Prec<R>::zero_skip_coarse(mass)
+                ? mass
+                : mass * momentum_upwind<R, kP2>(Prec<R>::half(u0 + u1), a.u[f - 1], u0, u1,
+                                                 a.u[f + 2], iex, cxl, cxr, dt_h);
+    }
     a.uF_x[cidx(nx, ii, jj)] = val;
     mirror(edge, a.uF_x, nx, ny, pad, ii, jj, val, false, false);
   }
@@ -1172,22 +1263,45 @@ __device__ __forceinline__ void tile_flux_uFy_impl(const StepArgs<R>& a, int bx,
   const R hex = geo_half<R>(a.edgedx[jj]);  // edgedx * 0.5
   const int i1 = min(i0 + a.rows, ny + 1 - pad);
   // u of rows ii-2 .. ii+1 around corner row ii, shifted down the column.
+  // Its differences are formed when a row first needs them (fresh) and then
+  // carried while rows keep moving; rows without mass in the whole warp
+  // (FP64 form) shift the values alone.
   ColWindow<R> uw;
-  uw.init(a.u[fidx(nx, i0 - 2, jj)], a.u[fidx(nx, i0 - 1, jj)], a.u[fidx(nx, i0, jj)],
-          a.u[fidx(nx, i0 + 1, jj)]);
+  uw.m2 = a.u[fidx(nx, i0 - 2, jj)];
+  uw.m1 = a.u[fidx(nx, i0 - 1, jj)];
+  uw.p0 = a.u[fidx(nx, i0, jj)];
+  uw.p1 = a.u[fidx(nx, i0 + 1, jj)];
+  bool fresh = false;
   for (int ii = i0; ii < i1; ++ii) {
     const int k = ii - i0;
     const size_t c = cidx(nx, ii, jj);
-    const R mass = Prec<R>::template mulp<kP2>(a.F_y[c] + a.F_y[c - 1], hex);
-    R val = mass;
-    if (!Prec<R>::zero_skip_coarse(mass)) {
-      const R wind = Prec<R>::half(a.v[c - 1] + a.v[c]);
-      const bool pos = Prec<R>::gt0(wind);
-      val = mass * uw.template face<kP2>(pos, s_iey[k], pos ? s_cy[k] : s_cy[k + 1], wind * dt_h);
+    const R Fa = a.F_y[c], Fb = a.F_y[c - 1];
+    const bool moved = !warp_zeros(Fa, Fb);
+    R val;
+    if (!moved) {
+      val = sum_zeros(Fa, Fb);
+    } else {
+      if (!fresh) uw.refresh();
+      fresh = true;
+      const R mass = Prec<R>::template mulp<kP2>(Fa + Fb, hex);
+      val = mass;
+      if (!Prec<R>::zero_skip_coarse(mass)) {
+        const R wind = Prec<R>::half(a.v[c - 1] + a.v[c]);
+        const bool pos = Prec<R>::gt0(wind);
+        val = mass * uw.template face<kP2>(pos, s_iey[k], pos ? s_cy[k] : s_cy[k + 1], wind * dt_h);
+      }
     }
     a.uF_y[fidx(nx, ii, jj)] = val;
     mirror(edge, a.uF_y, nx + 1, ny + 1, pad, ii, jj, val, false, false);
-    if (ii + 1 < i1) uw.shift(a.u[fidx(nx, ii + 2, jj)]);
+    if (ii + 1 < i1) {
+      const R next = a.u[fidx(nx, ii + 2, jj)];
+      if (moved) {
+        uw.shift(next);
+      } else {
+        uw.push(next);
+        fresh = false;
+      }
+    }
   }
 }
 
@@ -1213,12 +1327,17 @@ __device__ __forceinline__ void tile_flux_vFx_impl(const StepArgs<R>& a, int bx,
     const size_t f = fidx(nx, ii, jj);
     const size_t c = cidx(nx, ii, jj);
     const R u0 = a.u[f], F0 = a.F_x[f];
-    const R mass = Prec<R>::template mulp<kP2>(F0 + F_dn, s_hcy[ii - i0]);
-    const R val = Prec<R>::zero_skip_coarse(mass)
-                      ? mass
-                      : mass * momentum_upwind<R, kP2>(Prec<R>::half(u0 + u_dn), a.v[c - 2],
-                                                       a.v[c - 1], a.v[c], a.v[c + 1], iex, cxl,
-                                                       cxr, dt_h);
+    R val;
+    if (warp_zeros(F0, F_dn)) {
+      val = sum_zeros(F0, F_dn);  // FP64 form: no mass through any corner of the warp
+    } else {
+      const R mass = Prec<R>::template mulp<kP2>(F0 + F_dn, s_hcy[ii - i0]);
+      val = Prec<R>::zero_skip_coarse(mass)
+                ? mass
+                : mass * momentum_upwind<R, kP2>(Prec<R>::half(u0 + u_dn), a.v[c - 2],
+                                                 a.v[c - 1], a.v[c], a.v[c + 1], iex, cxl,
+                                                 cxr, dt_h);
+    }
     a.vF_x[f] = val;
     mirror(edge, a.vF_x, nx + 1, ny + 1, pad, ii, jj, val, false, false);
     u_dn = u0;
@@ -1244,24 +1363,44 @@ __device__ __forceinline__ void tile_flux_vFy_impl(const StepArgs<R>& a, int bx,
   const R dt_h = Prec<R>::from_d(a.dt_slot[1]);
   const R hcx = geo_half<R>(a.celldx[jj]);  // celldx * 0.5
   const int i1 = min(i0 + a.rows, ny - pad);
-  // v of face rows ii-1 .. ii+2 around cell row ii, shifted down the column.
+  // v of face rows ii-1 .. ii+2 around cell row ii, shifted down the column,
+  // its differences formed lazily as in tile_flux_uFy.
   ColWindow<R> vw;
-  vw.init(a.v[cidx(nx, i0 - 1, jj)], a.v[cidx(nx, i0, jj)], a.v[cidx(nx, i0 + 1, jj)],
-          a.v[cidx(nx, i0 + 2, jj)]);
+  vw.m2 = a.v[cidx(nx, i0 - 1, jj)];
+  vw.m1 = a.v[cidx(nx, i0, jj)];
+  vw.p0 = a.v[cidx(nx, i0 + 1, jj)];
+  vw.p1 = a.v[cidx(nx, i0 + 2, jj)];
+  bool fresh = false;
   R F0 = a.F_y[cidx(nx, i0, jj)];
   for (int ii = i0; ii < i1; ++ii) {
     const int k = ii - i0;
     const R F1 = a.F_y[cidx(nx, ii + 1, jj)];
-    const R mass = Prec<R>::template mulp<kP2>(F0 + F1, hcx);
-    R val = mass;
-    if (!Prec<R>::zero_skip_coarse(mass)) {
-      const R wind = Prec<R>::half(vw.m1 + vw.p0);
-      const bool pos = Prec<R>::gt0(wind);
-      val = mass * vw.template face<kP2>(pos, s_iey[k], pos ? s_cy[k] : s_cy[k + 1], wind * dt_h);
+    const bool moved = !warp_zeros(F0, F1);
+    R val;
+    if (!moved) {
+      val = sum_zeros(F0, F1);
+    } else {
+      if (!fresh) vw.refresh();
+      fresh = true;
+      const R mass = Prec<R>::template mulp<kP2>(F0 + F1, hcx);
+      val = mass;
+      if (!Prec<R>::zero_skip_coarse(mass)) {
+        const R wind = Prec<R>::half(vw.m1 + vw.p0);
+        const bool pos = Prec<R>::gt0(wind);
+        val = mass * vw.template face<kP2>(pos, s_iey[k], pos ? s_cy[k] : s_cy[k + 1], wind * dt_h);
+      }
     }
     a.vF_y[cidx(nx, ii, jj)] = val;
     mirror(edge, a.vF_y, nx, ny, pad, ii, jj, val, false, false);
-    if (ii + 1 < i1) vw.shift(a.v[cidx(nx, ii + 3, jj)]);
+    if (ii + 1 < i1) {
+      const R next = a.v[cidx(nx, ii + 3, jj)];
+      if (moved) {
+        vw.shift(next);
+      } else {
+        vw.push(next);
+        fresh = false;
+      }
+    }
     F0 = F1;
   }
 }
@@ -1338,24 +1477,35 @@ __device__ __forceinline__ void tile_momentum_update_impl(const StepArgs<R>& a, 
     const int k = ii - i0;
     const size_t f = fidx(nx, ii, jj);
     const size_t c = cidx(nx, ii, jj);
-    R diff;
-    if (kWhich == 0) diff = a.uF_x[c] - a.uF_x[c - 1];
-    else if (kWhich == 1) diff = a.uF_y[f + (nx + 1)] - a.uF_y[f];
-    else if (kWhich == 2) diff = a.vF_x[f + 1] - a.vF_x[f];
-    else diff = a.vF_y[c] - a.vF_y[c - nx];
+    R fa, fb;  // the flux difference is fa - fb
+    if (kWhich == 0) { fa = a.uF_x[c]; fb = a.uF_x[c - 1]; }
+    else if (kWhich == 1) { fa = a.uF_y[f + (nx + 1)]; fb = a.uF_y[f]; }
+    else if (kWhich == 2) { fa = a.vF_x[f + 1]; fb = a.vF_x[f]; }
+    else { fa = a.vF_y[c]; fb = a.vF_y[c - nx]; }
     R* mom = kU ? a.rho_u + f : a.rho_v + c;
     // mom - dt_h * diff / (hx * hy), the divisor rounded as the reference
-    // forms it (omp3/flow.c:581-584); no flux difference, no change.
+    // forms it (omp3/flow.c:581-584); no flux difference, no change (in the
+    // FP64 form equal fluxes in the whole warp skip the difference too).
     R m = *mom;
-    if (!Pr::zero_skip(diff)) {
-      m = Pr::template dsub<kP2>(m, dt_h_r * diff, hx_r * s_h[k],
-                                 Pr::template mulp<kP2>(s_row[k], ihx));
-      *mom = m;
+    if (!warp_same(fa, fb)) {
+      const R diff = fa - fb;
+      if (!Pr::zero_skip(diff)) {
+        m = Pr::template dsub<kP2>(m, dt_h_r * diff, hx_r * s_h[k],
+                                   Pr::template mulp<kP2>(s_row[k], ihx));
+        *mom = m;
+      }
     }
     if (kVel) {
+      const R ra = a.rho_r[c], rb = kU ? a.rho_r[c - 1] : a.rho_r[c - nx];
+      const R w0 = kU ? wx0 : s_wy0[k], w1 = kU ? wx1 : s_wy1[k];
       R rbar;
-      if (kU) rbar = face_average<R, kP2>(a.rho_r[c], wx0, a.rho_r[c - 1], wx1);
-      else rbar = face_average<R, kP2>(a.rho_r[c], s_wy0[k], a.rho_r[c - nx], s_wy1[k]);
+      // FP64 form, power-of-two tile: equal densities and weights either
+      // side in the whole warp give the face density 2 (ra w0) exactly.
+      if (kP2 && !Pr::kMixed && warp_all(lane_same(ra, rb) && lane_same(w0, w1))) {
+        rbar = Pr::twice(Pr::template mulp<true>(ra, w0));
+      } else {
+        rbar = face_average<R, kP2>(ra, w0, rb, w1);
+      }
       const R vel = face_velocity(m, rbar);
       if (kU) {
         a.u[f] = vel;
