@@ -333,14 +333,36 @@ __device__ __forceinline__ void tile_lag_pressure_impl(const StepArgs<R>& a, int
     P_dn = g1 * r_dn * a.e_r[c];
   }
   __syncthreads();
+  // Row ii+1's densities, energies and face momenta are loaded before row ii
+  // is processed (its stores do not touch them).
+  const bool u_col = jj >= pad && jj < nx + 1 - pad;
+  const bool v_col = jj >= pad && jj < nx - pad;
+  R rc_n = R(0), ec_n = R(0), rl_n = R(0), el_n = R(0), mu_n = R(0), mv_n = R(0);
+  auto load = [&](int ii) {
+    if (jj < nx) {
+      const size_t c = cidx(nx, ii, jj);
+      rc_n = a.rho_r[c];
+      ec_n = a.e_r[c];
+    }
+    if (t == 0 && jj >= 1 && jj - 1 < nx) {
+      const size_t c = cidx(nx, ii, jj - 1);
+      rl_n = a.rho_r[c];
+      el_n = a.e_r[c];
+    }
+    if (u_col && ii >= pad && ii < ny - pad) mu_n = a.rho_u[fidx(nx, ii, jj)];
+    if (v_col && ii >= pad && ii < ny + 1 - pad) mv_n = a.rho_v[cidx(nx, ii, jj)];
+  };
+  if (i0 < ny) load(i0);
   for (int k = 0; k < a.rows; ++k) {
     const int ii = i0 + k;
     if (ii >= ny) break;
+    const R rc_l = rc_n, ec_l = ec_n, rl_l = rl_n, el_l = el_n, mu_l = mu_n, mv_l = mv_n;
+    if (k + 1 < a.rows && ii + 1 < ny) load(ii + 1);
     R Pc = R(0), rc = R(0);
     if (jj < nx) {
       const size_t c = cidx(nx, ii, jj);
-      rc = a.rho_r[c];
-      Pc = g1 * rc * a.e_r[c];
+      rc = rc_l;
+      Pc = g1 * rc * ec_l;
       if (!Pr::kMixed) {
         a.P[c] = double(Pc);
         a.rho_old[c] = double(rc);
@@ -351,9 +373,8 @@ __device__ __forceinline__ void tile_lag_pressure_impl(const StepArgs<R>& a, int
     if (t == 0) {
       R Pl = R(0), rl = R(0);
       if (jj >= 1 && jj - 1 < nx) {
-        const size_t c = cidx(nx, ii, jj - 1);
-        rl = a.rho_r[c];
-        Pl = g1 * rl * a.e_r[c];
+        rl = rl_l;
+        Pl = g1 * rl * el_l;
       }
       sP[0] = Pl;
       sR[0] = rl;
@@ -362,7 +383,7 @@ __device__ __forceinline__ void tile_lag_pressure_impl(const StepArgs<R>& a, int
     if (ii >= pad && ii < ny - pad && jj >= pad && jj < nx + 1 - pad) {
       const size_t f = fidx(nx, ii, jj);
       const R Pl = sP[t], rl = sR[t];
-      R mom = a.rho_u[f];
+      R mom = mu_l;
       R rbar;
       // FP64 form, power-of-two tile: a warp whose faces all have equal
       // pressures, densities and weights either side keeps its momenta
@@ -386,7 +407,7 @@ __device__ __forceinline__ void tile_lag_pressure_impl(const StepArgs<R>& a, int
     }
     if (ii >= pad && ii < ny + 1 - pad && jj >= pad && jj < nx - pad) {
       const size_t c = cidx(nx, ii, jj);
-      R mom = a.rho_v[c];
+      R mom = mv_l;
       R rbar;
       if (kP2 && !Pr::kMixed &&
           warp_all(lane_same(Pc, P_dn) && lane_same(rc, r_dn) && lane_same(s_wy0[k], s_wy1[k]))) {
@@ -418,15 +439,17 @@ __device__ __forceinline__ void tile_lag_pressure(const StepArgs<R>& a, int bx, 
 
 // Artificial viscous stresses on interior cells, omp3/flow.c:173-207.
 template <typename R>
-__device__ __forceinline__ R visc_stress(R rho, R lo, R mid, R hi, R hi2) {
+// mid = w[0], hi = w[1]; lo = w[-1] and hi2 = w[2] are loaded only where
+// the cell is compressed.
+__device__ __forceinline__ R visc_stress(R rho, const R* w, R mid, R hi) {
   using Pr = Prec<R>;
   // Equal velocities either side of every cell of the warp: hi - mid = +0,
   // no compression (the result below, without the FP64 instructions).
   if (warp_same(hi, mid)) return R(0);
   const R m1 = Pr::min0(hi - mid);
   if (Pr::zero_skip(m1)) return R(0);  // no compression across the cell
-  const R m0 = Pr::min0(mid - lo);
-  const R m2 = Pr::min0(hi2 - hi);
+  const R m0 = Pr::min0(mid - w[-1]);
+  const R m2 = Pr::min0(w[2] - hi);
   return R(-kCQ) * rho * m1 * Pr::half(Pr::abs(m2 - m1) + Pr::abs(m1 - m0));
 }
 
@@ -447,12 +470,23 @@ __device__ __forceinline__ void tile_lag_viscosity(const StepArgs<R>& a, int bx,
   R vp = a.v[cidx(nx, i0 + 1, jj)];
   R m0 = Pr::min0(v0 - vm), m1 = Pr::min0(vp - v0);
   R g01 = Pr::abs(m1 - m0);
+  // Row ii+1's v, density and face velocities are loaded before row ii is
+  // processed.
+  R vp2_n = R(0), rho_n = R(0), um_n = R(0), up_n = R(0);
+  auto load = [&](int ii) {
+    const size_t f = fidx(nx, ii, jj);
+    vp2_n = a.v[cidx(nx, ii + 2, jj)];
+    rho_n = a.rho_r[cidx(nx, ii, jj)];
+    um_n = a.u[f];
+    up_n = a.u[f + 1];
+  };
+  if (i0 < i1) load(i0);
   for (int ii = i0; ii < i1; ++ii) {
-    const R vp2 = a.v[cidx(nx, ii + 2, jj)];
+    const R vp2 = vp2_n, rho = rho_n, um = um_n, up = up_n;
+    if (ii + 1 < i1) load(ii + 1);
     const size_t f = fidx(nx, ii, jj);
     const size_t c = cidx(nx, ii, jj);
-    const R rho = a.rho_r[c];
-    const R qx = visc_stress(rho, a.u[f - 1], a.u[f], a.u[f + 1], a.u[f + 2]);
+    const R qx = visc_stress(rho, a.u + f, um, up);
     R m2, g12, qy;
     if (!Pr::kMixed && warp_all(lane_same(vp2, vp) && Pr::is_zero(m1))) {
       // No jump of v across the cell or above it anywhere in the warp:
@@ -500,14 +534,25 @@ __device__ __forceinline__ void tile_lag_viscous_accel_impl(const StepArgs<R>& a
   const R dt = Pr::from_d(a.dt);
   const int i1 = min(i0 + a.rows, ny + 1 - pad);
   R qy_dn = (jj < nx - pad) ? a.Qyy[cidx(nx, i0 - 1, jj)] : R(0);
+  // The stresses of row ii+1 are loaded before row ii is processed.
+  R q1_n = R(0), q0_n = R(0), qy_n = R(0);
+  auto load = [&](int ii) {
+    const size_t c = cidx(nx, ii, jj);
+    if (ii < ny - pad) {
+      q1_n = a.Qxx[c];
+      q0_n = a.Qxx[c - 1];
+    }
+    if (jj < nx - pad) qy_n = a.Qyy[c];
+  };
+  if (i0 < i1) load(i0);
   for (int ii = i0; ii < i1; ++ii) {
     const int k = ii - i0;
+    const R q1 = q1_n, q0 = q0_n, qy = qy_n;
+    if (ii + 1 < i1) load(ii + 1);
     if (ii < ny - pad) {
       const size_t f = fidx(nx, ii, jj);
-      const size_t c = cidx(nx, ii, jj);
       // No stress gradient: the momentum and the velocity from the pressure
       // phase stand as they are.
-      const R q1 = a.Qxx[c], q0 = a.Qxx[c - 1];
       if (!warp_same(q1, q0)) {  // equal stresses in the whole warp: dqx = +0
         const R dqx = q1 - q0;
         if (!Pr::zero_skip(dqx)) {
@@ -521,7 +566,6 @@ __device__ __forceinline__ void tile_lag_viscous_accel_impl(const StepArgs<R>& a
     }
     if (jj < nx - pad) {
       const size_t c = cidx(nx, ii, jj);
-      const R qy = a.Qyy[c];
       if (!warp_same(qy, qy_dn)) {
         const R dqy = qy - qy_dn;
         if (!Pr::zero_skip(dqy)) {
@@ -1222,9 +1266,19 @@ __device__ __forceinline__ void tile_flux_uFx_impl(const StepArgs<R>& a, int bx,
   const R iex = geo_rcp<R, kP2>(a.edgedx[jj]);
   const R cxl = geo_v<R>(a.celldx[jj - 1]), cxr = geo_v<R>(a.celldx[jj]);
   const int i1 = min(i0 + a.rows, ny - pad);
+  // The mass fluxes of row ii+1 are loaded before row ii is processed.
+  R Fa_n = R(0), Fb_n = R(0);
+  if (i0 < i1) {
+    Fa_n = a.F_x[fidx(nx, i0, jj)];
+    Fb_n = a.F_x[fidx(nx, i0, jj) + 1];
+  }
   for (int ii = i0; ii < i1; ++ii) {
     const size_t f = fidx(nx, ii, jj);
-    const R Fa = a.F_x[f], Fb = a.F_x[f + 1];
+    const R Fa = Fa_n, Fb = Fb_n;
+    if (ii + 1 < i1) {
+      Fa_n = a.F_x[f + (nx + 1)];
+      Fb_n = a.F_x[f + (nx + 2)];
+    }
     R val;
     if (warp_zeros(Fa, Fb)) {
       // FP64 form: no mass through any cell of the warp; the flux is the
@@ -1272,10 +1326,22 @@ __device__ __forceinline__ void tile_flux_uFy_impl(const StepArgs<R>& a, int bx,
   uw.p0 = a.u[fidx(nx, i0, jj)];
   uw.p1 = a.u[fidx(nx, i0 + 1, jj)];
   bool fresh = false;
+  // The mass fluxes of row ii+1 and the window's next u are loaded before
+  // row ii is processed.
+  R Fa_n = R(0), Fb_n = R(0), u_next = R(0);
+  if (i0 < i1) {
+    Fa_n = a.F_y[cidx(nx, i0, jj)];
+    Fb_n = a.F_y[cidx(nx, i0, jj) - 1];
+  }
   for (int ii = i0; ii < i1; ++ii) {
     const int k = ii - i0;
     const size_t c = cidx(nx, ii, jj);
-    const R Fa = a.F_y[c], Fb = a.F_y[c - 1];
+    const R Fa = Fa_n, Fb = Fb_n;
+    if (ii + 1 < i1) {
+      Fa_n = a.F_y[c + nx];
+      Fb_n = a.F_y[c + nx - 1];
+      u_next = a.u[fidx(nx, ii + 2, jj)];
+    }
     const bool moved = !warp_zeros(Fa, Fb);
     R val;
     if (!moved) {
@@ -1294,7 +1360,7 @@ __device__ __forceinline__ void tile_flux_uFy_impl(const StepArgs<R>& a, int bx,
     a.uF_y[fidx(nx, ii, jj)] = val;
     mirror(edge, a.uF_y, nx + 1, ny + 1, pad, ii, jj, val, false, false);
     if (ii + 1 < i1) {
-      const R next = a.u[fidx(nx, ii + 2, jj)];
+      const R next = u_next;
       if (moved) {
         uw.shift(next);
       } else {
@@ -1323,10 +1389,20 @@ __device__ __forceinline__ void tile_flux_vFx_impl(const StepArgs<R>& a, int bx,
   const R cxl = geo_v<R>(a.celldx[jj - 1]), cxr = geo_v<R>(a.celldx[jj]);
   const int i1 = min(i0 + a.rows, ny + 1 - pad);
   R u_dn = a.u[fidx(nx, i0 - 1, jj)], F_dn = a.F_x[fidx(nx, i0 - 1, jj)];
+  // u and F_x of row ii+1 are loaded before row ii is processed.
+  R u_n = R(0), F_n = R(0);
+  if (i0 < i1) {
+    u_n = a.u[fidx(nx, i0, jj)];
+    F_n = a.F_x[fidx(nx, i0, jj)];
+  }
   for (int ii = i0; ii < i1; ++ii) {
     const size_t f = fidx(nx, ii, jj);
     const size_t c = cidx(nx, ii, jj);
-    const R u0 = a.u[f], F0 = a.F_x[f];
+    const R u0 = u_n, F0 = F_n;
+    if (ii + 1 < i1) {
+      u_n = a.u[f + (nx + 1)];
+      F_n = a.F_x[f + (nx + 1)];
+    }
     R val;
     if (warp_zeros(F0, F_dn)) {
       val = sum_zeros(F0, F_dn);  // FP64 form: no mass through any corner of the warp
@@ -1372,9 +1448,17 @@ __device__ __forceinline__ void tile_flux_vFy_impl(const StepArgs<R>& a, int bx,
   vw.p1 = a.v[cidx(nx, i0 + 2, jj)];
   bool fresh = false;
   R F0 = a.F_y[cidx(nx, i0, jj)];
+  // The next row's mass flux and the window's next v are loaded before row
+  // ii is processed.
+  R F1_n = R(0), v_next = R(0);
+  if (i0 < i1) F1_n = a.F_y[cidx(nx, i0 + 1, jj)];
   for (int ii = i0; ii < i1; ++ii) {
     const int k = ii - i0;
-    const R F1 = a.F_y[cidx(nx, ii + 1, jj)];
+    const R F1 = F1_n;
+    if (ii + 1 < i1) {
+      F1_n = a.F_y[cidx(nx, ii + 2, jj)];
+      v_next = a.v[cidx(nx, ii + 3, jj)];
+    }
     const bool moved = !warp_zeros(F0, F1);
     R val;
     if (!moved) {
@@ -1393,7 +1477,7 @@ __device__ __forceinline__ void tile_flux_vFy_impl(const StepArgs<R>& a, int bx,
     a.vF_y[cidx(nx, ii, jj)] = val;
     mirror(edge, a.vF_y, nx, ny, pad, ii, jj, val, false, false);
     if (ii + 1 < i1) {
-      const R next = a.v[cidx(nx, ii + 3, jj)];
+      const R next = v_next;
       if (moved) {
         vw.shift(next);
       } else {
@@ -1473,20 +1557,44 @@ __device__ __forceinline__ void tile_momentum_update_impl(const StepArgs<R>& a, 
     wx1 = geo_half_ratio<R, kP2>(a.celldx[jj - 1], ex);
   }
   const int i1 = min(i0 + a.rows, row_end);
+  if (i0 >= i1) return;
+  // The inputs of row ii: the fluxes fa, fb (difference fa - fb), the
+  // momentum m and the densities ra, rb either side of the face.  Row ii+1's
+  // are loaded before row ii is processed (its stores do not touch them), so
+  // that two rows of loads are in flight; where row ii+1's fb or rb is row
+  // ii's fa or ra (y fluxes, v faces), it is carried instead.
+  struct RowIn {
+    R fa, fb, m, ra, rb;
+  };
+  auto load = [&](int ii, const RowIn* prev) {
+    RowIn in;
+    const size_t f = fidx(nx, ii, jj);
+    const size_t c = cidx(nx, ii, jj);
+    if (kWhich == 0) { in.fa = a.uF_x[c]; in.fb = a.uF_x[c - 1]; }
+    else if (kWhich == 1) { in.fa = a.uF_y[f + (nx + 1)]; in.fb = prev ? prev->fa : a.uF_y[f]; }
+    else if (kWhich == 2) { in.fa = a.vF_x[f + 1]; in.fb = a.vF_x[f]; }
+    else { in.fa = a.vF_y[c]; in.fb = prev ? prev->fa : a.vF_y[c - nx]; }
+    in.m = kU ? a.rho_u[f] : a.rho_v[c];
+    in.ra = in.rb = R(0);
+    if (kVel) {
+      in.ra = a.rho_r[c];
+      in.rb = kU ? a.rho_r[c - 1] : (prev ? prev->ra : a.rho_r[c - nx]);
+    }
+    return in;
+  };
+  RowIn cur = load(i0, nullptr);
   for (int ii = i0; ii < i1; ++ii) {
     const int k = ii - i0;
     const size_t f = fidx(nx, ii, jj);
     const size_t c = cidx(nx, ii, jj);
-    R fa, fb;  // the flux difference is fa - fb
-    if (kWhich == 0) { fa = a.uF_x[c]; fb = a.uF_x[c - 1]; }
-    else if (kWhich == 1) { fa = a.uF_y[f + (nx + 1)]; fb = a.uF_y[f]; }
-    else if (kWhich == 2) { fa = a.vF_x[f + 1]; fb = a.vF_x[f]; }
-    else { fa = a.vF_y[c]; fb = a.vF_y[c - nx]; }
+    RowIn nxt = cur;
+    if (ii + 1 < i1) nxt = load(ii + 1, &cur);
+    const R fa = cur.fa, fb = cur.fb;
     R* mom = kU ? a.rho_u + f : a.rho_v + c;
     // mom - dt_h * diff / (hx * hy), the divisor rounded as the reference
     // forms it (omp3/flow.c:581-584); no flux difference, no change (in the
     // FP64 form equal fluxes in the whole warp skip the difference too).
-    R m = *mom;
+    R m = cur.m;
     if (!warp_same(fa, fb)) {
       const R diff = fa - fb;
       if (!Pr::zero_skip(diff)) {
@@ -1496,7 +1604,7 @@ __device__ __forceinline__ void tile_momentum_update_impl(const StepArgs<R>& a, 
       }
     }
     if (kVel) {
-      const R ra = a.rho_r[c], rb = kU ? a.rho_r[c - 1] : a.rho_r[c - nx];
+      const R ra = cur.ra, rb = cur.rb;
       const R w0 = kU ? wx0 : s_wy0[k], w1 = kU ? wx1 : s_wy1[k];
       R rbar;
       // FP64 form, power-of-two tile: equal densities and weights either
@@ -1515,6 +1623,7 @@ __device__ __forceinline__ void tile_momentum_update_impl(const StepArgs<R>& a, 
         mirror(edge, a.v, nx, ny + 1, pad, ii, jj, vel, false, true);
       }
     }
+    cur = nxt;
   }
 }
 
