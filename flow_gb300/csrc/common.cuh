@@ -42,11 +42,14 @@ constexpr int kMaxReduceBlocks = 1024;
 // Ghost-fill modes of handle_boundary_2d (arch; omp3/flow.c:156).
 enum : int { kNoInvert = 0, kInvertX = 1, kInvertY = 2 };
 
+// Indices are never negative here, so they are formed with one 32x32->64-bit
+// unsigned multiply-add (a signed int widened to size_t first costs a 64-bit
+// multiply).
 __host__ __device__ inline size_t cidx(int nx, int ii, int jj) {
-  return (size_t)ii * (size_t)nx + (size_t)jj;
+  return (size_t)(unsigned)ii * (unsigned)nx + (unsigned)jj;
 }
 __host__ __device__ inline size_t fidx(int nx, int ii, int jj) {
-  return (size_t)ii * (size_t)(nx + 1) + (size_t)jj;
+  return (size_t)(unsigned)ii * (unsigned)(nx + 1) + (unsigned)jj;
 }
 
 // Ordinary minimum (first argument when strictly smaller).

@@ -48,12 +48,12 @@ __global__ void __launch_bounds__(kCols) k_lag_energy_dt(const StepArgs<R> a) {
   }
 }
 template <typename R, bool kFirst>
-__global__ void __launch_bounds__(kCols, 8) k_mass_sweep_x(const StepArgs<R> a,
+__global__ void __launch_bounds__(kCols, Prec<R>::kMixed ? 8 : 7) k_mass_sweep_x(const StepArgs<R> a,
                                                         const SweepArgs<R> s) {
   tile_mass_sweep_x<R, kFirst>(a, s, blockIdx.x, blockIdx.y);
 }
 template <typename R, bool kFirst>
-__global__ void __launch_bounds__(kCols, 7) k_mass_sweep_y(const StepArgs<R> a,
+__global__ void __launch_bounds__(kCols, Prec<R>::kMixed ? 7 : 5) k_mass_sweep_y(const StepArgs<R> a,
                                                         const SweepArgs<R> s) {
   tile_mass_sweep_y<R, kFirst>(a, s, blockIdx.x, blockIdx.y);
 }

@@ -1045,17 +1045,37 @@ __device__ __forceinline__ void tile_mass_sweep_x_impl(const StepArgs<R>& a,
   const R dt_r = Pr::from_d(dt), dt_h_r = Pr::from_d(dt_h);
   __syncthreads();
   const int i1 = min(i0 + a.rows, ny - pad);
+  // Row ii+1's face velocity and the update inputs of its cell are loaded
+  // before row ii is processed; a warp whose faces are all at rest carries
+  // no flux and reads nothing else (the flux core returns +0 for them).
+  R u0_n = R(0);
+  double rin_n = 0.0, ein_n = 0.0, rold_n = 0.0;
+  auto load = [&](int ii) {
+    if (face_ok) u0_n = a.u[fidx(nx, ii, jj)];
+    if (cell_ok) {
+      const size_t c = cidx(nx, ii, jj);
+      rin_n = s.r_in[c];
+      ein_n = s.e_in[c];
+      rold_n = kFirst ? rin_n : a.rho[c];
+    }
+  };
+  if (i0 < i1) load(i0);
   for (int ii = i0; ii < i1; ++ii) {
     const int k = ii - i0;
+    const R u0 = u0_n;
+    const double r_in = rin_n, e_in = ein_n, r_old = rold_n;
+    if (ii + 1 < i1) load(ii + 1);
     R F = R(0), eF = R(0);
     if (face_ok) {
       const size_t f = fidx(nx, ii, jj);
       const size_t c = cidx(nx, ii, jj);
-      mass_energy_flux<R, false, kP2>(a.u[f - 1], a.u[f], a.u[f + 1], s.r_in_r[c - 2],
-                                 s.r_in_r[c - 1], s.r_in_r[c], s.r_in_r[c + 1],
-                                 s.e_in_r[c - 2], s.e_in_r[c - 1], s.e_in_r[c],
-                                 s.e_in_r[c + 1], iex, cxm, cx0, icx_r,
-                                 s_ey0r[k], dt_r, dt_h_r, &F, &eF);
+      if (!warp_all(Pr::is_zero(u0))) {
+        mass_energy_flux<R, false, kP2>(a.u[f - 1], u0, a.u[f + 1], s.r_in_r[c - 2],
+                                        s.r_in_r[c - 1], s.r_in_r[c], s.r_in_r[c + 1],
+                                        s.e_in_r[c - 2], s.e_in_r[c - 1], s.e_in_r[c],
+                                        s.e_in_r[c + 1], iex, cxm, cx0, icx_r,
+                                        s_ey0r[k], dt_r, dt_h_r, &F, &eF);
+      }
       if (face_owner) {
         a.F_x[f] = F;
         mirror(edge, a.F_x, nx + 1, ny, pad, ii, jj, F, true, false);
@@ -1065,10 +1085,8 @@ __device__ __forceinline__ void tile_mass_sweep_x_impl(const StepArgs<R>& a,
     seF[t] = eF;
     __syncthreads();
     if (cell_ok) {
-      const size_t c = cidx(nx, ii, jj);
-      const double r_old = kFirst ? s.r_in[c] : a.rho[c];
       double r_new, e_new;
-      mass_energy_update<R, kFirst, kP2>(s.r_in[c], s.e_in[c], r_old, dt_h,
+      mass_energy_update<R, kFirst, kP2>(r_in, e_in, r_old, dt_h,
                                          a.celldx[jj] * s_cyd[k],
                                          Prec<double>::mulp<kP2>(s_coef[k], icx),
                                          s_ey0[k], s_ey1[k], sF[t],
@@ -1177,10 +1195,26 @@ __device__ __forceinline__ void tile_mass_sweep_y_impl(const StepArgs<R>& a,
     a.F_y[c] = F0;
     mirror(edge, a.F_y, nx, ny + 1, pad, i0, jj, F0, false, true);
   }
+  // The window values of row ii+3 and the update inputs of row ii+1 are
+  // loaded before row ii is processed.
+  R rn_n = R(0), en_n = R(0), vn_n = R(0);
+  double rin_n = 0.0, ein_n = 0.0, rold_n = 0.0;
+  auto load = [&](int ii) {
+    const size_t c_next = cidx(nx, ii + 2, jj);
+    rn_n = s.r_in_r[c_next];
+    en_n = s.e_in_r[c_next];
+    vn_n = a.v[c_next];
+    const size_t c = cidx(nx, ii, jj);
+    rin_n = s.r_in[c];
+    ein_n = s.e_in[c];
+    rold_n = kFirst ? rin_n : a.rho[c];
+  };
+  if (i0 < i1) load(i0);
   for (int ii = i0; ii < i1; ++ii) {
     const int k = ii - i0;
-    const size_t c_next = cidx(nx, ii + 2, jj);
-    const R rn = s.r_in_r[c_next], en = s.e_in_r[c_next], vn = a.v[c_next];
+    const R rn = rn_n, en = en_n, vn = vn_n;
+    const double r_in = rin_n, e_in = ein_n, r_old = rold_n;
+    if (ii + 1 < i1) load(ii + 1);
     R F1 = R(0), eF1 = R(0);
     const bool was_fresh = fresh;
     // Shift the velocity window's values; face row k+1 has velocity vp.
@@ -1214,10 +1248,8 @@ __device__ __forceinline__ void tile_mass_sweep_y_impl(const StepArgs<R>& a,
       a.F_y[c] = F1;
       mirror(edge, a.F_y, nx, ny + 1, pad, ii + 1, jj, F1, false, true);
     }
-    const size_t c = cidx(nx, ii, jj);
-    const double r_old = kFirst ? s.r_in[c] : a.rho[c];
     double r_new, e_new;
-    mass_energy_update<R, kFirst, kP2>(s.r_in[c], s.e_in[c], r_old, dt_h,
+    mass_energy_update<R, kFirst, kP2>(r_in, e_in, r_old, dt_h,
                                        a.celldx[jj] * s_cyd[k],
                                        Prec<double>::mulp<kP2>(s_coef[k], icx), ex0, ex1,
                                        F0, F1, eF0, eF1, &r_new, &e_new);
@@ -1574,7 +1606,11 @@ __device__ __forceinline__ void tile_momentum_update_impl(const StepArgs<R>& a, 
     else if (kWhich == 1) { in.fa = a.uF_y[f + (nx + 1)]; in.fb = prev ? prev->fa : a.uF_y[f]; }
     else if (kWhich == 2) { in.fa = a.vF_x[f + 1]; in.fb = a.vF_x[f]; }
     else { in.fa = a.vF_y[c]; in.fb = prev ? prev->fa : a.vF_y[c - nx]; }
-    in.m = kU ? a.rho_u[f] : a.rho_v[c];
+    // The momentum is needed ahead only where the velocity is recomputed;
+    // otherwise it is read where a flux difference changes it (rows at rest
+    // do not read it).
+    in.m = R(0);
+    if (kVel) in.m = kU ? a.rho_u[f] : a.rho_v[c];
     in.ra = in.rb = R(0);
     if (kVel) {
       in.ra = a.rho_r[c];
@@ -1598,6 +1634,7 @@ __device__ __forceinline__ void tile_momentum_update_impl(const StepArgs<R>& a, 
     if (!warp_same(fa, fb)) {
       const R diff = fa - fb;
       if (!Pr::zero_skip(diff)) {
+        if (!kVel) m = *mom;
         m = Pr::template dsub<kP2>(m, dt_h_r * diff, hx_r * s_h[k],
                                    Pr::template mulp<kP2>(s_row[k], ihx));
         *mom = m;
