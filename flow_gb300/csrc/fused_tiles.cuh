@@ -394,7 +394,7 @@ __device__ __forceinline__ void tile_lag_pressure_impl(const StepArgs<R>& a, int
         rbar = Pr::twice(Pr::template mulp<true>(rc, wx0));
       } else {
         const R dp = Pc - Pl;
-        if (!Pr::zero_skip(dp)) {
+        if (!Pr::zero_skip_mem(dp)) {
           mom = Pr::template dsub<kP2>(mom, dt * dp, exr, iex);
           a.rho_u[f] = mom;
         }
@@ -414,7 +414,7 @@ __device__ __forceinline__ void tile_lag_pressure_impl(const StepArgs<R>& a, int
         rbar = Pr::twice(Pr::template mulp<true>(rc, s_wy0[k]));
       } else {
         const R dp = Pc - P_dn;
-        if (!Pr::zero_skip(dp)) {
+        if (!Pr::zero_skip_mem(dp)) {
           mom = Pr::template dsub<kP2>(mom, dt * dp, s_ey[k], s_iey[k]);
           a.rho_v[c] = mom;
         }
@@ -555,7 +555,7 @@ __device__ __forceinline__ void tile_lag_viscous_accel_impl(const StepArgs<R>& a
       // phase stand as they are.
       if (!warp_same(q1, q0)) {  // equal stresses in the whole warp: dqx = +0
         const R dqx = q1 - q0;
-        if (!Pr::zero_skip(dqx)) {
+        if (!Pr::zero_skip_mem(dqx)) {
           const R mom = Pr::template dsub<kP2>(a.rho_u[f], dt * dqx, cx, icx);
           const R vel = face_velocity(mom, a.uF_x[f]);
           a.rho_u[f] = mom;
@@ -568,7 +568,7 @@ __device__ __forceinline__ void tile_lag_viscous_accel_impl(const StepArgs<R>& a
       const size_t c = cidx(nx, ii, jj);
       if (!warp_same(qy, qy_dn)) {
         const R dqy = qy - qy_dn;
-        if (!Pr::zero_skip(dqy)) {
+        if (!Pr::zero_skip_mem(dqy)) {
           const R mom = Pr::template dsub<kP2>(a.rho_v[c], dt * dqy, s_cy[k], s_icy[k]);
           const R vel = face_velocity(mom, a.vF_y[c]);
           a.rho_v[c] = mom;
@@ -659,7 +659,8 @@ __device__ __forceinline__ void tile_lag_energy_dt_impl(const StepArgs<R>& a, in
         const R dvdy = Pr::template mulp<kP2>(v1 - v0, s_icy[k]);
         still = Pr::zero_skip_coarse(dudx) && Pr::zero_skip_coarse(dvdy);
         if (still) {
-          e_new = rz ? 0.0 : (Pr::kMixed ? a.e[c] : double(er));
+          // (Mixed form: the FP64 energy is not needed, as it is kept.)
+          e_new = rz ? 0.0 : (Pr::kMixed ? 0.0 : double(er));
         } else {
           inv_r = rz ? R(0) : Pr::rcp(r);
           const R div_dt = (dudx + dvdy) * dt_h;
@@ -676,14 +677,17 @@ __device__ __forceinline__ void tile_lag_energy_dt_impl(const StepArgs<R>& a, in
           }
         }
       }
-      store_cell(edge, a.e, a.e_r, nx, ny, pad, ii, jj, e_new);
+      // A still cell with mass keeps its energy: e, its bulk shadow and their
+      // ghost images already hold it, so nothing is stored.
+      const bool keep = still && !rz;
+      if (!keep) store_cell(edge, a.e, a.e_r, nx, ny, pad, ii, jj, e_new);
       // CFL: celldx / sqrt(c_s^2 + 2 Q / rho) with c_s^2 = gamma (gamma-1) e.
       // The reference squares c_s = sqrt(gamma (gamma-1) e), so a cell whose
       // energy went negative gives a NaN candidate whatever Q is, and its dt
       // is then the minimum over the other cells (the 4096^2 known-answer
       // problem does this on its first step, which runs at Courant ~0.9).
       // Skip such cells rather than use gamma (gamma-1) e + 2Q/rho directly.
-      const R e_nr = Pr::from_d(e_new);
+      const R e_nr = keep ? er : Pr::from_d(e_new);
       const R s2 = R(kGam * (kGam - 1.0)) * e_nr;
       R sx = s2, sy = s2;  // + 2 Q / rho, zero without viscous stress
       if (!Pr::zero_skip_coarse(qx) || !Pr::zero_skip_coarse(qy)) {
@@ -1633,7 +1637,7 @@ __device__ __forceinline__ void tile_momentum_update_impl(const StepArgs<R>& a, 
     R m = cur.m;
     if (!warp_same(fa, fb)) {
       const R diff = fa - fb;
-      if (!Pr::zero_skip(diff)) {
+      if (!Pr::zero_skip_mem(diff)) {
         if (!kVel) m = *mom;
         m = Pr::template dsub<kP2>(m, dt_h_r * diff, hx_r * s_h[k],
                                    Pr::template mulp<kP2>(s_row[k], ihx));

@@ -31,6 +31,9 @@ struct Prec<double> {
   // a whole flux or cell update.
   __device__ static __forceinline__ bool zero_skip(double x) { return d_is_zero(x); }
   __device__ static __forceinline__ bool zero_skip_coarse(double x) { return d_is_zero(x); }
+  // A zero increment whose update is skipped together with its loads and
+  // stores (a momentum that does not change is neither read nor written).
+  __device__ static __forceinline__ bool zero_skip_mem(double x) { return d_is_zero(x); }
   __device__ static __forceinline__ bool is_zero(double x) { return d_is_zero(x); }
   __device__ static __forceinline__ bool gt0(double x) { return d_gt0(x); }
   __device__ static __forceinline__ bool ge0(double x) { return d_ge0(x); }
@@ -117,6 +120,9 @@ struct Prec<float> {
   __device__ static __forceinline__ bool zero_skip_coarse(float x) {
     return __all_sync(__activemask(), x == 0.0f) != 0;
   }
+  // Skips that save memory traffic (a momentum that does not change is
+  // neither read nor written) are worth a warp vote here too.
+  __device__ static __forceinline__ bool zero_skip_mem(float x) { return zero_skip_coarse(x); }
   __device__ static __forceinline__ bool is_zero(float x) { return x == 0.0f; }
   __device__ static __forceinline__ bool gt0(float x) { return x > 0.0f; }
   __device__ static __forceinline__ bool ge0(float x) { return x >= 0.0f; }
