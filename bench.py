@@ -36,29 +36,38 @@ N_CELLS_SIDE = 4096
 B_ALG_FP64 = 64  # bytes/cell-step: rho, e, rho_u, rho_v read + written once
 
 # Algorithmic bytes per interior cell of each fused kernel: the arrays it must
-# read and write once (8 bytes each).  Used for the per-kernel HBM roofline.
+# read and write once (8 bytes each) on every cell.  Arrays that change only
+# where the flow moves (momenta, energy) are counted as read; their writes on
+# moving cells come on top.  Used for the per-kernel HBM roofline.
 KERNEL_BYTES_PER_CELL = {
-    "lag_pressure": 8 * 12,      # rho, e, rho_u, rho_v in; P, rho_old, rho_u, rho_v, u, v, 1/rho_x, 1/rho_y out
+    "lag_pressure": 8 * 10,      # rho, e, rho_u, rho_v in; P, rho_old, u, v, 1/rho_x, 1/rho_y out
     "lag_viscosity": 8 * 5,      # u, v, rho in; Qxx, Qyy out
-    "lag_viscous_accel": 8 * 12,  # Qxx, Qyy, rho_u, rho_v, 1/rho_x, 1/rho_y in; rho_u, rho_v, u, v out (+2 rereads)
-    "lag_energy_dt": 8 * 8,      # rho, P, e, Qxx, Qyy, u, v in; e out
-    "mass_sweep_x": 8 * 7,       # rho, e, rho_old, u in; rho, e, F_x out
-    "mass_sweep_y": 8 * 7,
-    "flux_uFx": 8 * 3,           # u, F_x in; uF_x out
-    "flux_uFy": 8 * 4,           # u, v, F_y in; uF_y out
-    "flux_vFx": 8 * 4,
-    "flux_vFy": 8 * 3,
-    "update_rho_u": 8 * 3,       # flux, rho_u in; rho_u out (+ rho, u when the velocity is recomputed)
-    "update_rho_v": 8 * 3,
+    "lag_viscous_accel": 8 * 2,  # Qxx, Qyy in (momenta and velocities where a stress gradient acts)
+    "lag_energy_dt": 8 * 7,      # rho, P, e, Qxx, Qyy, u, v in (e out where the cell is compressed)
+    "mass_sweep_x": 8 * 6,       # rho, e, u in; rho, e, F_x out
+    "mass_sweep_y": 8 * 6,
+    "flux_uFx": 8 * 2,           # F_x in; uF_x out (u where mass moves)
+    "flux_uFy": 8 * 3,           # F_y, u in; uF_y out
+    "flux_vFx": 8 * 3,           # F_x, u in; vF_x out
+    "flux_vFy": 8 * 3,           # F_y, v in; vF_y out
+    # Two launches per step: flux, rho_u, rho in and u out (32 B) for the one
+    # that recomputes the velocity, flux in (8 B) for the other (rho_u where
+    # the flux difference acts); the mean per launch.
+    "update_rho_u": 20,
+    "update_rho_v": 20,
 }
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per interior cell of
-# one launch, from an ncu capture of the FP64 fused kernels on Sedov 2048^2
-# (4.19 M cells); scaled to a launch by its cell count.
+# one launch, from an ncu capture of the FP64 fused kernels on the Sedov blast
+# at 2048^2 (4.19 M cells, after three timesteps); scaled to a launch by its
+# cell count.
 NCU_TRAFFIC_BYTES_PER_CELL = {
-    "mass_sweep_y": (108.8e6 + 58.4e6) / 2048 ** 2,
-    "lag_energy_dt": (236.7e6 + 23.0e6) / 2048 ** 2,
-    "flux_uFy": (102.1e6 + 13.3e6) / 2048 ** 2,
+    "lag_pressure": 68.7,
+    "lag_viscosity": 31.3,
+    "lag_viscous_accel": 16.1,
+    "lag_energy_dt": 48.5,
+    "mass_sweep_x": 36.3,
+    "mass_sweep_y": 44.9,
 }
 
 
@@ -562,7 +571,13 @@ def run_gpu(args):
                      "peak_kind": peak_kind},
         "fp64_pipe": {"fma_per_s_peak": fma_rate.value,
                       "note": "FP64 issue rate measured on this GPU; the FP64 timestep is bound here"},
-        "kernels": [{"name": k, "launches": c, "ms": t, "share": t / sum(x[2] for x in kernels)}
+        # Per kernel: launches, total ms, share of the step, and its achieved
+        # GB/s on its algorithmic bytes (KERNEL_BYTES_PER_CELL) with the
+        # fraction of the measured HBM copy bandwidth.
+        "kernels": [{"name": k, "launches": c, "ms": t, "share": t / sum(x[2] for x in kernels),
+                     "alg_gbs": KERNEL_BYTES_PER_CELL.get(k, B_ALG_FP64) * cells / (t / c * 1e-3) / 1e9,
+                     "alg_frac": KERNEL_BYTES_PER_CELL.get(k, B_ALG_FP64) * cells
+                                 / (t / c * 1e-3) / 1e9 / peak}
                     for k, c, t in kernels],
         "forms": forms,
         "cpu_baseline": cpu,
