@@ -632,17 +632,30 @@ __device__ __forceinline__ void tile_lag_energy_dt_impl(const StepArgs<R>& a, in
     const R dt_h = Pr::from_d(a.dt_h);
     const int i1 = min(i0 + a.rows, ny - pad);
     R v0 = a.v[cidx(nx, i0, jj)];
+    // Mixed form: row ii+1's inputs are loaded before row ii is processed.
+    // (The FP64 form, at 64 registers without it, loses more occupancy than
+    // it gains.)  The FP64 pressure is read only where a cell is compressed.
+    constexpr bool kAhead = Pr::kMixed;
+    R v1_n = R(0), r_n = R(0), er_n = R(0), qx_n = R(0), qy_n = R(0), u0_n = R(0), u1_n = R(0);
+    auto load = [&](int ii) {
+      const size_t c = cidx(nx, ii, jj);
+      const size_t f = c + (size_t)ii;  // fidx(nx, ii, jj)
+      v1_n = a.v[c + nx];
+      r_n = a.rho_r[c];
+      er_n = a.e_r[c];
+      qx_n = a.Qxx[c];
+      qy_n = a.Qyy[c];
+      u0_n = a.u[f];
+      u1_n = a.u[f + 1];
+    };
+    if (kAhead && i0 < i1) load(i0);
     for (int ii = i0; ii < i1; ++ii) {
       const int k = ii - i0;
       const size_t c = cidx(nx, ii, jj);
-      const size_t f = fidx(nx, ii, jj);
-      const R v1 = a.v[c + nx];
-      const R r = a.rho_r[c];
-      const R er = a.e_r[c];
-      const R p = Pr::kMixed ? R(kG1) * r * er : R(a.P[c]);
-      const R qx = a.Qxx[c], qy = a.Qyy[c];
+      if (!kAhead) load(ii);
+      const R v1 = v1_n, r = r_n, er = er_n, qx = qx_n, qy = qy_n, u0f = u0_n, u1f = u1_n;
+      if (kAhead && ii + 1 < i1) load(ii + 1);
       const bool rz = Pr::is_zero(r);
-      const R u0f = a.u[f], u1f = a.u[f + 1];
       // A cell whose faces do not move relative to each other does no work
       // and takes no shock heating: every increment below is a zero, so e is
       // left as it is (a cell at rest, or in uniform translation).  In the
@@ -662,6 +675,7 @@ __device__ __forceinline__ void tile_lag_energy_dt_impl(const StepArgs<R>& a, in
           // (Mixed form: the FP64 energy is not needed, as it is kept.)
           e_new = rz ? 0.0 : (Pr::kMixed ? 0.0 : double(er));
         } else {
+          const R p = Pr::kMixed ? R(kG1) * r * er : R(a.P[c]);
           inv_r = rz ? R(0) : Pr::rcp(r);
           const R div_dt = (dudx + dvdy) * dt_h;
           // e_q = e - dt_h (Qxx dudx + Qyy dvdy) / rho, kept as an increment.

@@ -199,20 +199,32 @@ __global__ void __launch_bounds__(kRedThreads)
 }
 
 // Each block sums whole interior rows (threads stride along the row), so the
-// traversal needs no division of a flat index.
+// traversal needs no division of a flat index.  Two columns per iteration
+// into two pairs of sums (independent loads and FP64 chains in flight), and
+// rho*e contracted into one FMA: two FP64 instructions per cell, the FP64
+// pipe's share of this reduction on GB300.
 __global__ void __launch_bounds__(kRedThreads)
-    k_conservation(int nx, int ny, int pad, const double* rho, const double* e,
-                   double* ra) {
-  double ms = 0.0, es = 0.0;
+    k_conservation(int nx, int ny, int pad, const double* __restrict__ rho,
+                   const double* __restrict__ e, double* ra) {
+  double ms0 = 0.0, es0 = 0.0, ms1 = 0.0, es1 = 0.0;
   for (int ii = pad + blockIdx.x; ii < ny - pad; ii += gridDim.x) {
     const double* rr = rho + (size_t)ii * nx;
     const double* er = e + (size_t)ii * nx;
-    for (int jj = pad + threadIdx.x; jj < nx - pad; jj += blockDim.x) {
-      const double d = rr[jj];
-      ms += d;
-      es += d * er[jj];
+    int jj = pad + threadIdx.x;
+    for (; jj + kRedThreads < nx - pad; jj += 2 * kRedThreads) {
+      const double d0 = rr[jj], d1 = rr[jj + kRedThreads];
+      const double f0 = er[jj], f1 = er[jj + kRedThreads];
+      ms0 += d0;
+      ms1 += d1;
+      es0 = fma(d0, f0, es0);
+      es1 = fma(d1, f1, es1);
+    }
+    if (jj < nx - pad) {
+      ms0 += rr[jj];
+      es0 = fma(rr[jj], er[jj], es0);
     }
   }
+  double ms = ms0 + ms1, es = es0 + es1;
   __shared__ double s_m[kRedThreads / 32], s_e[kRedThreads / 32];
   __shared__ bool s_last;
   ms = warp_sum(ms);
