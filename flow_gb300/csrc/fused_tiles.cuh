@@ -195,9 +195,9 @@ __device__ __forceinline__ bool block_mesh_pow2(const StepArgs<R>& a, int col0, 
 }
 
 // Runs tile(kPow2) with kPow2 = true for FP64 tiles whose mesh spacings are
-// all powers of two.  (The mixed form gains nothing measurable from it: its
-// FP64 work is the conservative update, where the products by power-of-two
-// face lengths are exact either way.)
+// all powers of two.  (The mixed form's FP32 arithmetic gains nothing from
+// it; its mass sweeps, whose FP64 conservative update multiplies by the face
+// lengths, dispatch with FLOW_POW2_DISPATCH_ALL.)
 #define FLOW_POW2_DISPATCH(R, a, col0, row0, CALL_TRUE, CALL_FALSE)          \
   do {                                                                      \
     if constexpr (!Prec<R>::kMixed) {                                       \
@@ -205,6 +205,14 @@ __device__ __forceinline__ bool block_mesh_pow2(const StepArgs<R>& a, int col0, 
         CALL_TRUE;                                                          \
         return;                                                             \
       }                                                                     \
+    }                                                                       \
+    CALL_FALSE;                                                             \
+  } while (0)
+#define FLOW_POW2_DISPATCH_ALL(a, col0, row0, CALL_TRUE, CALL_FALSE)         \
+  do {                                                                      \
+    if (block_mesh_pow2(a, col0, row0)) {                                   \
+      CALL_TRUE;                                                            \
+      return;                                                               \
     }                                                                       \
     CALL_FALSE;                                                             \
   } while (0)
@@ -245,7 +253,7 @@ __device__ __forceinline__ R geo_half(double h) { return Prec<R>::from_d(d_half(
 template <typename R, bool kP2>
 __device__ __forceinline__ double geo_rcp_d(double h) {
   if constexpr (Prec<R>::kMixed) {
-    return d_rcp(h);
+    return kP2 ? d_pow2_rcp(h) : d_rcp(h);
   } else {
     return kP2 ? d_pow2_rcp(h) : 1.0 / h;
   }
@@ -948,12 +956,14 @@ static __device__ __noinline__ double still_quotient_mixed(double n, double d) {
   return fma(r0, fma(-d, q, n), q);
 }
 
+// The fluxes arrive widened to FP64 (f0, f1 mass, ef0, ef1 energy; exact
+// for the mixed form's FP32 fluxes), each face's once.
 template <typename R, bool kFirst, bool kP2>
 __device__ __forceinline__ void mass_energy_update(double r_in, double e_in,
                                                    double r_old, double dt_h,
                                                    double vol, double ivol, double a0,
-                                                   double a1, R F0, R F1, R eF0,
-                                                   R eF1, double* r_out,
+                                                   double a1, double f0, double f1,
+                                                   double ef0, double ef1, double* r_out,
                                                    double* e_out) {
   using Pr = Prec<R>;
   // No mass or energy crosses any cell of the warp (a warp-uniform test): the
@@ -961,8 +971,8 @@ __device__ __forceinline__ void mass_energy_update(double r_in, double e_in,
   // reference's rho_old*e/den round trip -- which gives e itself when the
   // product rho_old*e is exact and den is rho_old, as in the still background
   // of a blast.  The FP64 form takes the per-lane skip below otherwise.
-  const bool none = warp_all(Pr::is_zero(F0) && Pr::is_zero(F1) &&
-                             (Pr::kMixed || (Pr::is_zero(eF0) && Pr::is_zero(eF1))));
+  const bool none = warp_all(d_is_zero(f0) && d_is_zero(f1) &&
+                             (Pr::kMixed || (d_is_zero(ef0) && d_is_zero(ef1))));
   if (none) {
     const double rho_e = __dmul_rn(r_old, e_in);
     const double den = kFirst ? r_old : r_in;
@@ -977,12 +987,15 @@ __device__ __forceinline__ void mass_energy_update(double r_in, double e_in,
     }
     return;
   }
-  const double f0 = Pr::to_d(F0), f1 = Pr::to_d(F1);
-  const double de = Pr::to_d(eF1) - Pr::to_d(eF0);
+  const double de = ef1 - ef0;
   double r_new, rho_e;
   if (Pr::kMixed) {
     const double coef = ivol;
-    r_new = fma(-coef, fma(a1, f1, -(a0 * f0)), r_in);
+    // On power-of-two tiles the face-length products are exact exponent adds
+    // (the same numbers as the FMA below, which rounds once after them).
+    const double net = kP2 ? __dadd_rn(d_mul_pow2(f1, a1), -d_mul_pow2(f0, a0))
+                           : fma(a1, f1, -(a0 * f0));
+    r_new = fma(-coef, net, r_in);
     rho_e = fma(-coef, de, r_old * e_in);
   } else if (Pr::zero_skip(f0) && Pr::zero_skip(f1) && Pr::zero_skip(de)) {
     // Nothing crosses the cell's faces: the updates subtract zeros.  (The
@@ -1028,7 +1041,8 @@ template <typename R, bool kFirst, bool kP2>
 __device__ __forceinline__ void tile_mass_sweep_x_impl(const StepArgs<R>& a,
                                                        const SweepArgs<R>& s, int bx, int by) {
   using Pr = Prec<R>;
-  __shared__ R sF[kCols], seF[kCols], s_ey0r[kMaxRows];
+  __shared__ R s_ey0r[kMaxRows];
+  __shared__ double sF[kCols], seF[kCols];  // the row's face fluxes, widened once
   __shared__ double s_coef[kMaxRows], s_cyd[kMaxRows], s_ey0[kMaxRows], s_ey1[kMaxRows];
   const int nx = a.nx, ny = a.ny, pad = a.pad;
   const int t = threadIdx.x;
@@ -1099,8 +1113,8 @@ __device__ __forceinline__ void tile_mass_sweep_x_impl(const StepArgs<R>& a,
         mirror(edge, a.F_x, nx + 1, ny, pad, ii, jj, F, true, false);
       }
     }
-    sF[t] = F;
-    seF[t] = eF;
+    sF[t] = Pr::to_d(F);
+    seF[t] = Pr::to_d(eF);
     __syncthreads();
     if (cell_ok) {
       double r_new, e_new;
@@ -1119,7 +1133,7 @@ __device__ __forceinline__ void tile_mass_sweep_x_impl(const StepArgs<R>& a,
 template <typename R, bool kFirst>
 __device__ __forceinline__ void tile_mass_sweep_x(const StepArgs<R>& a, const SweepArgs<R>& s,
                                                   int bx, int by) {
-  FLOW_POW2_DISPATCH(R, a, a.pad + bx * (kCols - 1), a.pad + by * a.rows,
+  FLOW_POW2_DISPATCH_ALL(a, a.pad + bx * (kCols - 1), a.pad + by * a.rows,
                      (tile_mass_sweep_x_impl<R, kFirst, true>(a, s, bx, by)),
                      (tile_mass_sweep_x_impl<R, kFirst, false>(a, s, bx, by)));
 }
@@ -1213,6 +1227,8 @@ __device__ __forceinline__ void tile_mass_sweep_y_impl(const StepArgs<R>& a,
     a.F_y[c] = F0;
     mirror(edge, a.F_y, nx, ny + 1, pad, i0, jj, F0, false, true);
   }
+  // The fluxes of the face below, widened once and carried to the next row.
+  double f0d = Pr::to_d(F0), ef0d = Pr::to_d(eF0);
   // The window values of row ii+3 and the update inputs of row ii+1 are
   // loaded before row ii is processed.
   R rn_n = R(0), en_n = R(0), vn_n = R(0);
@@ -1267,21 +1283,22 @@ __device__ __forceinline__ void tile_mass_sweep_y_impl(const StepArgs<R>& a,
       mirror(edge, a.F_y, nx, ny + 1, pad, ii + 1, jj, F1, false, true);
     }
     double r_new, e_new;
+    const double f1d = Pr::to_d(F1), ef1d = Pr::to_d(eF1);
     mass_energy_update<R, kFirst, kP2>(r_in, e_in, r_old, dt_h,
                                        a.celldx[jj] * s_cyd[k],
                                        Prec<double>::mulp<kP2>(s_coef[k], icx), ex0, ex1,
-                                       F0, F1, eF0, eF1, &r_new, &e_new);
+                                       f0d, f1d, ef0d, ef1d, &r_new, &e_new);
     store_cell(edge, s.r_out, s.r_out_r, nx, ny, pad, ii, jj, r_new);
     store_cell(edge, s.e_out, s.e_out_r, nx, ny, pad, ii, jj, e_new);
-    F0 = F1;
-    eF0 = eF1;
+    f0d = f1d;
+    ef0d = ef1d;
   }
 }
 
 template <typename R, bool kFirst>
 __device__ __forceinline__ void tile_mass_sweep_y(const StepArgs<R>& a, const SweepArgs<R>& s,
                                                   int bx, int by) {
-  FLOW_POW2_DISPATCH(R, a, a.pad + bx * kCols, a.pad + by * a.rows,
+  FLOW_POW2_DISPATCH_ALL(a, a.pad + bx * kCols, a.pad + by * a.rows,
                      (tile_mass_sweep_y_impl<R, kFirst, true>(a, s, bx, by)),
                      (tile_mass_sweep_y_impl<R, kFirst, false>(a, s, bx, by)));
 }
