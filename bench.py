@@ -58,16 +58,20 @@ KERNEL_BYTES_PER_CELL = {
 }
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per interior cell of
-# one launch, from an ncu capture of the FP64 fused kernels on the Sedov blast
-# at 2048^2 (4.19 M cells, after three timesteps); scaled to a launch by its
-# cell count.
+# one launch, from an ncu capture (one pass) of the FP64 fused kernels on the
+# Sedov blast at the benchmark size, 4096^2, after five timesteps; scaled to a
+# launch by its cell count.
 NCU_TRAFFIC_BYTES_PER_CELL = {
-    "lag_pressure": 68.7,
-    "lag_viscosity": 31.3,
+    "lag_pressure": 78.1,
+    "lag_viscosity": 38.8,
     "lag_viscous_accel": 16.1,
-    "lag_energy_dt": 48.5,
-    "mass_sweep_x": 36.3,
-    "mass_sweep_y": 44.9,
+    "lag_energy_dt": 48.6,
+    "mass_sweep_x": 53.3,
+    "mass_sweep_y": 45.4,
+    "flux_uFx": 13.1,
+    "flux_uFy": 22.3,
+    "flux_vFx": 22.2,
+    "flux_vFy": 22.2,
 }
 
 
