@@ -199,7 +199,7 @@ __global__ void __launch_bounds__(kRedThreads)
 }
 
 // Each block sums whole interior rows (threads stride along the row), so the
-// traversal needs no division of a flat index.  Two columns per iteration
+// traversal needs no division of a flat index.  Four columns per iteration
 // into two pairs of sums (independent loads and FP64 chains in flight), and
 // rho*e contracted into one FMA: two FP64 instructions per cell, the FP64
 // pipe's share of this reduction on GB300.
@@ -211,15 +211,19 @@ __global__ void __launch_bounds__(kRedThreads)
     const double* rr = rho + (size_t)ii * nx;
     const double* er = e + (size_t)ii * nx;
     int jj = pad + threadIdx.x;
-    for (; jj + kRedThreads < nx - pad; jj += 2 * kRedThreads) {
-      const double d0 = rr[jj], d1 = rr[jj + kRedThreads];
-      const double f0 = er[jj], f1 = er[jj + kRedThreads];
-      ms0 += d0;
-      ms1 += d1;
-      es0 = fma(d0, f0, es0);
-      es1 = fma(d1, f1, es1);
+    for (; jj + 3 * kRedThreads < nx - pad; jj += 4 * kRedThreads) {
+      double d[4], f[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        d[q] = rr[jj + q * kRedThreads];
+        f[q] = er[jj + q * kRedThreads];
+      }
+      ms0 += d[0] + d[1];
+      ms1 += d[2] + d[3];
+      es0 = fma(d[1], f[1], fma(d[0], f[0], es0));
+      es1 = fma(d[3], f[3], fma(d[2], f[2], es1));
     }
-    if (jj < nx - pad) {
+    for (; jj < nx - pad; jj += kRedThreads) {
       ms0 += rr[jj];
       es0 = fma(rr[jj], er[jj], es0);
     }
