@@ -40,16 +40,18 @@ enum Shape : int {
   kShInterior = 1,  // interior cells: viscosity, energy, y sweep, uF_x, vF_y
   kShFaces = 2,     // interior faces and corners: viscous accel, uF_y, vF_x
   kShSweepX = 3,    // x sweep (127 new columns per tile)
-  kShFaceU = 4,     // x-face momentum updates
-  kShFaceV = 5,     // y-face momentum updates
-  kNumShapes = 6
+  kShFaceU = 4,     // x-faces: momentum y pair for rho_u
+  kShFaceV = 5,     // y-faces: momentum y pair for rho_v
+  kShMomXV = 6,     // y-faces, 127 per tile: momentum x pair for rho_v
+  kNumShapes = 7
 };
 
 enum Phase : int {
   kPhPressure, kPhViscosity, kPhAccel, kPhEnergy,
   kPhSweepX1, kPhSweepY1, kPhSweepX2, kPhSweepY2,
-  kPhFluxUFx, kPhFluxUFy, kPhFluxVFx, kPhFluxVFy,
-  kPhUpd0V, kPhUpd0, kPhUpd1V, kPhUpd1, kPhUpd2V, kPhUpd2, kPhUpd3V, kPhUpd3,
+  // Momentum pairs (flux fused with its update); V: the pair recomputes the
+  // velocity.
+  kPhMomUxV, kPhMomUx, kPhMomUyV, kPhMomUy, kPhMomVxV, kPhMomVx, kPhMomVyV, kPhMomVy,
 };
 
 template <typename R>
@@ -78,11 +80,32 @@ struct BatchDev {
 __device__ __forceinline__ int shape_of(int ph) {
   switch (ph) {
     case kPhPressure: return kShCells;
-    case kPhAccel: case kPhFluxUFy: case kPhFluxVFx: return kShFaces;
-    case kPhSweepX1: case kPhSweepX2: return kShSweepX;
-    case kPhUpd0V: case kPhUpd0: case kPhUpd1V: case kPhUpd1: return kShFaceU;
-    case kPhUpd2V: case kPhUpd2: case kPhUpd3V: case kPhUpd3: return kShFaceV;
+    case kPhAccel: return kShFaces;
+    // x pair for rho_u: x-faces pad .. nx-pad, 127 per tile, as the x sweep.
+    case kPhSweepX1: case kPhSweepX2: case kPhMomUxV: case kPhMomUx: return kShSweepX;
+    case kPhMomUyV: case kPhMomUy: return kShFaceU;
+    case kPhMomVyV: case kPhMomVy: return kShFaceV;
+    case kPhMomVxV: case kPhMomVx: return kShMomXV;
     default: return kShInterior;
+  }
+}
+
+// The momentum pairs' tiles are called functions, compiled with their own
+// register allocation: inlined into the one kernel with every other phase,
+// they made the register allocator spill several KB per thread.  (The other
+// phases stay inlined: through the call's generic pointer to the shared
+// instance, their tiles ran slower.)  A call per tile costs nothing per cell.
+template <typename R, int kPh>
+__device__ __noinline__ void tile_call(const Instance<R>& __restrict__ I, int tx, int ty) {
+  switch (kPh) {
+    case kPhMomUxV: tile_mom_x<R, false, true>(I.a, tx, ty); break;
+    case kPhMomUx: tile_mom_x<R, false, false>(I.a, tx, ty); break;
+    case kPhMomUyV: tile_mom_y<R, false, true>(I.a, tx, ty); break;
+    case kPhMomUy: tile_mom_y<R, false, false>(I.a, tx, ty); break;
+    case kPhMomVxV: tile_mom_x<R, true, true>(I.a, tx, ty); break;
+    case kPhMomVx: tile_mom_x<R, true, false>(I.a, tx, ty); break;
+    case kPhMomVyV: tile_mom_y<R, true, true>(I.a, tx, ty); break;
+    default: tile_mom_y<R, true, false>(I.a, tx, ty); break;
   }
 }
 
@@ -97,18 +120,14 @@ __device__ __forceinline__ void run_tile(int ph, const Instance<R>& I, int tx, i
     case kPhSweepY1: tile_mass_sweep_y<R, true>(I.a, I.first, tx, ty); break;
     case kPhSweepX2: tile_mass_sweep_x<R, false>(I.a, I.second, tx, ty); break;
     case kPhSweepY2: tile_mass_sweep_y<R, false>(I.a, I.second, tx, ty); break;
-    case kPhFluxUFx: tile_flux_uFx(I.a, tx, ty); break;
-    case kPhFluxUFy: tile_flux_uFy(I.a, tx, ty); break;
-    case kPhFluxVFx: tile_flux_vFx(I.a, tx, ty); break;
-    case kPhFluxVFy: tile_flux_vFy(I.a, tx, ty); break;
-    case kPhUpd0V: tile_momentum_update<R, 0, true>(I.a, tx, ty); break;
-    case kPhUpd0: tile_momentum_update<R, 0, false>(I.a, tx, ty); break;
-    case kPhUpd1V: tile_momentum_update<R, 1, true>(I.a, tx, ty); break;
-    case kPhUpd1: tile_momentum_update<R, 1, false>(I.a, tx, ty); break;
-    case kPhUpd2V: tile_momentum_update<R, 2, true>(I.a, tx, ty); break;
-    case kPhUpd2: tile_momentum_update<R, 2, false>(I.a, tx, ty); break;
-    case kPhUpd3V: tile_momentum_update<R, 3, true>(I.a, tx, ty); break;
-    default: tile_momentum_update<R, 3, false>(I.a, tx, ty); break;
+    case kPhMomUxV: tile_call<R, kPhMomUxV>(I, tx, ty); break;
+    case kPhMomUx: tile_call<R, kPhMomUx>(I, tx, ty); break;
+    case kPhMomUyV: tile_call<R, kPhMomUyV>(I, tx, ty); break;
+    case kPhMomUy: tile_call<R, kPhMomUy>(I, tx, ty); break;
+    case kPhMomVxV: tile_call<R, kPhMomVxV>(I, tx, ty); break;
+    case kPhMomVx: tile_call<R, kPhMomVx>(I, tx, ty); break;
+    case kPhMomVyV: tile_call<R, kPhMomVyV>(I, tx, ty); break;
+    default: tile_call<R, kPhMomVy>(I, tx, ty); break;
   }
 }
 
@@ -155,15 +174,9 @@ __device__ __forceinline__ int phase_list(int tt, int* ph) {
   ph[n++] = x_first ? kPhSweepX1 : kPhSweepY1;
   ph[n++] = x_first ? kPhSweepY2 : kPhSweepX2;
   if (tt % 2) {
-    ph[n++] = kPhFluxUFx; ph[n++] = kPhUpd0V;
-    ph[n++] = kPhFluxUFy; ph[n++] = kPhUpd1;
-    ph[n++] = kPhFluxVFx; ph[n++] = kPhUpd2V;
-    ph[n++] = kPhFluxVFy; ph[n++] = kPhUpd3;
+    ph[n++] = kPhMomUxV; ph[n++] = kPhMomUy; ph[n++] = kPhMomVxV; ph[n++] = kPhMomVy;
   } else {
-    ph[n++] = kPhFluxUFy; ph[n++] = kPhUpd1V;
-    ph[n++] = kPhFluxUFx; ph[n++] = kPhUpd0;
-    ph[n++] = kPhFluxVFy; ph[n++] = kPhUpd3V;
-    ph[n++] = kPhFluxVFx; ph[n++] = kPhUpd2;
+    ph[n++] = kPhMomUyV; ph[n++] = kPhMomUx; ph[n++] = kPhMomVyV; ph[n++] = kPhMomVx;
   }
   return n;
 }
@@ -313,6 +326,7 @@ int tiles_for(int shape, int nx, int ny, int rows, int* tx) {
     case kShFaces: cols = nx - 3; nrows = ny - 3; break;
     case kShSweepX: cols = nx - 3; nrows = ny - 4; per = kCols - 1; break;
     case kShFaceU: cols = nx - 3; nrows = ny - 4; break;
+    case kShMomXV: cols = nx - 4; nrows = ny - 3; per = kCols - 1; break;
     default: cols = nx - 4; nrows = ny - 3; break;
   }
   *tx = (cols + per - 1) / per;
@@ -333,7 +347,8 @@ Instance<R> make_instance(const BatchImpl& B, int i) {
   a.edgedx = D(L.mesh); a.edgedy = D(L.mesh) + m; a.celldx = D(L.mesh) + 2 * m;
   a.celldy = D(L.mesh) + 3 * m;
   a.rho = D(L.rho); a.e = D(L.e);
-  a.rho_u = Rp(L.rho_u); a.rho_v = Rp(L.rho_v); a.u = Rp(L.u); a.v = Rp(L.v);
+  a.rho_u = Rp(L.rho_u); a.rho_v = Rp(L.rho_v); a.u = Rp(L.uF_y); a.v = Rp(L.vF_x);
+  a.u_out = Rp(L.u); a.v_out = Rp(L.v);  // the Lagrangian velocities live in uF_y/vF_x
   a.Qxx = Rp(L.Qxx); a.Qyy = Rp(L.Qyy); a.F_x = Rp(L.F_x); a.F_y = Rp(L.F_y);
   a.uF_x = Rp(L.uF_x); a.uF_y = Rp(L.uF_y); a.vF_x = Rp(L.vF_x); a.vF_y = Rp(L.vF_y);
   a.ra = D(L.ra);

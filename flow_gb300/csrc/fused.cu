@@ -57,25 +57,15 @@ __global__ void __launch_bounds__(kCols, Prec<R>::kMixed ? 7 : 5) k_mass_sweep_y
                                                         const SweepArgs<R> s) {
   tile_mass_sweep_y<R, kFirst>(a, s, blockIdx.x, blockIdx.y);
 }
-template <typename R>
-__global__ void __launch_bounds__(kCols) k_flux_uFx(const StepArgs<R> a) {
-  tile_flux_uFx(a, blockIdx.x, blockIdx.y);
+// Momentum pairs (flux fused with its update): x pairs share a row's fluxes
+// through shared memory (127 faces per CTA), y pairs march down columns.
+template <typename R, bool kV, bool kVel>
+__global__ void __launch_bounds__(kCols) k_mom_x(const StepArgs<R> a) {
+  tile_mom_x<R, kV, kVel>(a, blockIdx.x, blockIdx.y);
 }
-template <typename R>
-__global__ void __launch_bounds__(kCols) k_flux_uFy(const StepArgs<R> a) {
-  tile_flux_uFy(a, blockIdx.x, blockIdx.y);
-}
-template <typename R>
-__global__ void __launch_bounds__(kCols) k_flux_vFx(const StepArgs<R> a) {
-  tile_flux_vFx(a, blockIdx.x, blockIdx.y);
-}
-template <typename R>
-__global__ void __launch_bounds__(kCols) k_flux_vFy(const StepArgs<R> a) {
-  tile_flux_vFy(a, blockIdx.x, blockIdx.y);
-}
-template <typename R, int kWhich, bool kVel>
-__global__ void __launch_bounds__(kCols) k_momentum_update(const StepArgs<R> a) {
-  tile_momentum_update<R, kWhich, kVel>(a, blockIdx.x, blockIdx.y);
+template <typename R, bool kV, bool kVel>
+__global__ void __launch_bounds__(kCols) k_mom_y(const StepArgs<R> a) {
+  tile_mom_y<R, kV, kVel>(a, blockIdx.x, blockIdx.y);
 }
 
 inline dim3 strip_grid(int cols, int rows, int tile_rows, int cols_per_cta = kCols) {
@@ -83,12 +73,19 @@ inline dim3 strip_grid(int cols, int rows, int tile_rows, int cols_per_cta = kCo
               (unsigned)((rows + tile_rows - 1) / tile_rows));
 }
 
-template <typename R, int W, bool V>
-void launch_update(cudaStream_t s, const StepArgs<R>& a) {
-  const bool u = W < 2;
-  const int cols = u ? (a.nx + 1 - 2 * a.pad) : (a.nx - 2 * a.pad);
-  const int rows = u ? (a.ny - 2 * a.pad) : (a.ny + 1 - 2 * a.pad);
-  k_momentum_update<R, W, V><<<strip_grid(cols, rows, a.rows), kCols, 0, s>>>(a);
+// x pair for rho_u (kV false): x-faces pad .. nx-pad, 127 per CTA; for rho_v:
+// y-faces pad .. nx-pad-1.  Rows: the faces' rows.
+template <typename R, bool kV, bool kVel>
+void launch_mom_x(cudaStream_t s, const StepArgs<R>& a) {
+  const int cols = kV ? (a.nx - 2 * a.pad) : (a.nx + 1 - 2 * a.pad);
+  const int rows = kV ? (a.ny + 1 - 2 * a.pad) : (a.ny - 2 * a.pad);
+  k_mom_x<R, kV, kVel><<<strip_grid(cols, rows, a.rows, kCols - 1), kCols, 0, s>>>(a);
+}
+template <typename R, bool kV, bool kVel>
+void launch_mom_y(cudaStream_t s, const StepArgs<R>& a) {
+  const int cols = kV ? (a.nx - 2 * a.pad) : (a.nx + 1 - 2 * a.pad);
+  const int rows = kV ? (a.ny + 1 - 2 * a.pad) : (a.ny - 2 * a.pad);
+  k_mom_y<R, kV, kVel><<<strip_grid(cols, rows, a.rows), kCols, 0, s>>>(a);
 }
 
 template <typename R>
@@ -130,43 +127,26 @@ void launch_step(cudaStream_t s, const StepArgs<R>& a, int tt,
   prof.mark(x_first ? "mass_sweep_y" : "mass_sweep_x");
   launch_mass(s, a, x_first, false, second);
 
-  // Momentum: flux kernel, then update kernel, in the reference order.
-  const dim3 g_cell = strip_grid(nx - 2 * pad, ny - 2 * pad, a.rows);
-  const dim3 g_corner = strip_grid(nx + 1 - 2 * pad, ny + 1 - 2 * pad, a.rows);
+  // Momentum: each flux fused with its update, in the reference order; the
+  // pair that recomputes a velocity comes first in each chain.
   if (tt % 2) {
-    prof.mark("flux_uFx");
-    k_flux_uFx<R><<<g_cell, kCols, 0, s>>>(a);
-    prof.mark("update_rho_u");
-    launch_update<R, 0, true>(s, a);
-    prof.mark("flux_uFy");
-    k_flux_uFy<R><<<g_corner, kCols, 0, s>>>(a);
-    prof.mark("update_rho_u");
-    launch_update<R, 1, false>(s, a);
-    prof.mark("flux_vFx");
-    k_flux_vFx<R><<<g_corner, kCols, 0, s>>>(a);
-    prof.mark("update_rho_v");
-    launch_update<R, 2, true>(s, a);
-    prof.mark("flux_vFy");
-    k_flux_vFy<R><<<g_cell, kCols, 0, s>>>(a);
-    prof.mark("update_rho_v");
-    launch_update<R, 3, false>(s, a);
+    prof.mark("mom_uFx");
+    launch_mom_x<R, false, true>(s, a);
+    prof.mark("mom_uFy");
+    launch_mom_y<R, false, false>(s, a);
+    prof.mark("mom_vFx");
+    launch_mom_x<R, true, true>(s, a);
+    prof.mark("mom_vFy");
+    launch_mom_y<R, true, false>(s, a);
   } else {
-    prof.mark("flux_uFy");
-    k_flux_uFy<R><<<g_corner, kCols, 0, s>>>(a);
-    prof.mark("update_rho_u");
-    launch_update<R, 1, true>(s, a);
-    prof.mark("flux_uFx");
-    k_flux_uFx<R><<<g_cell, kCols, 0, s>>>(a);
-    prof.mark("update_rho_u");
-    launch_update<R, 0, false>(s, a);
-    prof.mark("flux_vFy");
-    k_flux_vFy<R><<<g_cell, kCols, 0, s>>>(a);
-    prof.mark("update_rho_v");
-    launch_update<R, 3, true>(s, a);
-    prof.mark("flux_vFx");
-    k_flux_vFx<R><<<g_corner, kCols, 0, s>>>(a);
-    prof.mark("update_rho_v");
-    launch_update<R, 2, false>(s, a);
+    prof.mark("mom_uFy");
+    launch_mom_y<R, false, true>(s, a);
+    prof.mark("mom_uFx");
+    launch_mom_x<R, false, false>(s, a);
+    prof.mark("mom_vFy");
+    launch_mom_y<R, true, true>(s, a);
+    prof.mark("mom_vFx");
+    launch_mom_x<R, true, false>(s, a);
   }
 }
 
@@ -268,7 +248,10 @@ int fused_solve(Mesh* mesh, int tt, double* P, double* rho, double* rho_old,
   fill_mesh_args(a, mesh, tt, reduce_array);
   a.rho = rho; a.e = e; a.rho_r = rho; a.e_r = e;
   a.P = P; a.rho_old = rho_old;
-  a.u = u; a.v = v; a.rho_u = rho_u; a.rho_v = rho_v; a.Qxx = Qxx; a.Qyy = Qyy;
+  // The Lagrangian phase and the sweeps keep the velocities in uF_y/vF_x (the
+  // fused momentum pairs store no fluxes); the advected ones land in u/v.
+  a.u = uF_y; a.v = vF_x; a.u_out = u; a.v_out = v;
+  a.rho_u = rho_u; a.rho_v = rho_v; a.Qxx = Qxx; a.Qyy = Qyy;
   a.F_x = F_x; a.F_y = F_y; a.uF_x = uF_x; a.uF_y = uF_y; a.vF_x = vF_x;
   a.vF_y = vF_y;
   // The first mass sweep writes into the two cell-sized buffers that hold
@@ -333,7 +316,8 @@ int mixed_solve(Mesh* mesh, int tt, double* rho, double* e, float* rho_u,
   fill_mesh_args(a, mesh, tt, reduce_array);
   a.rho = rho; a.e = e; a.rho_r = F(L.rho_r); a.e_r = F(L.e_r);
   a.P = nullptr; a.rho_old = nullptr;
-  a.u = F(L.u); a.v = F(L.v); a.rho_u = rho_u; a.rho_v = rho_v;
+  a.u = F(L.uF_y); a.v = F(L.vF_x); a.u_out = F(L.u); a.v_out = F(L.v);
+  a.rho_u = rho_u; a.rho_v = rho_v;
   a.Qxx = F(L.Qxx); a.Qyy = F(L.Qyy); a.F_x = F(L.F_x); a.F_y = F(L.F_y);
   a.uF_x = F(L.uF_x); a.uF_y = F(L.uF_y); a.vF_x = F(L.vF_x); a.vF_y = F(L.vF_y);
   const SweepArgs<float> first{rho, e, a.rho_r, a.e_r, D(L.s_r), D(L.s_e),

@@ -59,8 +59,10 @@ struct StepArgs {
   R* e_r;
   double* P;        // FP64 form only: the reference's P and rho_old outputs
   double* rho_old;
-  R* u;
+  R* u;             // velocities of the Lagrangian phase and the mass sweeps
   R* v;
+  R* u_out;         // the caller's velocity arrays: the advected velocities
+  R* v_out;
   R* rho_u;
   R* rho_v;
   R* Qxx;
@@ -1316,394 +1318,345 @@ __device__ __forceinline__ R momentum_upwind(R wind, R m2, R m1, R p0, R p1,
   return mc_face<R, kP2>(pos, m2, m1, p0, p1, inv_h, pos ? d_left : d_right, wind * dt_h);
 }
 
-// uF_x on interior cells (omp3/flow.c:778-823).
-template <typename R, bool kP2>
-__device__ __forceinline__ void tile_flux_uFx_impl(const StepArgs<R>& a, int bx, int by) {
-  __shared__ R s_hey[kMaxRows];
-  const int nx = a.nx, ny = a.ny, pad = a.pad;
-  const int jj = pad + bx * kCols + threadIdx.x;
-  const int i0 = pad + by * a.rows;
-  const bool edge = tile_near_edge(nx, ny, pad, pad + bx * kCols, i0, a.rows);
-  if (threadIdx.x < a.rows && i0 + (int)threadIdx.x < ny) {
-    s_hey[threadIdx.x] = geo_half<R>(a.edgedy[i0 + threadIdx.x]);
-  }
-  __syncthreads();
-  if (jj >= nx - pad) return;
-  const R dt_h = Prec<R>::from_d(a.dt_slot[1]);
-  const R iex = geo_rcp<R, kP2>(a.edgedx[jj]);
-  const R cxl = geo_v<R>(a.celldx[jj - 1]), cxr = geo_v<R>(a.celldx[jj]);
-  const int i1 = min(i0 + a.rows, ny - pad);
-  // The mass fluxes of row ii+1 are loaded before row ii is processed.
-  R Fa_n = R(0), Fb_n = R(0);
-  if (i0 < i1) {
-    Fa_n = a.F_x[fidx(nx, i0, jj)];
-    Fb_n = a.F_x[fidx(nx, i0, jj) + 1];
-  }
-  for (int ii = i0; ii < i1; ++ii) {
-    const size_t f = fidx(nx, ii, jj);
-    const R Fa = Fa_n, Fb = Fb_n;
-    if (ii + 1 < i1) {
-      Fa_n = a.F_x[f + (nx + 1)];
-      Fb_n = a.F_x[f + (nx + 2)];
-    }
-    R val;
-    if (warp_zeros(Fa, Fb)) {
-      // FP64 form: no mass through any cell of the warp; the flux is the
-      // zero mass (a zero sum scaled by a positive spacing).
-      val = sum_zeros(Fa, Fb);
-    } else {
-      const R u0 = a.u[f], u1 = a.u[f + 1];
-      const R mass = Prec<R>::template mulp<kP2>(Fa + Fb, s_hey[ii - i0]);
-      // No mass through the cell, no momentum flux (the upwind value is skipped).
-      val = Prec<R>::zero_skip_coarse(mass)
-                ? mass
-                : mass * momentum_upwind<R, kP2>(Prec<R>::half(u0 + u1), a.u[f - 1], u0, u1,
-                                                 a.u[f + 2], iex, cxl, cxr, dt_h);
-    }
-    a.uF_x[cidx(nx, ii, jj)] = val;
-    mirror(edge, a.uF_x, nx, ny, pad, ii, jj, val, false, false);
-  }
-}
+// The momentum phase fuses each momentum flux with the update it feeds, so
+// no flux array is written or read back: four kernels instead of eight.
+// Velocities: StepArgs::u/v hold the velocities the Lagrangian phase left,
+// in buffers the fused step has no other use for; the caller's arrays
+// u_out/v_out receive the advected velocities.  The pair that recomputes a
+// velocity (kVel) reads the old one from u/v and writes u_out/v_out, and the
+// pairs after it read u_out/v_out -- no kernel writes an array it reads at
+// other points, so tiles need no ordering between them.
+//
+// Pairs, each in the reference's arithmetic (omp3/flow.c:577-970):
+//   x pair, rho_u: uF_x at cells (778-823) -> rho_u at x-faces (577-600)
+//   x pair, rho_v: vF_x at corners (877-925) -> rho_v at y-faces (683-706)
+//   y pair, rho_u: uF_y at corners (826-874) -> rho_u at x-faces (622-645)
+//   y pair, rho_v: vF_y at cells (928-970) -> rho_v at y-faces (728-751)
+// A flux the reference reads from a ghost point is the mirror source's
+// (the reflective fill of the flux arrays, no sign change).
 
-// uF_y on corners (omp3/flow.c:826-874).
-template <typename R, bool kP2>
-__device__ __forceinline__ void tile_flux_uFy_impl(const StepArgs<R>& a, int bx, int by) {
-  __shared__ R s_iey[kMaxRows], s_cy[kMaxRows + 1];
-  const int nx = a.nx, ny = a.ny, pad = a.pad;
-  const int jj = pad + bx * kCols + threadIdx.x;
-  const int i0 = pad + by * a.rows;
-  const bool edge = tile_near_edge(nx, ny, pad, pad + bx * kCols, i0, a.rows);
-  if (threadIdx.x < a.rows + 1) {
-    const int ii = i0 - 1 + threadIdx.x;
-    if (ii < ny) s_cy[threadIdx.x] = geo_v<R>(a.celldy[ii]);
-    if (threadIdx.x >= 1 && ii < ny) s_iey[threadIdx.x - 1] = geo_rcp<R, kP2>(a.edgedy[ii]);
-  }
-  __syncthreads();
-  if (jj >= nx + 1 - pad) return;
-  const R dt_h = Prec<R>::from_d(a.dt_slot[1]);
-  const R hex = geo_half<R>(a.edgedx[jj]);  // edgedx * 0.5
-  const int i1 = min(i0 + a.rows, ny + 1 - pad);
-  // u of rows ii-2 .. ii+1 around corner row ii, shifted down the column.
-  // Its differences are formed when a row first needs them (fresh) and then
-  // carried while rows keep moving; rows without mass in the whole warp
-  // (FP64 form) shift the values alone.
-  ColWindow<R> uw;
-  uw.m2 = a.u[fidx(nx, i0 - 2, jj)];
-  uw.m1 = a.u[fidx(nx, i0 - 1, jj)];
-  uw.p0 = a.u[fidx(nx, i0, jj)];
-  uw.p1 = a.u[fidx(nx, i0 + 1, jj)];
-  bool fresh = false;
-  // The mass fluxes of row ii+1 and the window's next u are loaded before
-  // row ii is processed.
-  R Fa_n = R(0), Fb_n = R(0), u_next = R(0);
-  if (i0 < i1) {
-    Fa_n = a.F_y[cidx(nx, i0, jj)];
-    Fb_n = a.F_y[cidx(nx, i0, jj) - 1];
-  }
-  for (int ii = i0; ii < i1; ++ii) {
-    const int k = ii - i0;
-    const size_t c = cidx(nx, ii, jj);
-    const R Fa = Fa_n, Fb = Fb_n;
-    if (ii + 1 < i1) {
-      Fa_n = a.F_y[c + nx];
-      Fb_n = a.F_y[c + nx - 1];
-      u_next = a.u[fidx(nx, ii + 2, jj)];
-    }
-    const bool moved = !warp_zeros(Fa, Fb);
-    R val;
-    if (!moved) {
-      val = sum_zeros(Fa, Fb);
-    } else {
-      if (!fresh) uw.refresh();
-      fresh = true;
-      const R mass = Prec<R>::template mulp<kP2>(Fa + Fb, hex);
-      val = mass;
-      if (!Prec<R>::zero_skip_coarse(mass)) {
-        const R wind = Prec<R>::half(a.v[c - 1] + a.v[c]);
-        const bool pos = Prec<R>::gt0(wind);
-        val = mass * uw.template face<kP2>(pos, s_iey[k], pos ? s_cy[k] : s_cy[k + 1], wind * dt_h);
-      }
-    }
-    a.uF_y[fidx(nx, ii, jj)] = val;
-    mirror(edge, a.uF_y, nx + 1, ny + 1, pad, ii, jj, val, false, false);
-    if (ii + 1 < i1) {
-      const R next = u_next;
-      if (moved) {
-        uw.shift(next);
-      } else {
-        uw.push(next);
-        fresh = false;
-      }
-    }
-  }
-}
-
-// vF_x on corners (omp3/flow.c:877-925).
-template <typename R, bool kP2>
-__device__ __forceinline__ void tile_flux_vFx_impl(const StepArgs<R>& a, int bx, int by) {
-  __shared__ R s_hcy[kMaxRows];
-  const int nx = a.nx, ny = a.ny, pad = a.pad;
-  const int jj = pad + bx * kCols + threadIdx.x;
-  const int i0 = pad + by * a.rows;
-  const bool edge = tile_near_edge(nx, ny, pad, pad + bx * kCols, i0, a.rows);
-  if (threadIdx.x < a.rows && i0 + (int)threadIdx.x < ny) {
-    s_hcy[threadIdx.x] = geo_half<R>(a.celldy[i0 + threadIdx.x]);
-  }
-  __syncthreads();
-  if (jj >= nx + 1 - pad) return;
-  const R dt_h = Prec<R>::from_d(a.dt_slot[1]);
-  const R iex = geo_rcp<R, kP2>(a.edgedx[jj]);
-  const R cxl = geo_v<R>(a.celldx[jj - 1]), cxr = geo_v<R>(a.celldx[jj]);
-  const int i1 = min(i0 + a.rows, ny + 1 - pad);
-  R u_dn = a.u[fidx(nx, i0 - 1, jj)], F_dn = a.F_x[fidx(nx, i0 - 1, jj)];
-  // u and F_x of row ii+1 are loaded before row ii is processed.
-  R u_n = R(0), F_n = R(0);
-  if (i0 < i1) {
-    u_n = a.u[fidx(nx, i0, jj)];
-    F_n = a.F_x[fidx(nx, i0, jj)];
-  }
-  for (int ii = i0; ii < i1; ++ii) {
-    const size_t f = fidx(nx, ii, jj);
-    const size_t c = cidx(nx, ii, jj);
-    const R u0 = u_n, F0 = F_n;
-    if (ii + 1 < i1) {
-      u_n = a.u[f + (nx + 1)];
-      F_n = a.F_x[f + (nx + 1)];
-    }
-    R val;
-    if (warp_zeros(F0, F_dn)) {
-      val = sum_zeros(F0, F_dn);  // FP64 form: no mass through any corner of the warp
-    } else {
-      const R mass = Prec<R>::template mulp<kP2>(F0 + F_dn, s_hcy[ii - i0]);
-      val = Prec<R>::zero_skip_coarse(mass)
-                ? mass
-                : mass * momentum_upwind<R, kP2>(Prec<R>::half(u0 + u_dn), a.v[c - 2],
-                                                 a.v[c - 1], a.v[c], a.v[c + 1], iex, cxl,
-                                                 cxr, dt_h);
-    }
-    a.vF_x[f] = val;
-    mirror(edge, a.vF_x, nx + 1, ny + 1, pad, ii, jj, val, false, false);
-    u_dn = u0;
-    F_dn = F0;
-  }
-}
-
-// vF_y on interior cells (omp3/flow.c:928-970).
-template <typename R, bool kP2>
-__device__ __forceinline__ void tile_flux_vFy_impl(const StepArgs<R>& a, int bx, int by) {
-  __shared__ R s_iey[kMaxRows], s_cy[kMaxRows + 1];
-  const int nx = a.nx, ny = a.ny, pad = a.pad;
-  const int jj = pad + bx * kCols + threadIdx.x;
-  const int i0 = pad + by * a.rows;
-  const bool edge = tile_near_edge(nx, ny, pad, pad + bx * kCols, i0, a.rows);
-  if (threadIdx.x < a.rows + 1) {
-    const int ii = i0 - 1 + threadIdx.x;
-    if (ii < ny) s_cy[threadIdx.x] = geo_v<R>(a.celldy[ii]);
-    if (threadIdx.x >= 1 && ii < ny) s_iey[threadIdx.x - 1] = geo_rcp<R, kP2>(a.edgedy[ii]);
-  }
-  __syncthreads();
-  if (jj >= nx - pad) return;
-  const R dt_h = Prec<R>::from_d(a.dt_slot[1]);
-  const R hcx = geo_half<R>(a.celldx[jj]);  // celldx * 0.5
-  const int i1 = min(i0 + a.rows, ny - pad);
-  // v of face rows ii-1 .. ii+2 around cell row ii, shifted down the column,
-  // its differences formed lazily as in tile_flux_uFy.
-  ColWindow<R> vw;
-  vw.m2 = a.v[cidx(nx, i0 - 1, jj)];
-  vw.m1 = a.v[cidx(nx, i0, jj)];
-  vw.p0 = a.v[cidx(nx, i0 + 1, jj)];
-  vw.p1 = a.v[cidx(nx, i0 + 2, jj)];
-  bool fresh = false;
-  R F0 = a.F_y[cidx(nx, i0, jj)];
-  // The next row's mass flux and the window's next v are loaded before row
-  // ii is processed.
-  R F1_n = R(0), v_next = R(0);
-  if (i0 < i1) F1_n = a.F_y[cidx(nx, i0 + 1, jj)];
-  for (int ii = i0; ii < i1; ++ii) {
-    const int k = ii - i0;
-    const R F1 = F1_n;
-    if (ii + 1 < i1) {
-      F1_n = a.F_y[cidx(nx, ii + 2, jj)];
-      v_next = a.v[cidx(nx, ii + 3, jj)];
-    }
-    const bool moved = !warp_zeros(F0, F1);
-    R val;
-    if (!moved) {
-      val = sum_zeros(F0, F1);
-    } else {
-      if (!fresh) vw.refresh();
-      fresh = true;
-      const R mass = Prec<R>::template mulp<kP2>(F0 + F1, hcx);
-      val = mass;
-      if (!Prec<R>::zero_skip_coarse(mass)) {
-        const R wind = Prec<R>::half(vw.m1 + vw.p0);
-        const bool pos = Prec<R>::gt0(wind);
-        val = mass * vw.template face<kP2>(pos, s_iey[k], pos ? s_cy[k] : s_cy[k + 1], wind * dt_h);
-      }
-    }
-    a.vF_y[cidx(nx, ii, jj)] = val;
-    mirror(edge, a.vF_y, nx, ny, pad, ii, jj, val, false, false);
-    if (ii + 1 < i1) {
-      const R next = v_next;
-      if (moved) {
-        vw.shift(next);
-      } else {
-        vw.push(next);
-        fresh = false;
-      }
-    }
-    F0 = F1;
-  }
-}
-
-template <typename R>
-__device__ __forceinline__ void tile_flux_uFx(const StepArgs<R>& a, int bx, int by) {
-  FLOW_POW2_DISPATCH(R, a, a.pad + bx * kCols, a.pad + by * a.rows,
-                     (tile_flux_uFx_impl<R, true>(a, bx, by)),
-                     (tile_flux_uFx_impl<R, false>(a, bx, by)));
-}
-template <typename R>
-__device__ __forceinline__ void tile_flux_uFy(const StepArgs<R>& a, int bx, int by) {
-  FLOW_POW2_DISPATCH(R, a, a.pad + bx * kCols, a.pad + by * a.rows,
-                     (tile_flux_uFy_impl<R, true>(a, bx, by)),
-                     (tile_flux_uFy_impl<R, false>(a, bx, by)));
-}
-template <typename R>
-__device__ __forceinline__ void tile_flux_vFx(const StepArgs<R>& a, int bx, int by) {
-  FLOW_POW2_DISPATCH(R, a, a.pad + bx * kCols, a.pad + by * a.rows,
-                     (tile_flux_vFx_impl<R, true>(a, bx, by)),
-                     (tile_flux_vFx_impl<R, false>(a, bx, by)));
-}
-template <typename R>
-__device__ __forceinline__ void tile_flux_vFy(const StepArgs<R>& a, int bx, int by) {
-  FLOW_POW2_DISPATCH(R, a, a.pad + bx * kCols, a.pad + by * a.rows,
-                     (tile_flux_vFy_impl<R, true>(a, bx, by)),
-                     (tile_flux_vFy_impl<R, false>(a, bx, by)));
-}
-
-// Momentum updates (omp3/flow.c:577-668, 683-771).  kWhich: 0 rho_u by uF_x,
-// 1 rho_u by uF_y, 2 rho_v by vF_x, 3 rho_v by vF_y; kVel recomputes the
-// velocity from the post-advection density.
-template <typename R, int kWhich, bool kVel, bool kP2>
-__device__ __forceinline__ void tile_momentum_update_impl(const StepArgs<R>& a, int bx, int by) {
+// The momentum update of one face from its flux difference fa - fb, the
+// velocity recomputed from the post-advection density when kVel (written to
+// vout with its ghost images).  kU: an x-face (rho_u, u) else a y-face.
+// h/inv_h: the divisor's row factor, hx/ihx its column factor; w0, w1 the
+// face-density weights, ra, rb the densities either side.
+template <typename R, bool kU, bool kVel, bool kP2>
+__device__ __forceinline__ void momentum_face_update(const StepArgs<R>& a, bool edge, int ii,
+                                                     int jj, R fa, R fb, R dt_h, R hx, R ihx,
+                                                     R h, R inv_h, R w0, R w1, R* vout) {
   using Pr = Prec<R>;
-  constexpr bool kU = kWhich < 2;
+  const int nx = a.nx, ny = a.ny, pad = a.pad;
+  const size_t f = fidx(nx, ii, jj);
+  const size_t c = cidx(nx, ii, jj);
+  R* mom = kU ? a.rho_u + f : a.rho_v + c;
+  // mom - dt_h * diff / (hx * hy), the divisor rounded as the reference
+  // forms it (omp3/flow.c:581-584); no flux difference, no change (in the
+  // FP64 form equal fluxes in the whole warp skip the difference too).  The
+  // momentum is read only where it is needed.
+  R m = kVel ? *mom : R(0);
+  if (!warp_same(fa, fb)) {
+    const R diff = fa - fb;
+    if (!Pr::zero_skip_mem(diff)) {
+      if (!kVel) m = *mom;
+      m = Pr::template dsub<kP2>(m, dt_h * diff, hx * h, Pr::template mulp<kP2>(inv_h, ihx));
+      *mom = m;
+    }
+  }
+  if (kVel) {
+    const R ra = a.rho_r[c], rb = kU ? a.rho_r[c - 1] : a.rho_r[c - nx];
+    R rbar;
+    // FP64 form, power-of-two tile: equal densities and weights either side
+    // in the whole warp give the face density 2 (ra w0) exactly.
+    if (kP2 && !Pr::kMixed && warp_all(lane_same(ra, rb) && lane_same(w0, w1))) {
+      rbar = Pr::twice(Pr::template mulp<true>(ra, w0));
+    } else {
+      rbar = face_average<R, kP2>(ra, w0, rb, w1);
+    }
+    const R vel = face_velocity(m, rbar);
+    if (kU) {
+      vout[f] = vel;
+      mirror(edge, vout, nx + 1, ny, pad, ii, jj, vel, true, false);
+    } else {
+      vout[c] = vel;
+      mirror(edge, vout, nx, ny + 1, pad, ii, jj, vel, false, true);
+    }
+  }
+}
+
+// x pairs: the flux points of a row are spread over the CTA's threads and
+// shared through shared memory; 127 faces per CTA of 128 threads.
+//   kV = false (rho_u): thread t holds the uF_x of cell c0 + t (c0 = pad-1 +
+//     127 bx; ghost cells pad-1 and nx-pad take their mirror source's) and,
+//     for t >= 1, updates x-face c0 + t from cells c0 + t - 1 and c0 + t.
+//   kV = true (rho_v): thread t holds the vF_x of corner c0 + t (c0 = pad +
+//     127 bx) and, for t < 127, updates y-face c0 + t from corners c0 + t and
+//     c0 + t + 1.
+template <typename R, bool kV, bool kVel, bool kP2>
+__device__ __forceinline__ void tile_mom_x_impl(const StepArgs<R>& a, int bx, int by) {
+  using Pr = Prec<R>;
+  __shared__ R s_half[kMaxRows], s_h[kMaxRows], s_row[kMaxRows];
+  __shared__ R s_wy0[kMaxRows], s_wy1[kMaxRows];
+  __shared__ R sF[kCols];
+  const int nx = a.nx, ny = a.ny, pad = a.pad;
+  const int t = threadIdx.x;
+  const int c0 = (kV ? pad : pad - 1) + bx * (kCols - 1);
+  const int j = c0 + t;
+  const int i0 = pad + by * a.rows;
+  const bool edge = tile_near_edge(nx, ny, pad, c0, i0, a.rows);
+  const int i1 = min(i0 + a.rows, kV ? ny + 1 - pad : ny - pad);
+  if (t < a.rows) {
+    const int ii = i0 + t;
+    if (ii < ny) {
+      // Flux: edgedy/2 (uF_x) or celldy/2 (vF_x); update divisor: celldy.
+      s_half[t] = geo_half<R>(kV ? a.celldy[ii] : a.edgedy[ii]);
+      s_h[t] = geo_v<R>(a.celldy[ii]);
+      s_row[t] = geo_rcp<R, kP2>(a.celldy[ii]);
+      if (kV && kVel) {
+        s_wy0[t] = geo_half_ratio<R, kP2>(a.celldy[ii], a.edgedy[ii]);
+        s_wy1[t] = geo_half_ratio<R, kP2>(a.celldy[ii - 1], a.edgedy[ii]);
+      }
+    }
+  }
+  // The flux point: cells pad-1 .. nx-pad (rho_u), corners pad .. nx-pad (rho_v).
+  const bool flux_ok = kV ? (j < nx + 1 - pad) : (j <= nx - pad);
+  const int js = kV ? j : (j < pad ? 2 * pad - 1 - j : (j >= nx - pad ? 2 * (nx - pad) - 1 - j : j));
+  const bool upd = kV ? (t < kCols - 1 && j < nx - pad) : (t >= 1 && j < nx + 1 - pad);
+  R iex = R(0), cxl = R(0), cxr = R(0), hx = R(0), ihx = R(0), wx0 = R(0), wx1 = R(0);
+  if (flux_ok) {
+    iex = geo_rcp<R, kP2>(a.edgedx[js]);
+    cxl = geo_v<R>(a.celldx[js - 1]);
+    cxr = geo_v<R>(a.celldx[js]);
+  }
+  if (upd) {
+    hx = geo_v<R>(a.edgedx[j]);
+    ihx = geo_rcp<R, kP2>(a.edgedx[j]);
+    if (!kV && kVel) {
+      wx0 = geo_half_ratio<R, kP2>(a.celldx[j], a.edgedx[j]);
+      wx1 = geo_half_ratio<R, kP2>(a.celldx[j - 1], a.edgedx[j]);
+    }
+  }
+  const R dt_h = Pr::from_d(a.dt_slot[1]);
+  // Velocities the fluxes read: rho_u's uF_x reads u before its update when
+  // this pair updates it, else after; rho_v's vF_x reads the advected u and
+  // v before or after its own update likewise.
+  const R* uu = (!kV && kVel) ? a.u : a.u_out;
+  const R* vv = kVel ? a.v : a.v_out;
+  R* const vout = kV ? a.v_out : a.u_out;
+  __syncthreads();
+  if (i0 >= i1) return;
+  // Row ii+1's mass fluxes (and for rho_v the u below and at the corner) are
+  // loaded before row ii is processed.
+  R Fa_n = R(0), Fb_n = R(0), u0_n = R(0);
+  R F_dn = R(0), u_dn = R(0);
+  auto load = [&](int ii) {
+    if (!flux_ok) return;
+    const size_t f = fidx(nx, ii, js);
+    Fa_n = a.F_x[f];
+    Fb_n = kV ? R(0) : a.F_x[f + 1];
+    if (kV) u0_n = uu[f];
+  };
+  if (kV && flux_ok) {
+    const size_t f = fidx(nx, i0 - 1, j);
+    F_dn = a.F_x[f];
+    u_dn = uu[f];
+  }
+  load(i0);
+  for (int ii = i0; ii < i1; ++ii) {
+    const int k = ii - i0;
+    const R Fa = Fa_n, Fb = Fb_n, u0 = u0_n;
+    if (ii + 1 < i1) load(ii + 1);
+    R val = R(0);
+    if (flux_ok) {
+      const size_t f = fidx(nx, ii, js);
+      if (!kV) {
+        if (warp_zeros(Fa, Fb)) {
+          // FP64 form: no mass through any cell of the warp; the flux is the
+          // zero mass (a zero sum scaled by a positive spacing).
+          val = sum_zeros(Fa, Fb);
+        } else {
+          const R ua = uu[f], ub = uu[f + 1];
+          const R mass = Pr::template mulp<kP2>(Fa + Fb, s_half[k]);
+          // No mass through the cell, no momentum flux.
+          val = Pr::zero_skip_coarse(mass)
+                    ? mass
+                    : mass * momentum_upwind<R, kP2>(Pr::half(ua + ub), uu[f - 1], ua, ub,
+                                                     uu[f + 2], iex, cxl, cxr, dt_h);
+        }
+      } else {
+        const size_t c = cidx(nx, ii, js);
+        if (warp_zeros(Fa, F_dn)) {
+          val = sum_zeros(Fa, F_dn);  // FP64 form: no mass through any corner of the warp
+        } else {
+          const R mass = Pr::template mulp<kP2>(Fa + F_dn, s_half[k]);
+          val = Pr::zero_skip_coarse(mass)
+                    ? mass
+                    : mass * momentum_upwind<R, kP2>(Pr::half(u0 + u_dn), vv[c - 2], vv[c - 1],
+                                                     vv[c], vv[c + 1], iex, cxl, cxr, dt_h);
+        }
+        F_dn = Fa;
+        u_dn = u0;
+      }
+    }
+    sF[t] = val;
+    __syncthreads();
+    if (upd) {
+      const R fa = kV ? sF[t + 1] : sF[t];
+      const R fb = kV ? sF[t] : sF[t - 1];
+      momentum_face_update<R, !kV, kVel, kP2>(a, edge, ii, j, fa, fb, dt_h, hx, ihx, s_h[k],
+                                              s_row[k], kV ? s_wy0[k] : wx0,
+                                              kV ? s_wy1[k] : wx1, vout);
+    }
+    __syncthreads();
+  }
+}
+
+// y pairs: each thread marches down its column, carrying the flux of the
+// previous row.
+//   kV = false (rho_u): uF_y at corners i0 .. i1 of column jj (u window
+//     rows ci-2 .. ci+1), updates x-faces i0 .. i1-1 from corners ii, ii+1.
+//   kV = true (rho_v): vF_y at cells i0-1 .. i1-1 (v window rows ci-1 ..
+//     ci+2; the ghost rows pad-1 and ny-pad take their mirror source's),
+//     updates y-faces i0 .. i1-1 from cells ii-1, ii.
+// The windows form their differences only where mass moves in the warp
+// (FP64 form), as the y mass sweep does.
+template <typename R, bool kV, bool kVel, bool kP2>
+__device__ __forceinline__ void tile_mom_y_impl(const StepArgs<R>& a, int bx, int by) {
+  using Pr = Prec<R>;
+  // Flux tables over flux rows q = ci - fr0 (fr0 the first flux row): 1/edgedy
+  // of the row, celldy of the row below (s_cy[q]) and of the row (s_cy[q + 1]).
+  __shared__ R s_iey[kMaxRows + 2], s_cy[kMaxRows + 3];
   __shared__ R s_h[kMaxRows], s_row[kMaxRows], s_wy0[kMaxRows], s_wy1[kMaxRows];
   const int nx = a.nx, ny = a.ny, pad = a.pad;
   const int jj = pad + bx * kCols + threadIdx.x;
   const int i0 = pad + by * a.rows;
   const bool edge = tile_near_edge(nx, ny, pad, pad + bx * kCols, i0, a.rows);
-  const double dt_h = a.dt_slot[1];
+  const int i1 = min(i0 + a.rows, kV ? ny + 1 - pad : ny - pad);
+  // Flux rows: corners i0 .. i1 (rho_u); cells i0-1 .. i1-1 (rho_v), a ghost
+  // row computed at its mirror source.
+  const int fr0 = kV ? i0 - 1 : i0;
+  const int nfr = i1 - i0 + 1;
+  auto src_row = [&](int ci) {
+    if (!kV) return ci;
+    return ci < pad ? 2 * pad - 1 - ci : (ci >= ny - pad ? 2 * (ny - pad) - 1 - ci : ci);
+  };
+  // (Entries of a ghost flux row are never used: its flux is its mirror
+  // source's.)
+  for (int q = threadIdx.x; q <= nfr; q += kCols) {
+    const int ci = fr0 + q;
+    if (q < nfr) s_iey[q] = geo_rcp<R, kP2>(a.edgedy[ci]);
+    s_cy[q] = geo_v<R>(a.celldy[ci - 1]);
+  }
   if (threadIdx.x < a.rows) {
     const int ii = i0 + threadIdx.x;
     if (ii < ny) {
-      // Row factor of the flux divergence: 1/celldy for x fluxes of rho_u
-      // and rho_v, 1/edgedy for the y fluxes.
-      const double h = (kWhich == 0 || kWhich == 2) ? a.celldy[ii] : a.edgedy[ii];
-      s_h[threadIdx.x] = geo_v<R>(h);
-      s_row[threadIdx.x] = geo_rcp<R, kP2>(h);
-      if (!kU && kVel) {
-        const double ey = a.edgedy[ii];
-        s_wy0[threadIdx.x] = geo_half_ratio<R, kP2>(a.celldy[ii], ey);
-        s_wy1[threadIdx.x] = geo_half_ratio<R, kP2>(a.celldy[ii - 1], ey);
+      // Update divisor row factor: edgedy for both y pairs.
+      s_h[threadIdx.x] = geo_v<R>(a.edgedy[ii]);
+      s_row[threadIdx.x] = geo_rcp<R, kP2>(a.edgedy[ii]);
+      if (kV && kVel) {
+        s_wy0[threadIdx.x] = geo_half_ratio<R, kP2>(a.celldy[ii], a.edgedy[ii]);
+        s_wy1[threadIdx.x] = geo_half_ratio<R, kP2>(a.celldy[ii - 1], a.edgedy[ii]);
       }
     }
   }
   __syncthreads();
-  const int col_end = kU ? nx + 1 - pad : nx - pad;
-  const int row_end = kU ? ny - pad : ny + 1 - pad;
-  if (jj >= col_end) return;
-  const double hx = (kWhich == 0 || kWhich == 2) ? a.edgedx[jj] : a.celldx[jj];
-  const R hx_r = geo_v<R>(hx);
-  const R ihx = geo_rcp<R, kP2>(hx);
-  const R dt_h_r = Pr::from_d(dt_h);
+  if (jj >= (kV ? nx - pad : nx + 1 - pad) || i0 >= i1) return;
+  const R dt_h = Pr::from_d(a.dt_slot[1]);
+  const R hcol = geo_half<R>(kV ? a.celldx[jj] : a.edgedx[jj]);  // flux: celldx/2 or edgedx/2
+  const R hx = geo_v<R>(a.celldx[jj]);
+  const R ihx = geo_rcp<R, kP2>(a.celldx[jj]);
   R wx0 = R(0), wx1 = R(0);
-  if (kU && kVel) {
-    const double ex = a.edgedx[jj];
-    wx0 = geo_half_ratio<R, kP2>(a.celldx[jj], ex);
-    wx1 = geo_half_ratio<R, kP2>(a.celldx[jj - 1], ex);
+  if (!kV && kVel) {
+    wx0 = geo_half_ratio<R, kP2>(a.celldx[jj], a.edgedx[jj]);
+    wx1 = geo_half_ratio<R, kP2>(a.celldx[jj - 1], a.edgedx[jj]);
   }
-  const int i1 = min(i0 + a.rows, row_end);
-  if (i0 >= i1) return;
-  // The inputs of row ii: the fluxes fa, fb (difference fa - fb), the
-  // momentum m and the densities ra, rb either side of the face.  Row ii+1's
-  // are loaded before row ii is processed (its stores do not touch them), so
-  // that two rows of loads are in flight; where row ii+1's fb or rb is row
-  // ii's fa or ra (y fluxes, v faces), it is carried instead.
-  struct RowIn {
-    R fa, fb, m, ra, rb;
-  };
-  auto load = [&](int ii, const RowIn* prev) {
-    RowIn in;
-    const size_t f = fidx(nx, ii, jj);
-    const size_t c = cidx(nx, ii, jj);
-    if (kWhich == 0) { in.fa = a.uF_x[c]; in.fb = a.uF_x[c - 1]; }
-    else if (kWhich == 1) { in.fa = a.uF_y[f + (nx + 1)]; in.fb = prev ? prev->fa : a.uF_y[f]; }
-    else if (kWhich == 2) { in.fa = a.vF_x[f + 1]; in.fb = a.vF_x[f]; }
-    else { in.fa = a.vF_y[c]; in.fb = prev ? prev->fa : a.vF_y[c - nx]; }
-    // The momentum is needed ahead only where the velocity is recomputed;
-    // otherwise it is read where a flux difference changes it (rows at rest
-    // do not read it).
-    in.m = R(0);
-    if (kVel) in.m = kU ? a.rho_u[f] : a.rho_v[c];
-    in.ra = in.rb = R(0);
-    if (kVel) {
-      in.ra = a.rho_r[c];
-      in.rb = kU ? a.rho_r[c - 1] : (prev ? prev->ra : a.rho_r[c - nx]);
+  // The window's velocity: before this pair's update when it recomputes it.
+  const R* w = kV ? (kVel ? a.v : a.v_out) : (kVel ? a.u : a.u_out);
+  const R* vwind = a.v;  // rho_u's wind: v before the rho_v pairs
+  R* const vout = kV ? a.v_out : a.u_out;
+  auto widx = [&](int row) { return kV ? cidx(nx, row, jj) : fidx(nx, row, jj); };
+  // Window of flux row ci: rows ci-2 .. ci+1 (corners) or ci-1 .. ci+2 (cells).
+  const int wlo = kV ? -1 : -2;
+  ColWindow<R> win;
+  int wrow = src_row(fr0);  // flux row the window is at
+  win.m2 = w[widx(wrow + wlo)];
+  win.m1 = w[widx(wrow + wlo + 1)];
+  win.p0 = w[widx(wrow + wlo + 2)];
+  win.p1 = w[widx(wrow + wlo + 3)];
+  bool fresh = false;
+  // Flux at flux row ci (the window at ci) from its mass fluxes Fa, Fb; q its
+  // table index.
+  auto flux_at = [&](int ci, int q, R Fa, R Fb) -> R {
+    const size_t c = cidx(nx, ci, jj);
+    if (warp_zeros(Fa, Fb)) {
+      fresh = false;  // the window shifts its values alone until mass moves
+      return sum_zeros(Fa, Fb);
     }
-    return in;
+    if (!fresh) win.refresh();
+    fresh = true;
+    const R mass = Pr::template mulp<kP2>(Fa + Fb, hcol);
+    if (Pr::zero_skip_coarse(mass)) return mass;
+    const R wind = kV ? Pr::half(win.m1 + win.p0) : Pr::half(vwind[c - 1] + vwind[c]);
+    const bool pos = Pr::gt0(wind);
+    return mass * win.template face<kP2>(pos, s_iey[q], pos ? s_cy[q] : s_cy[q + 1], wind * dt_h);
   };
-  RowIn cur = load(i0, nullptr);
+  // The mass fluxes of flux row ci and the value that moves the window there
+  // from row ci-1, loaded a row ahead of their use.
+  R Fa_n = R(0), Fb_n = R(0), wv_n = R(0);
+  auto load = [&](int ci) {
+    const size_t c = cidx(nx, ci, jj);
+    Fa_n = a.F_y[c];
+    Fb_n = kV ? a.F_y[c + nx] : a.F_y[c - 1];
+    wv_n = w[widx(ci + wlo + 3)];
+  };
+  load(wrow);
+  R prev = flux_at(wrow, wrow - fr0, Fa_n, Fb_n);
+  const R top = prev;  // rho_v: the flux of the first flux row's mirror source
+  // A loop row computes its flux row unless that is a ghost row or (bottom
+  // wall) the row computed above.
+  const bool bottom = kV && fr0 != src_row(fr0);
+  if (i0 < i1 && !(bottom && i0 == src_row(fr0)) && src_row(kV ? i0 : i0 + 1) == (kV ? i0 : i0 + 1)) {
+    load(kV ? i0 : i0 + 1);
+  } else if (bottom && i0 + 1 < i1) {
+    load(i0 + 1);
+  }
   for (int ii = i0; ii < i1; ++ii) {
     const int k = ii - i0;
-    const size_t f = fidx(nx, ii, jj);
-    const size_t c = cidx(nx, ii, jj);
-    RowIn nxt = cur;
-    if (ii + 1 < i1) nxt = load(ii + 1, &cur);
-    const R fa = cur.fa, fb = cur.fb;
-    R* mom = kU ? a.rho_u + f : a.rho_v + c;
-    // mom - dt_h * diff / (hx * hy), the divisor rounded as the reference
-    // forms it (omp3/flow.c:581-584); no flux difference, no change (in the
-    // FP64 form equal fluxes in the whole warp skip the difference too).
-    R m = cur.m;
-    if (!warp_same(fa, fb)) {
-      const R diff = fa - fb;
-      if (!Pr::zero_skip_mem(diff)) {
-        if (!kVel) m = *mom;
-        m = Pr::template dsub<kP2>(m, dt_h_r * diff, hx_r * s_h[k],
-                                   Pr::template mulp<kP2>(s_row[k], ihx));
-        *mom = m;
-      }
+    // The new flux row: corner ii+1 (rho_u), cell ii (rho_v).
+    const int ci = kV ? ii : ii + 1;
+    const int cs = src_row(ci);
+    R cur;
+    if (kV && cs != ci) {
+      // A ghost row (top wall): its mirror source is the previous flux row.
+      cur = prev;
+    } else if (bottom && ci == wrow) {
+      cur = top;  // the bottom wall's first interior row: computed already
+    } else {
+      const R Fa = Fa_n, Fb = Fb_n, wv = wv_n;
+      const int cn = ci + 1;
+      if (ii + 1 < i1 && src_row(cn) == cn) load(cn);
+      if (fresh) win.shift(wv);
+      else win.push(wv);
+      ++wrow;
+      cur = flux_at(cs, cs - fr0, Fa, Fb);
     }
-    if (kVel) {
-      const R ra = cur.ra, rb = cur.rb;
-      const R w0 = kU ? wx0 : s_wy0[k], w1 = kU ? wx1 : s_wy1[k];
-      R rbar;
-      // FP64 form, power-of-two tile: equal densities and weights either
-      // side in the whole warp give the face density 2 (ra w0) exactly.
-      if (kP2 && !Pr::kMixed && warp_all(lane_same(ra, rb) && lane_same(w0, w1))) {
-        rbar = Pr::twice(Pr::template mulp<true>(ra, w0));
-      } else {
-        rbar = face_average<R, kP2>(ra, w0, rb, w1);
-      }
-      const R vel = face_velocity(m, rbar);
-      if (kU) {
-        a.u[f] = vel;
-        mirror(edge, a.u, nx + 1, ny, pad, ii, jj, vel, true, false);
-      } else {
-        a.v[c] = vel;
-        mirror(edge, a.v, nx, ny + 1, pad, ii, jj, vel, false, true);
-      }
-    }
-    cur = nxt;
+    momentum_face_update<R, !kV, kVel, kP2>(a, edge, ii, jj, cur, prev, dt_h, hx, ihx, s_h[k],
+                                            s_row[k], kV ? s_wy0[k] : wx0, kV ? s_wy1[k] : wx1,
+                                            vout);
+    prev = cur;
   }
 }
 
-template <typename R, int kWhich, bool kVel>
-__device__ __forceinline__ void tile_momentum_update(const StepArgs<R>& a, int bx, int by) {
+template <typename R, bool kV, bool kVel>
+__device__ __forceinline__ void tile_mom_x(const StepArgs<R>& a, int bx, int by) {
+  FLOW_POW2_DISPATCH(R, a, (kV ? a.pad : a.pad - 1) + bx * (kCols - 1), a.pad + by * a.rows,
+                     (tile_mom_x_impl<R, kV, kVel, true>(a, bx, by)),
+                     (tile_mom_x_impl<R, kV, kVel, false>(a, bx, by)));
+}
+template <typename R, bool kV, bool kVel>
+__device__ __forceinline__ void tile_mom_y(const StepArgs<R>& a, int bx, int by) {
   FLOW_POW2_DISPATCH(R, a, a.pad + bx * kCols, a.pad + by * a.rows,
-                     (tile_momentum_update_impl<R, kWhich, kVel, true>(a, bx, by)),
-                     (tile_momentum_update_impl<R, kWhich, kVel, false>(a, bx, by)));
+                     (tile_mom_y_impl<R, kV, kVel, true>(a, bx, by)),
+                     (tile_mom_y_impl<R, kV, kVel, false>(a, bx, by)));
 }
 
 }  // namespace tiles
