@@ -46,15 +46,13 @@ KERNEL_BYTES_PER_CELL = {
     "lag_energy_dt": 8 * 7,      # rho, P, e, Qxx, Qyy, u, v in (e out where the cell is compressed)
     "mass_sweep_x": 8 * 6,       # rho, e, u in; rho, e, F_x out
     "mass_sweep_y": 8 * 6,
-    "flux_uFx": 8 * 2,           # F_x in; uF_x out (u where mass moves)
-    "flux_uFy": 8 * 3,           # F_y, u in; uF_y out
-    "flux_vFx": 8 * 3,           # F_x, u in; vF_x out
-    "flux_vFy": 8 * 3,           # F_y, v in; vF_y out
-    # Two launches per step: flux, rho_u, rho in and u out (32 B) for the one
-    # that recomputes the velocity, flux in (8 B) for the other (rho_u where
-    # the flux difference acts); the mean per launch.
-    "update_rho_u": 20,
-    "update_rho_v": 20,
+    # Momentum pairs (flux fused with its update), one launch per step each;
+    # the velocity is recomputed (rho, the momentum in, the velocity out:
+    # 24 B) in every other step's launch, so half of it counts per launch.
+    "mom_uFx": 8 + 12,           # F_x in (u where mass moves)
+    "mom_uFy": 16 + 12,          # F_y, u in
+    "mom_vFx": 16 + 12,          # F_x, u in (v where mass moves)
+    "mom_vFy": 16 + 12,          # F_y, v in
 }
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per interior cell of
@@ -68,10 +66,6 @@ NCU_TRAFFIC_BYTES_PER_CELL = {
     "lag_energy_dt": 48.6,
     "mass_sweep_x": 53.3,
     "mass_sweep_y": 45.4,
-    "flux_uFx": 13.1,
-    "flux_uFy": 22.3,
-    "flux_vFx": 22.2,
-    "flux_vFy": 22.2,
 }
 
 
@@ -586,7 +580,7 @@ def run_gpu(args):
         "forms": forms,
         "cpu_baseline": cpu,
         "clocks": clk.summary(),
-        "gpu_launches": 15 * args.steps,
+        "gpu_launches": 11 * args.steps,  # 10 timestep kernels + the conservation totals
         "mass": mass, "energy": energy,
     }
     print(json.dumps(line), flush=True)
