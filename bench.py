@@ -40,9 +40,9 @@ B_ALG_FP64 = 64  # bytes/cell-step: rho, e, rho_u, rho_v read + written once
 # where the flow moves (momenta, energy) are counted as read; their writes on
 # moving cells come on top.  Used for the per-kernel HBM roofline.
 KERNEL_BYTES_PER_CELL = {
-    "lag_pressure": 8 * 10,      # rho, e, rho_u, rho_v in; P, rho_old, u, v, 1/rho_x, 1/rho_y out
+    "lag_pressure": 8 * 8,       # rho, e, rho_u, rho_v in; P, rho_old, u, v out
     "lag_viscosity": 8 * 5,      # u, v, rho in; Qxx, Qyy out
-    "lag_viscous_accel": 8 * 2,  # Qxx, Qyy in (momenta and velocities where a stress gradient acts)
+    "lag_viscous_accel": 8 * 2,  # Qxx, Qyy in (momenta, densities, velocities where a stress gradient acts)
     "lag_energy_dt": 8 * 7,      # rho, P, e, Qxx, Qyy, u, v in (e out where the cell is compressed)
     "mass_sweep_x": 8 * 6,       # rho, e, u in; rho, e, F_x out
     "mass_sweep_y": 8 * 6,

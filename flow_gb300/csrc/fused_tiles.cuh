@@ -303,9 +303,8 @@ __device__ __forceinline__ R face_average(R a, R wa, R b, R wb) {
 
 // Pressure (EOS on the fly) -> face momenta -> velocities.  Covers every cell
 // (the FP64 form writes P and rho_old for ghosts too, as equation_of_state and
-// the rho_old copy of the reference do) and every interior x/y face.  The
-// reciprocal of each face density is kept in F_x/F_y (free until the
-// advection phase) for the viscous update.  omp3/flow.c:55-70, 110-158.
+// the rho_old copy of the reference do) and every interior x/y face.
+// omp3/flow.c:55-70, 110-158.
 template <typename R, bool kP2>
 __device__ __forceinline__ void tile_lag_pressure_impl(const StepArgs<R>& a, int bx, int by) {
   using Pr = Prec<R>;
@@ -412,7 +411,6 @@ __device__ __forceinline__ void tile_lag_pressure_impl(const StepArgs<R>& a, int
       }
       const R vel = face_velocity(mom, rbar);
       a.u[f] = vel;
-      a.uF_x[f] = rbar;
       mirror(edge, a.u, nx + 1, ny, pad, ii, jj, vel, true, false);
     }
     if (ii >= pad && ii < ny + 1 - pad && jj >= pad && jj < nx - pad) {
@@ -432,7 +430,6 @@ __device__ __forceinline__ void tile_lag_pressure_impl(const StepArgs<R>& a, int
       }
       const R vel = face_velocity(mom, rbar);
       a.v[c] = vel;
-      a.vF_y[c] = rbar;
       mirror(edge, a.v, nx, ny + 1, pad, ii, jj, vel, false, true);
     }
     P_dn = Pc;
@@ -521,11 +518,11 @@ __device__ __forceinline__ void tile_lag_viscosity(const StepArgs<R>& a, int bx,
 }
 
 // Viscous acceleration of the face momenta and velocities,
-// omp3/flow.c:212-244.  The face-density reciprocals come from F_x/F_y.
+// omp3/flow.c:212-244.  The face densities are formed again where needed.
 template <typename R, bool kP2>
 __device__ __forceinline__ void tile_lag_viscous_accel_impl(const StepArgs<R>& a, int bx, int by) {
   using Pr = Prec<R>;
-  __shared__ R s_cy[kMaxRows], s_icy[kMaxRows];
+  __shared__ R s_cy[kMaxRows], s_icy[kMaxRows], s_wy0[kMaxRows], s_wy1[kMaxRows];
   const int nx = a.nx, ny = a.ny, pad = a.pad;
   const int jj = pad + bx * kCols + threadIdx.x;
   const int i0 = pad + by * a.rows;
@@ -535,12 +532,20 @@ __device__ __forceinline__ void tile_lag_viscous_accel_impl(const StepArgs<R>& a
     if (ii < ny) {
       s_cy[threadIdx.x] = geo_v<R>(a.celldy[ii]);
       s_icy[threadIdx.x] = geo_rcp<R, kP2>(a.celldy[ii]);
+      s_wy0[threadIdx.x] = geo_half_ratio<R, kP2>(a.celldy[ii], a.edgedy[ii]);
+      s_wy1[threadIdx.x] = geo_half_ratio<R, kP2>(a.celldy[ii - 1], a.edgedy[ii]);
     }
   }
   __syncthreads();
   if (jj >= nx + 1 - pad) return;
   const R cx = geo_v<R>(a.celldx[jj]);
   const R icx = geo_rcp<R, kP2>(a.celldx[jj]);
+  // Face-density weights (the pressure phase's): where a stress gradient
+  // changes a face's momentum, the face density is formed again from the two
+  // cell densities -- the same expression on the same values, so the same
+  // number -- rather than stored for every face by the pressure phase.
+  const R wx0 = geo_half_ratio<R, kP2>(a.celldx[jj], a.edgedx[jj]);
+  const R wx1 = geo_half_ratio<R, kP2>(a.celldx[jj - 1], a.edgedx[jj]);
   const R dt = Pr::from_d(a.dt);
   const int i1 = min(i0 + a.rows, ny + 1 - pad);
   R qy_dn = (jj < nx - pad) ? a.Qyy[cidx(nx, i0 - 1, jj)] : R(0);
@@ -567,7 +572,9 @@ __device__ __forceinline__ void tile_lag_viscous_accel_impl(const StepArgs<R>& a
         const R dqx = q1 - q0;
         if (!Pr::zero_skip_mem(dqx)) {
           const R mom = Pr::template dsub<kP2>(a.rho_u[f], dt * dqx, cx, icx);
-          const R vel = face_velocity(mom, a.uF_x[f]);
+          const size_t c = cidx(nx, ii, jj);
+          const R vel =
+              face_velocity(mom, face_average<R, kP2>(a.rho_r[c], wx0, a.rho_r[c - 1], wx1));
           a.rho_u[f] = mom;
           a.u[f] = vel;
           mirror(edge, a.u, nx + 1, ny, pad, ii, jj, vel, true, false);
@@ -580,7 +587,8 @@ __device__ __forceinline__ void tile_lag_viscous_accel_impl(const StepArgs<R>& a
         const R dqy = qy - qy_dn;
         if (!Pr::zero_skip_mem(dqy)) {
           const R mom = Pr::template dsub<kP2>(a.rho_v[c], dt * dqy, s_cy[k], s_icy[k]);
-          const R vel = face_velocity(mom, a.vF_y[c]);
+          const R vel = face_velocity(
+              mom, face_average<R, kP2>(a.rho_r[c], s_wy0[k], a.rho_r[c - nx], s_wy1[k]));
           a.rho_v[c] = mom;
           a.v[c] = vel;
           mirror(edge, a.v, nx, ny + 1, pad, ii, jj, vel, false, true);
@@ -1339,11 +1347,13 @@ __device__ __forceinline__ R momentum_upwind(R wind, R m2, R m1, R p0, R p1,
 // velocity recomputed from the post-advection density when kVel (written to
 // vout with its ghost images).  kU: an x-face (rho_u, u) else a y-face.
 // h/inv_h: the divisor's row factor, hx/ihx its column factor; w0, w1 the
-// face-density weights, ra, rb the densities either side.
+// face-density weights, ra, rb the densities either side and m_in the
+// momentum (kVel; loaded by the caller, possibly a row ahead).
 template <typename R, bool kU, bool kVel, bool kP2>
 __device__ __forceinline__ void momentum_face_update(const StepArgs<R>& a, bool edge, int ii,
                                                      int jj, R fa, R fb, R dt_h, R hx, R ihx,
-                                                     R h, R inv_h, R w0, R w1, R* vout) {
+                                                     R h, R inv_h, R w0, R w1, R m_in, R ra,
+                                                     R rb, R* vout) {
   using Pr = Prec<R>;
   const int nx = a.nx, ny = a.ny, pad = a.pad;
   const size_t f = fidx(nx, ii, jj);
@@ -1353,7 +1363,7 @@ __device__ __forceinline__ void momentum_face_update(const StepArgs<R>& a, bool 
   // forms it (omp3/flow.c:581-584); no flux difference, no change (in the
   // FP64 form equal fluxes in the whole warp skip the difference too).  The
   // momentum is read only where it is needed.
-  R m = kVel ? *mom : R(0);
+  R m = kVel ? m_in : R(0);
   if (!warp_same(fa, fb)) {
     const R diff = fa - fb;
     if (!Pr::zero_skip_mem(diff)) {
@@ -1363,7 +1373,6 @@ __device__ __forceinline__ void momentum_face_update(const StepArgs<R>& a, bool 
     }
   }
   if (kVel) {
-    const R ra = a.rho_r[c], rb = kU ? a.rho_r[c - 1] : a.rho_r[c - nx];
     R rbar;
     // FP64 form, power-of-two tile: equal densities and weights either side
     // in the whole warp give the face density 2 (ra w0) exactly.
@@ -1502,9 +1511,16 @@ __device__ __forceinline__ void tile_mom_x_impl(const StepArgs<R>& a, int bx, in
     if (upd) {
       const R fa = kV ? sF[t + 1] : sF[t];
       const R fb = kV ? sF[t] : sF[t - 1];
+      const size_t c = cidx(nx, ii, j);
+      R m = R(0), ra = R(0), rb = R(0);
+      if (kVel) {
+        m = kV ? a.rho_v[c] : a.rho_u[fidx(nx, ii, j)];
+        ra = a.rho_r[c];
+        rb = kV ? a.rho_r[c - nx] : a.rho_r[c - 1];
+      }
       momentum_face_update<R, !kV, kVel, kP2>(a, edge, ii, j, fa, fb, dt_h, hx, ihx, s_h[k],
                                               s_row[k], kV ? s_wy0[k] : wx0,
-                                              kV ? s_wy1[k] : wx1, vout);
+                                              kV ? s_wy1[k] : wx1, m, ra, rb, vout);
     }
     __syncthreads();
   }
@@ -1611,6 +1627,18 @@ __device__ __forceinline__ void tile_mom_y_impl(const StepArgs<R>& a, int bx, in
   load(wrow);
   R prev = flux_at(wrow, wrow - fr0, Fa_n, Fb_n);
   const R top = prev;  // rho_v: the flux of the first flux row's mirror source
+  // The update inputs of face row ii (momentum and densities, kVel), loaded a
+  // row ahead; rho_v's lower density is the row below's upper one.
+  R m_n = R(0), ra_n = R(0), rb_n = R(0);
+  auto load_upd = [&](int ii) {
+    if (!kVel) return;
+    const size_t c = cidx(nx, ii, jj);
+    m_n = kV ? a.rho_v[c] : a.rho_u[fidx(nx, ii, jj)];
+    rb_n = kV ? ra_n : a.rho_r[c - 1];
+    ra_n = a.rho_r[c];
+  };
+  if (kVel && kV) ra_n = a.rho_r[cidx(nx, i0 - 1, jj)];
+  load_upd(i0);
   // A loop row computes its flux row unless that is a ghost row or (bottom
   // wall) the row computed above.
   const bool bottom = kV && fr0 != src_row(fr0);
@@ -1639,9 +1667,11 @@ __device__ __forceinline__ void tile_mom_y_impl(const StepArgs<R>& a, int bx, in
       ++wrow;
       cur = flux_at(cs, cs - fr0, Fa, Fb);
     }
+    const R m = m_n, ra = ra_n, rb = rb_n;
+    if (ii + 1 < i1) load_upd(ii + 1);
     momentum_face_update<R, !kV, kVel, kP2>(a, edge, ii, jj, cur, prev, dt_h, hx, ihx, s_h[k],
                                             s_row[k], kV ? s_wy0[k] : wx0, kV ? s_wy1[k] : wx1,
-                                            vout);
+                                            m, ra, rb, vout);
     prev = cur;
   }
 }
