@@ -17,16 +17,39 @@ using namespace tiles;
 // bits; all candidates are non-negative, so bit order = value order).
 constexpr int kRaMinBits = 6;
 
+// Programmatic dependent launch: every kernel of the step is launched with
+// programmatic stream serialisation, lets the next kernel launch as soon as
+// all its own CTAs have started (pdl_trigger), and waits for the previous
+// kernel to complete (its writes visible) before touching the state
+// (pdl_wait).  The next kernel's CTAs thus take the SMs its predecessor's
+// last wave leaves idle.  Outside such a launch both are no-ops.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() {
+  asm volatile("griddepcontrol.launch_dependents;" :::);
+}
+
 template <typename R>
 __global__ void __launch_bounds__(kCols) k_lag_pressure(const StepArgs<R> a) {
+  pdl_wait();
+  pdl_trigger();
+  // The first kernel of the step clears the CFL minimum and the block ticket
+  // of the shock-heating kernel (three kernels later, which waits for it).
+  if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) {
+    *reinterpret_cast<unsigned long long*>(a.ra + kRaTicket) = 0ull;
+    *a.min_slot = ~0ull;
+  }
   tile_lag_pressure(a, blockIdx.x, blockIdx.y);
 }
 template <typename R>
 __global__ void __launch_bounds__(kCols) k_lag_viscosity(const StepArgs<R> a) {
+  pdl_wait();
+  pdl_trigger();
   tile_lag_viscosity(a, blockIdx.x, blockIdx.y);
 }
 template <typename R>
 __global__ void __launch_bounds__(kCols) k_lag_viscous_accel(const StepArgs<R> a) {
+  pdl_wait();
+  pdl_trigger();
   tile_lag_viscous_accel(a, blockIdx.x, blockIdx.y);
 }
 // Shock heating + CFL minimum; the last block to finish (ticket in
@@ -34,6 +57,8 @@ __global__ void __launch_bounds__(kCols) k_lag_viscous_accel(const StepArgs<R> a
 template <typename R>
 __global__ void __launch_bounds__(kCols) k_lag_energy_dt(const StepArgs<R> a) {
   __shared__ bool s_last;
+  pdl_wait();
+  pdl_trigger();
   tile_lag_energy_dt(a, blockIdx.x, blockIdx.y);
   if (threadIdx.x == 0) {
     __threadfence();
@@ -50,22 +75,46 @@ __global__ void __launch_bounds__(kCols) k_lag_energy_dt(const StepArgs<R> a) {
 template <typename R, bool kFirst>
 __global__ void __launch_bounds__(kCols, Prec<R>::kMixed ? 8 : 7) k_mass_sweep_x(const StepArgs<R> a,
                                                         const SweepArgs<R> s) {
+  pdl_wait();
+  pdl_trigger();
   tile_mass_sweep_x<R, kFirst>(a, s, blockIdx.x, blockIdx.y);
 }
 template <typename R, bool kFirst>
 __global__ void __launch_bounds__(kCols, Prec<R>::kMixed ? 7 : 5) k_mass_sweep_y(const StepArgs<R> a,
                                                         const SweepArgs<R> s) {
+  pdl_wait();
+  pdl_trigger();
   tile_mass_sweep_y<R, kFirst>(a, s, blockIdx.x, blockIdx.y);
 }
 // Momentum pairs (flux fused with its update): x pairs share a row's fluxes
 // through shared memory (127 faces per CTA), y pairs march down columns.
 template <typename R, bool kV, bool kVel>
 __global__ void __launch_bounds__(kCols) k_mom_x(const StepArgs<R> a) {
+  pdl_wait();
+  pdl_trigger();
   tile_mom_x<R, kV, kVel>(a, blockIdx.x, blockIdx.y);
 }
 template <typename R, bool kV, bool kVel>
 __global__ void __launch_bounds__(kCols) k_mom_y(const StepArgs<R> a) {
+  pdl_wait();
+  pdl_trigger();
   tile_mom_y<R, kV, kVel>(a, blockIdx.x, blockIdx.y);
+}
+
+// Launches kernel k with programmatic stream serialisation (see pdl_wait).
+template <typename... KArgs, typename... Args>
+void launch_pdl(void (*k)(KArgs...), dim3 grid, cudaStream_t s, Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = dim3(kCols);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, k, args...);
 }
 
 inline dim3 strip_grid(int cols, int rows, int tile_rows, int cols_per_cta = kCols) {
@@ -79,13 +128,13 @@ template <typename R, bool kV, bool kVel>
 void launch_mom_x(cudaStream_t s, const StepArgs<R>& a) {
   const int cols = kV ? (a.nx - 2 * a.pad) : (a.nx + 1 - 2 * a.pad);
   const int rows = kV ? (a.ny + 1 - 2 * a.pad) : (a.ny - 2 * a.pad);
-  k_mom_x<R, kV, kVel><<<strip_grid(cols, rows, a.rows, kCols - 1), kCols, 0, s>>>(a);
+  launch_pdl(k_mom_x<R, kV, kVel>, strip_grid(cols, rows, a.rows, kCols - 1), s, a);
 }
 template <typename R, bool kV, bool kVel>
 void launch_mom_y(cudaStream_t s, const StepArgs<R>& a) {
   const int cols = kV ? (a.nx - 2 * a.pad) : (a.nx + 1 - 2 * a.pad);
   const int rows = kV ? (a.ny + 1 - 2 * a.pad) : (a.ny - 2 * a.pad);
-  k_mom_y<R, kV, kVel><<<strip_grid(cols, rows, a.rows), kCols, 0, s>>>(a);
+  launch_pdl(k_mom_y<R, kV, kVel>, strip_grid(cols, rows, a.rows), s, a);
 }
 
 template <typename R>
@@ -94,13 +143,13 @@ void launch_mass(cudaStream_t s, const StepArgs<R>& a, bool dir_y, bool first,
   const int pad = a.pad;
   if (dir_y) {
     const dim3 g = strip_grid(a.nx - 2 * pad, a.ny - 2 * pad, a.rows);
-    if (first) k_mass_sweep_y<R, true><<<g, kCols, 0, s>>>(a, sw);
-    else k_mass_sweep_y<R, false><<<g, kCols, 0, s>>>(a, sw);
+    if (first) launch_pdl(k_mass_sweep_y<R, true>, g, s, a, sw);
+    else launch_pdl(k_mass_sweep_y<R, false>, g, s, a, sw);
   } else {
     // Faces pad .. nx-pad; every CTA advances 127 columns.
     const dim3 g = strip_grid(a.nx + 1 - 2 * pad, a.ny - 2 * pad, a.rows, kCols - 1);
-    if (first) k_mass_sweep_x<R, true><<<g, kCols, 0, s>>>(a, sw);
-    else k_mass_sweep_x<R, false><<<g, kCols, 0, s>>>(a, sw);
+    if (first) launch_pdl(k_mass_sweep_x<R, true>, g, s, a, sw);
+    else launch_pdl(k_mass_sweep_x<R, false>, g, s, a, sw);
   }
 }
 
@@ -111,15 +160,13 @@ void launch_step(cudaStream_t s, const StepArgs<R>& a, int tt,
                  StepProfiler& prof) {
   const int nx = a.nx, ny = a.ny, pad = a.pad;
   prof.mark("lag_pressure");
-  k_lag_pressure<R><<<strip_grid(nx, ny, a.rows), kCols, 0, s>>>(a);
+  launch_pdl(k_lag_pressure<R>, strip_grid(nx, ny, a.rows), s, a);
   prof.mark("lag_viscosity");
-  k_lag_viscosity<R><<<strip_grid(nx - 2 * pad, ny - 2 * pad, a.rows), kCols, 0, s>>>(a);
+  launch_pdl(k_lag_viscosity<R>, strip_grid(nx - 2 * pad, ny - 2 * pad, a.rows), s, a);
   prof.mark("lag_viscous_accel");
-  k_lag_viscous_accel<R><<<strip_grid(nx + 1 - 2 * pad, ny + 1 - 2 * pad, a.rows), kCols, 0, s>>>(a);
+  launch_pdl(k_lag_viscous_accel<R>, strip_grid(nx + 1 - 2 * pad, ny + 1 - 2 * pad, a.rows), s, a);
   prof.mark("lag_energy_dt");
-  cudaMemsetAsync(a.ra + kRaTicket, 0, sizeof(double), s);
-  cudaMemsetAsync(a.ra + kRaMinBits, 0xff, sizeof(double), s);
-  k_lag_energy_dt<R><<<strip_grid(nx - 2 * pad, ny - 2 * pad, a.rows), kCols, 0, s>>>(a);
+  launch_pdl(k_lag_energy_dt<R>, strip_grid(nx - 2 * pad, ny - 2 * pad, a.rows), s, a);
 
   const bool x_first = (tt % 2 == 0);
   prof.mark(x_first ? "mass_sweep_x" : "mass_sweep_y");
