@@ -16,6 +16,8 @@ using namespace tiles;
 // reduce_array slot holding the running CFL minimum of the fused step (uint64
 // bits; all candidates are non-negative, so bit order = value order).
 constexpr int kRaMinBits = 6;
+// reduce_array slot holding the whole-mesh power-of-two flag of the step.
+constexpr int kRaMeshPow2 = 7;
 
 // Programmatic dependent launch: every kernel of the step is launched with
 // programmatic stream serialisation, lets the next kernel launch as soon as
@@ -26,6 +28,26 @@ constexpr int kRaMinBits = 6;
 __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 __device__ __forceinline__ void pdl_trigger() {
   asm volatile("griddepcontrol.launch_dependents;" :::);
+}
+
+// Whether every mesh spacing (celldx, edgedx: 0 .. nx; celldy, edgedy: 0 ..
+// ny) is a positive normal power of two: one block, the first kernel of the
+// step.  The tiles then skip their own spacing tests (block_mesh_pow2).
+constexpr int kPow2Threads = 1024;
+__global__ void __launch_bounds__(kPow2Threads)
+    k_mesh_pow2(int nx, int ny, const double* celldx, const double* edgedx,
+                const double* celldy, const double* edgedy, unsigned long long* flag) {
+  pdl_wait();
+  pdl_trigger();
+  bool ok = true;
+  for (int j = threadIdx.x; j <= nx; j += kPow2Threads) {
+    ok = ok && d_is_pow2(celldx[j]) && d_is_pow2(edgedx[j]);
+  }
+  for (int i = threadIdx.x; i <= ny; i += kPow2Threads) {
+    ok = ok && d_is_pow2(celldy[i]) && d_is_pow2(edgedy[i]);
+  }
+  ok = __syncthreads_and(ok) != 0;
+  if (threadIdx.x == 0) *flag = ok ? 1ull : 0ull;
 }
 
 template <typename R>
@@ -103,10 +125,11 @@ __global__ void __launch_bounds__(kCols) k_mom_y(const StepArgs<R> a) {
 
 // Launches kernel k with programmatic stream serialisation (see pdl_wait).
 template <typename... KArgs, typename... Args>
-void launch_pdl(void (*k)(KArgs...), dim3 grid, cudaStream_t s, Args... args) {
+void launch_pdl_block(void (*k)(KArgs...), dim3 grid, dim3 block, cudaStream_t s,
+                      Args... args) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = grid;
-  cfg.blockDim = dim3(kCols);
+  cfg.blockDim = block;
   cfg.dynamicSmemBytes = 0;
   cfg.stream = s;
   cudaLaunchAttribute attr[1];
@@ -115,6 +138,10 @@ void launch_pdl(void (*k)(KArgs...), dim3 grid, cudaStream_t s, Args... args) {
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   cudaLaunchKernelEx(&cfg, k, args...);
+}
+template <typename... KArgs, typename... Args>
+void launch_pdl(void (*k)(KArgs...), dim3 grid, cudaStream_t s, Args... args) {
+  launch_pdl_block(k, grid, dim3(kCols), s, args...);
 }
 
 inline dim3 strip_grid(int cols, int rows, int tile_rows, int cols_per_cta = kCols) {
@@ -159,6 +186,12 @@ void launch_step(cudaStream_t s, const StepArgs<R>& a, int tt,
                  const SweepArgs<R>& first, const SweepArgs<R>& second,
                  StepProfiler& prof) {
   const int nx = a.nx, ny = a.ny, pad = a.pad;
+  prof.mark("lag_pressure");
+  // The whole-mesh spacing test the tiles read (the mesh may change between
+  // calls, so it is formed every step; one block, a few microseconds).
+  prof.mark("mesh_pow2");
+  launch_pdl_block(k_mesh_pow2, dim3(1), dim3(kPow2Threads), s, nx, ny, a.celldx, a.edgedx,
+                   a.celldy, a.edgedy, const_cast<unsigned long long*>(a.mesh_pow2));
   prof.mark("lag_pressure");
   launch_pdl(k_lag_pressure<R>, strip_grid(nx, ny, a.rows), s, a);
   prof.mark("lag_viscosity");
@@ -226,6 +259,7 @@ void fill_mesh_args(StepArgs<R>& a, const Mesh* mesh, int tt, double* ra) {
   a.celldy = mesh->celldy;
   a.ra = ra;
   a.min_slot = reinterpret_cast<unsigned long long*>(ra + kRaMinBits);
+  a.mesh_pow2 = reinterpret_cast<unsigned long long*>(ra + kRaMeshPow2);
   a.dt_slot = ra + kRaDt;
   a.dt = mesh->dt;
   a.dt_h = mesh->dt_h;

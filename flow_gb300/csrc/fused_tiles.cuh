@@ -75,6 +75,9 @@ struct StepArgs {
   R* vF_y;
   double* ra;                  // caller scratch (reduce_array)
   unsigned long long* min_slot;  // running CFL minimum (FP64 bit pattern)
+  // 1 when every mesh spacing is a positive normal power of two (formed on
+  // the device at the start of the step); null or 0: tested per tile.
+  const unsigned long long* mesh_pow2;
   double* dt_slot;             // [0] dt, [1] dt_h for the advection phase
   double dt, dt_h, max_dt;     // Lagrangian-phase pair (host values), max_dt
   int first_step;
@@ -186,6 +189,8 @@ __device__ __forceinline__ bool tile_near_edge(int nx, int ny, int pad, int col0
 // multiplications by their reciprocals.  Block-uniform (barrier).
 template <typename R>
 __device__ __forceinline__ bool block_mesh_pow2(const StepArgs<R>& a, int col0, int row0) {
+  // The whole mesh (one cached word) before the tile's own spacings.
+  if (a.mesh_pow2 && *a.mesh_pow2 == 1ull) return true;
   bool ok = true;
   for (int j = col0 - 2 + (int)threadIdx.x; j < col0 + kCols + 2; j += kCols) {
     if (j >= 0 && j <= a.nx) ok = ok && d_is_pow2(a.celldx[j]) && d_is_pow2(a.edgedx[j]);
