@@ -186,7 +186,6 @@ void launch_step(cudaStream_t s, const StepArgs<R>& a, int tt,
                  const SweepArgs<R>& first, const SweepArgs<R>& second,
                  StepProfiler& prof) {
   const int nx = a.nx, ny = a.ny, pad = a.pad;
-  prof.mark("lag_pressure");
   // The whole-mesh spacing test the tiles read (the mesh may change between
   // calls, so it is formed every step; one block, a few microseconds).
   prof.mark("mesh_pow2");
