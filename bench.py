@@ -53,6 +53,7 @@ KERNEL_BYTES_PER_CELL = {
     "mom_uFy": 16 + 12,          # F_y, u in
     "mom_vFx": 16 + 12,          # F_x, u in (v where mass moves)
     "mom_vFy": 16 + 12,          # F_y, v in
+    "mesh_pow2": 0,              # the step's one-block mesh test (spacings only)
 }
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per interior cell of

@@ -114,12 +114,12 @@ __device__ __forceinline__ void run_tile(int ph, const Instance<R>& I, int tx, i
   switch (ph) {
     case kPhPressure: tile_lag_pressure(I.a, tx, ty); break;
     case kPhViscosity: tile_lag_viscosity(I.a, tx, ty); break;
-    case kPhAccel: tile_lag_viscous_accel(I.a, tx, ty); break;
+    case kPhAccel: tile_lag_viscous_accel<R, false>(I.a, tx, ty); break;
     case kPhEnergy: tile_lag_energy_dt(I.a, tx, ty); break;
-    case kPhSweepX1: tile_mass_sweep_x<R, true>(I.a, I.first, tx, ty); break;
-    case kPhSweepY1: tile_mass_sweep_y<R, true>(I.a, I.first, tx, ty); break;
-    case kPhSweepX2: tile_mass_sweep_x<R, false>(I.a, I.second, tx, ty); break;
-    case kPhSweepY2: tile_mass_sweep_y<R, false>(I.a, I.second, tx, ty); break;
+    case kPhSweepX1: tile_mass_sweep_x<R, true, false>(I.a, I.first, tx, ty); break;
+    case kPhSweepY1: tile_mass_sweep_y<R, true, false>(I.a, I.first, tx, ty); break;
+    case kPhSweepX2: tile_mass_sweep_x<R, false, false>(I.a, I.second, tx, ty); break;
+    case kPhSweepY2: tile_mass_sweep_y<R, false, false>(I.a, I.second, tx, ty); break;
     case kPhMomUxV: tile_call<R, kPhMomUxV>(I, tx, ty); break;
     case kPhMomUx: tile_call<R, kPhMomUx>(I, tx, ty); break;
     case kPhMomUyV: tile_call<R, kPhMomUyV>(I, tx, ty); break;

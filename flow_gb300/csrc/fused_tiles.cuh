@@ -524,7 +524,10 @@ __device__ __forceinline__ void tile_lag_viscosity(const StepArgs<R>& a, int bx,
 
 // Viscous acceleration of the face momenta and velocities,
 // omp3/flow.c:212-244.  The face densities are formed again where needed.
-template <typename R, bool kP2>
+// kEarly: the first row's loads are issued before the barrier that publishes
+// the row tables (off in the persistent batched kernel, whose register budget
+// is spent across all its phases).
+template <typename R, bool kP2, bool kEarly>
 __device__ __forceinline__ void tile_lag_viscous_accel_impl(const StepArgs<R>& a, int bx, int by) {
   using Pr = Prec<R>;
   __shared__ R s_cy[kMaxRows], s_icy[kMaxRows], s_wy0[kMaxRows], s_wy1[kMaxRows];
@@ -541,8 +544,26 @@ __device__ __forceinline__ void tile_lag_viscous_accel_impl(const StepArgs<R>& a
       s_wy1[threadIdx.x] = geo_half_ratio<R, kP2>(a.celldy[ii - 1], a.edgedy[ii]);
     }
   }
+  const bool col_ok = jj < nx + 1 - pad;
+  const int i1 = min(i0 + a.rows, ny + 1 - pad);
+  // The stresses of row ii+1 are loaded before row ii is processed (the
+  // first row's before the barrier that publishes the row tables, kEarly).
+  R q1_n = R(0), q0_n = R(0), qy_n = R(0), qy_dn = R(0);
+  auto load = [&](int ii) {
+    const size_t c = cidx(nx, ii, jj);
+    if (ii < ny - pad) {
+      q1_n = a.Qxx[c];
+      q0_n = a.Qxx[c - 1];
+    }
+    if (jj < nx - pad) qy_n = a.Qyy[c];
+  };
+  auto prime = [&]() {
+    if (jj < nx - pad) qy_dn = a.Qyy[cidx(nx, i0 - 1, jj)];
+    if (i0 < i1) load(i0);
+  };
+  if (kEarly && col_ok) prime();
   __syncthreads();
-  if (jj >= nx + 1 - pad) return;
+  if (!col_ok) return;
   const R cx = geo_v<R>(a.celldx[jj]);
   const R icx = geo_rcp<R, kP2>(a.celldx[jj]);
   // Face-density weights (the pressure phase's): where a stress gradient
@@ -552,19 +573,7 @@ __device__ __forceinline__ void tile_lag_viscous_accel_impl(const StepArgs<R>& a
   const R wx0 = geo_half_ratio<R, kP2>(a.celldx[jj], a.edgedx[jj]);
   const R wx1 = geo_half_ratio<R, kP2>(a.celldx[jj - 1], a.edgedx[jj]);
   const R dt = Pr::from_d(a.dt);
-  const int i1 = min(i0 + a.rows, ny + 1 - pad);
-  R qy_dn = (jj < nx - pad) ? a.Qyy[cidx(nx, i0 - 1, jj)] : R(0);
-  // The stresses of row ii+1 are loaded before row ii is processed.
-  R q1_n = R(0), q0_n = R(0), qy_n = R(0);
-  auto load = [&](int ii) {
-    const size_t c = cidx(nx, ii, jj);
-    if (ii < ny - pad) {
-      q1_n = a.Qxx[c];
-      q0_n = a.Qxx[c - 1];
-    }
-    if (jj < nx - pad) qy_n = a.Qyy[c];
-  };
-  if (i0 < i1) load(i0);
+  if (!kEarly) prime();
   for (int ii = i0; ii < i1; ++ii) {
     const int k = ii - i0;
     const R q1 = q1_n, q0 = q0_n, qy = qy_n;
@@ -604,11 +613,11 @@ __device__ __forceinline__ void tile_lag_viscous_accel_impl(const StepArgs<R>& a
   }
 }
 
-template <typename R>
+template <typename R, bool kEarly = true>
 __device__ __forceinline__ void tile_lag_viscous_accel(const StepArgs<R>& a, int bx, int by) {
   FLOW_POW2_DISPATCH(R, a, a.pad + bx * kCols, a.pad + by * a.rows,
-                     (tile_lag_viscous_accel_impl<R, true>(a, bx, by)),
-                     (tile_lag_viscous_accel_impl<R, false>(a, bx, by)));
+                     (tile_lag_viscous_accel_impl<R, true, kEarly>(a, bx, by)),
+                     (tile_lag_viscous_accel_impl<R, false, kEarly>(a, bx, by)));
 }
 
 __device__ __forceinline__ unsigned long long warp_min_u64(unsigned long long x) {
@@ -1052,7 +1061,7 @@ struct SweepArgs {
 // face is shared with the next CTA and written only by its owner).  In the
 // second sweep of a step the old density of a cell is read from rho just
 // before the same thread overwrites that cell.
-template <typename R, bool kFirst, bool kP2>
+template <typename R, bool kFirst, bool kP2, bool kEarly>
 __device__ __forceinline__ void tile_mass_sweep_x_impl(const StepArgs<R>& a,
                                                        const SweepArgs<R>& s, int bx, int by) {
   using Pr = Prec<R>;
@@ -1090,11 +1099,12 @@ __device__ __forceinline__ void tile_mass_sweep_x_impl(const StepArgs<R>& a,
     icx_r = Pr::from_d(icx);
   }
   const R dt_r = Pr::from_d(dt), dt_h_r = Pr::from_d(dt_h);
-  __syncthreads();
   const int i1 = min(i0 + a.rows, ny - pad);
   // Row ii+1's face velocity and the update inputs of its cell are loaded
-  // before row ii is processed; a warp whose faces are all at rest carries
-  // no flux and reads nothing else (the flux core returns +0 for them).
+  // before row ii is processed (the first row's before the barrier that
+  // publishes the row tables, kEarly); a warp whose faces are all at rest
+  // carries no flux and reads nothing else (the flux core returns +0 for
+  // them).
   R u0_n = R(0);
   double rin_n = 0.0, ein_n = 0.0, rold_n = 0.0;
   auto load = [&](int ii) {
@@ -1106,7 +1116,9 @@ __device__ __forceinline__ void tile_mass_sweep_x_impl(const StepArgs<R>& a,
       rold_n = kFirst ? rin_n : a.rho[c];
     }
   };
-  if (i0 < i1) load(i0);
+  if (kEarly && i0 < i1) load(i0);
+  __syncthreads();
+  if (!kEarly && i0 < i1) load(i0);
   for (int ii = i0; ii < i1; ++ii) {
     const int k = ii - i0;
     const R u0 = u0_n;
@@ -1145,17 +1157,17 @@ __device__ __forceinline__ void tile_mass_sweep_x_impl(const StepArgs<R>& a,
   }
 }
 
-template <typename R, bool kFirst>
+template <typename R, bool kFirst, bool kEarly = true>
 __device__ __forceinline__ void tile_mass_sweep_x(const StepArgs<R>& a, const SweepArgs<R>& s,
                                                   int bx, int by) {
   FLOW_POW2_DISPATCH_ALL(a, a.pad + bx * (kCols - 1), a.pad + by * a.rows,
-                     (tile_mass_sweep_x_impl<R, kFirst, true>(a, s, bx, by)),
-                     (tile_mass_sweep_x_impl<R, kFirst, false>(a, s, bx, by)));
+                     (tile_mass_sweep_x_impl<R, kFirst, true, kEarly>(a, s, bx, by)),
+                     (tile_mass_sweep_x_impl<R, kFirst, false, kEarly>(a, s, bx, by)));
 }
 
 // y sweep: each thread marches down its column; face row ii+1 is computed
 // in iteration ii and reused by the cell below.
-template <typename R, bool kFirst, bool kP2>
+template <typename R, bool kFirst, bool kP2, bool kEarly>
 __device__ __forceinline__ void tile_mass_sweep_y_impl(const StepArgs<R>& a,
                                                        const SweepArgs<R>& s, int bx, int by) {
   using Pr = Prec<R>;
@@ -1183,11 +1195,7 @@ __device__ __forceinline__ void tile_mass_sweep_y_impl(const StepArgs<R>& a,
       }
     }
   }
-  __syncthreads();
-  if (jj >= nx - pad) return;
-  const double icx = geo_rcp_d<R, kP2>(a.celldx[jj]);
-  const double ex0 = a.edgedx[jj], ex1 = a.edgedx[jj + 1];
-  const R ex0_r = geo_v<R>(ex0), dt_r = Pr::from_d(dt), dt_h_r = Pr::from_d(dt_h);
+  const bool col_ok = jj < nx - pad;
   const int i1 = min(i0 + a.rows, ny - pad);
   const int last_face = ny - pad;  // the north boundary face row
   // Windows at face row f: cells f-2..f+1 (densities and energies with their
@@ -1199,11 +1207,28 @@ __device__ __forceinline__ void tile_mass_sweep_y_impl(const StepArgs<R>& a,
   // operands, so the same values.
   ColSteps<R> rw;
   ColWindow<R> ew;
-  R vm = a.v[cidx(nx, i0 - 1, jj)];
-  R v0 = a.v[cidx(nx, i0, jj)];
-  R vp = a.v[cidx(nx, i0 + 1, jj)];
+  R vm = R(0), v0 = R(0), vp = R(0);
   R dvm, dvp, dv2;
-  {
+  // The window values of row ii+3 and the update inputs of row ii+1 are
+  // loaded before row ii is processed.
+  R rn_n = R(0), en_n = R(0), vn_n = R(0);
+  double rin_n = 0.0, ein_n = 0.0, rold_n = 0.0;
+  auto load = [&](int ii) {
+    const size_t c_next = cidx(nx, ii + 2, jj);
+    rn_n = s.r_in_r[c_next];
+    en_n = s.e_in_r[c_next];
+    vn_n = a.v[c_next];
+    const size_t c = cidx(nx, ii, jj);
+    rin_n = s.r_in[c];
+    ein_n = s.e_in[c];
+    rold_n = kFirst ? rin_n : a.rho[c];
+  };
+  // The windows' first values and the first row's inputs are loaded before
+  // the barrier that publishes the row tables (kEarly), else after it.
+  auto prime = [&]() {
+    vm = a.v[cidx(nx, i0 - 1, jj)];
+    v0 = a.v[cidx(nx, i0, jj)];
+    vp = a.v[cidx(nx, i0 + 1, jj)];
     R r[4], e[4];
     for (int q = 0; q < 4; ++q) {
       const size_t c = cidx(nx, i0 - 2 + q, jj);
@@ -1212,7 +1237,17 @@ __device__ __forceinline__ void tile_mass_sweep_y_impl(const StepArgs<R>& a,
     }
     rw.m2 = r[0]; rw.m1 = r[1]; rw.p0 = r[2]; rw.p1 = r[3];
     ew.m2 = e[0]; ew.m1 = e[1]; ew.p0 = e[2]; ew.p1 = e[3];
+  };
+  if (kEarly && col_ok) {
+    prime();
+    if (i0 < i1) load(i0);
   }
+  __syncthreads();
+  if (!col_ok) return;
+  const double icx = geo_rcp_d<R, kP2>(a.celldx[jj]);
+  const double ex0 = a.edgedx[jj], ex1 = a.edgedx[jj + 1];
+  const R ex0_r = geo_v<R>(ex0), dt_r = Pr::from_d(dt), dt_h_r = Pr::from_d(dt_h);
+  if (!kEarly) prime();
   auto refresh = [&]() {
     rw.refresh();
     ew.refresh();
@@ -1244,21 +1279,7 @@ __device__ __forceinline__ void tile_mass_sweep_y_impl(const StepArgs<R>& a,
   }
   // The fluxes of the face below, widened once and carried to the next row.
   double f0d = Pr::to_d(F0), ef0d = Pr::to_d(eF0);
-  // The window values of row ii+3 and the update inputs of row ii+1 are
-  // loaded before row ii is processed.
-  R rn_n = R(0), en_n = R(0), vn_n = R(0);
-  double rin_n = 0.0, ein_n = 0.0, rold_n = 0.0;
-  auto load = [&](int ii) {
-    const size_t c_next = cidx(nx, ii + 2, jj);
-    rn_n = s.r_in_r[c_next];
-    en_n = s.e_in_r[c_next];
-    vn_n = a.v[c_next];
-    const size_t c = cidx(nx, ii, jj);
-    rin_n = s.r_in[c];
-    ein_n = s.e_in[c];
-    rold_n = kFirst ? rin_n : a.rho[c];
-  };
-  if (i0 < i1) load(i0);
+  if (!kEarly && i0 < i1) load(i0);
   for (int ii = i0; ii < i1; ++ii) {
     const int k = ii - i0;
     const R rn = rn_n, en = en_n, vn = vn_n;
@@ -1310,12 +1331,12 @@ __device__ __forceinline__ void tile_mass_sweep_y_impl(const StepArgs<R>& a,
   }
 }
 
-template <typename R, bool kFirst>
+template <typename R, bool kFirst, bool kEarly = true>
 __device__ __forceinline__ void tile_mass_sweep_y(const StepArgs<R>& a, const SweepArgs<R>& s,
                                                   int bx, int by) {
   FLOW_POW2_DISPATCH_ALL(a, a.pad + bx * kCols, a.pad + by * a.rows,
-                     (tile_mass_sweep_y_impl<R, kFirst, true>(a, s, bx, by)),
-                     (tile_mass_sweep_y_impl<R, kFirst, false>(a, s, bx, by)));
+                     (tile_mass_sweep_y_impl<R, kFirst, true, kEarly>(a, s, bx, by)),
+                     (tile_mass_sweep_y_impl<R, kFirst, false, kEarly>(a, s, bx, by)));
 }
 
 // ===========================================================================
@@ -1456,10 +1477,9 @@ __device__ __forceinline__ void tile_mom_x_impl(const StepArgs<R>& a, int bx, in
   const R* uu = (!kV && kVel) ? a.u : a.u_out;
   const R* vv = kVel ? a.v : a.v_out;
   R* const vout = kV ? a.v_out : a.u_out;
-  __syncthreads();
-  if (i0 >= i1) return;
   // Row ii+1's mass fluxes (and for rho_v the u below and at the corner) are
-  // loaded before row ii is processed.
+  // loaded before row ii is processed; the first row's before the barrier
+  // that publishes the row tables.
   R Fa_n = R(0), Fb_n = R(0), u0_n = R(0);
   R F_dn = R(0), u_dn = R(0);
   auto load = [&](int ii) {
@@ -1469,12 +1489,16 @@ __device__ __forceinline__ void tile_mom_x_impl(const StepArgs<R>& a, int bx, in
     Fb_n = kV ? R(0) : a.F_x[f + 1];
     if (kV) u0_n = uu[f];
   };
-  if (kV && flux_ok) {
-    const size_t f = fidx(nx, i0 - 1, j);
-    F_dn = a.F_x[f];
-    u_dn = uu[f];
+  if (i0 < i1) {
+    if (kV && flux_ok) {
+      const size_t f = fidx(nx, i0 - 1, j);
+      F_dn = a.F_x[f];
+      u_dn = uu[f];
+    }
+    load(i0);
   }
-  load(i0);
+  __syncthreads();
+  if (i0 >= i1) return;
   for (int ii = i0; ii < i1; ++ii) {
     const int k = ii - i0;
     const R Fa = Fa_n, Fb = Fb_n, u0 = u0_n;
