@@ -135,6 +135,24 @@ int st_shock_heating(int nx, int ny, Mesh* mesh, double dt_h, double* e,
   return check_launch("shock_heating_and_work");
 }
 
+// A page-locked pair of doubles per host thread for the values the host
+// waits on (dt, the totals): a copy into it is one DMA, where a copy into
+// pageable memory is staged through a driver buffer.  Kept for the life of
+// the thread; NULL if page-locked memory cannot be had (the caller then
+// copies into its own memory).
+double* pinned_pair() {
+  thread_local double* buf = nullptr;
+  thread_local bool tried = false;
+  if (!tried) {
+    tried = true;
+    if (cudaMallocHost(&buf, 2 * sizeof(double)) != cudaSuccess) {
+      buf = nullptr;
+      cudaGetLastError();
+    }
+  }
+  return buf;
+}
+
 int st_set_timestep(int nx, int ny, const double* Qxx, const double* Qyy,
                     const double* rho, const double* e, Mesh* mesh,
                     double* reduce_array, int first_step, const double* celldx,
@@ -145,8 +163,10 @@ int st_set_timestep(int nx, int ny, const double* Qxx, const double* Qyy,
   MeshView m{mesh->edgedx, mesh->edgedy, celldx, celldy};
   launch_min_timestep(s, nx, ny, mesh->pad, mesh->max_dt, mesh->dt_h,
                       first_step, Qxx, Qyy, rho, e, m, reduce_array);
-  double pair[2];
-  cudaMemcpyAsync(pair, reduce_array + kRaDt, sizeof(pair),
+  double local[2];
+  double* pair = pinned_pair();
+  if (!pair) pair = local;
+  cudaMemcpyAsync(pair, reduce_array + kRaDt, 2 * sizeof(double),
                   cudaMemcpyDeviceToHost, s);
   const cudaError_t err = cudaStreamSynchronize(s);
   if (err != cudaSuccess) {
@@ -274,8 +294,10 @@ int st_conservation(int nx, int ny, int pad, const double* rho, const double* e,
   launch_conservation(s, nx, ny, pad, rho, e, reduce_array);
   FLOW_TRY(check_launch("conservation"));
   if (!sync) return GB300_OK;
-  double tot[2];
-  cudaMemcpyAsync(tot, reduce_array + kRaMass, sizeof(tot),
+  double local[2];
+  double* tot = pinned_pair();
+  if (!tot) tot = local;
+  cudaMemcpyAsync(tot, reduce_array + kRaMass, 2 * sizeof(double),
                   cudaMemcpyDeviceToHost, s);
   const cudaError_t err = cudaStreamSynchronize(s);
   if (err != cudaSuccess) {

@@ -10,6 +10,8 @@
 // results bit for bit.  The fused, faster timestep lives in fused.cu.
 //
 // Every kernel is a 2-D launch: x over columns (coalesced), y over rows.
+#include <atomic>
+
 #include "common.cuh"
 #include "stages.h"
 
@@ -198,37 +200,130 @@ __global__ void __launch_bounds__(kRedThreads)
   }
 }
 
-// Each block sums whole interior rows (threads stride along the row), so the
-// traversal needs no division of a flat index.  Four columns per iteration
-// into two pairs of sums (independent loads and FP64 chains in flight), and
-// rho*e contracted into one FMA: two FP64 instructions per cell, the FP64
-// pipe's share of this reduction on GB300.
+// Partial sums of one thread: two (mass, energy) pairs.
+struct ConsSums {
+  double m0, e0, m1, e1;
+};
+
+// The FP64 work of the conservation sums sits in calls, so that a warp that
+// skips it skips its instructions (a predicated FP64 instruction still takes
+// its issue slots on the FP64 pipe).  plain: bit q set where group q is summed.
+__device__ __noinline__ ConsSums cons_add_groups(ConsSums s, unsigned plain, double d0,
+                                                 double d1, double d2, double d3, double f0,
+                                                 double f1, double f2, double f3) {
+  if (plain & 1u) {
+    s.m0 += d0;
+    s.e0 = fma(d0, f0, s.e0);
+  }
+  if (plain & 2u) {
+    s.m1 += d1;
+    s.e1 = fma(d1, f1, s.e1);
+  }
+  if (plain & 4u) {
+    s.m0 += d2;
+    s.e0 = fma(d2, f2, s.e0);
+  }
+  if (plain & 8u) {
+    s.m1 += d3;
+    s.e1 = fma(d3, f3, s.e1);
+  }
+  return s;
+}
+// A run of n groups of 32 cells holding one (rho, e) pair: n*rho and
+// n*(rho*e) per lane.
+__device__ __noinline__ ConsSums cons_add_run(ConsSums s, int n, unsigned long long r_bits,
+                                              unsigned long long e_bits) {
+  const double dn = (double)n, r = __longlong_as_double(r_bits);
+  s.m1 += dn * r;
+  s.e1 += dn * (r * __longlong_as_double(e_bits));
+  return s;
+}
+
+// The interior is cut into chunks of 4 x 256 columns of one row (each warp
+// 4 groups of 32 consecutive cells) and the chunks are dealt to the blocks in
+// turn: a block loads its next chunk before it sums the current one (16 loads
+// of independent columns in flight per thread), into two pairs of sums, rho*e
+// contracted into one FMA -- two FP64 instructions per cell, the FP64 pipe's
+// share of this reduction on GB300.  The grid is one wave of resident blocks.
+// Columns past the last whole chunk of a row (rows whose interior is not a
+// multiple of 1024 wide) are summed after the chunks, by 256-column groups
+// and a ragged end.  A group whose 32 cells hold one (rho, e) pair (bit for
+// bit; the fluid at rest around a blast) is counted instead: the warp keeps
+// the pair of its current run of such groups and their number, and adds
+// n*rho and n*(rho*e) per lane when the run ends -- integer work in place of
+// 64 FP64 instructions per group, and the same sum to rounding.
+constexpr int kConsChunk = 4 * kRedThreads;
+
 __global__ void __launch_bounds__(kRedThreads)
     k_conservation(int nx, int ny, int pad, const double* __restrict__ rho,
                    const double* __restrict__ e, double* ra) {
-  double ms0 = 0.0, es0 = 0.0, ms1 = 0.0, es1 = 0.0;
-  for (int ii = pad + blockIdx.x; ii < ny - pad; ii += gridDim.x) {
-    const double* rr = rho + (size_t)ii * nx;
-    const double* er = e + (size_t)ii * nx;
-    int jj = pad + threadIdx.x;
-    for (; jj + 3 * kRedThreads < nx - pad; jj += 4 * kRedThreads) {
-      double d[4], f[4];
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        d[q] = rr[jj + q * kRedThreads];
-        f[q] = er[jj + q * kRedThreads];
-      }
-      ms0 += d[0] + d[1];
-      ms1 += d[2] + d[3];
-      es0 = fma(d[1], f[1], fma(d[0], f[0], es0));
-      es1 = fma(d[3], f[3], fma(d[2], f[2], es1));
+  ConsSums acc{0.0, 0.0, 0.0, 0.0};
+  unsigned long long run_r = 0ull, run_e = 0ull;  // warp-uniform
+  int run_n = 0;
+  // Group q of 32 cells of a warp: counted into the run (returns 0), or to be
+  // summed (returns bit q).
+  auto group = [&](double d, double f, int q) -> unsigned {
+    const unsigned long long db = __double_as_longlong(d), fb = __double_as_longlong(f);
+    const unsigned long long d0 = __shfl_sync(0xffffffffu, db, 0);
+    const unsigned long long f0 = __shfl_sync(0xffffffffu, fb, 0);
+    if (!__all_sync(0xffffffffu, db == d0 && fb == f0)) return 1u << q;
+    if (d0 != run_r || f0 != run_e) {
+      if (run_n > 0) acc = cons_add_run(acc, run_n, run_r, run_e);
+      run_r = d0;
+      run_e = f0;
+      run_n = 0;
     }
-    for (; jj < nx - pad; jj += kRedThreads) {
-      ms0 += rr[jj];
-      es0 = fma(rr[jj], er[jj], es0);
+    ++run_n;
+    return 0u;
+  };
+  const int w = nx - 2 * pad, rows = ny - 2 * pad;
+  const int t = threadIdx.x;
+  const int per_row = w / kConsChunk;
+  const long long chunks = (long long)rows * per_row;
+  double d[4], f[4];
+  auto load = [&](long long c, double* dd, double* ff) {
+    const int r = (int)(c / per_row);
+    const size_t base = (size_t)(pad + r) * nx + pad + (size_t)(c - (long long)r * per_row) * kConsChunk + t;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      dd[q] = rho[base + q * kRedThreads];
+      ff[q] = e[base + q * kRedThreads];
+    }
+  };
+  long long c = blockIdx.x;
+  if (c < chunks) load(c, d, f);
+  while (c < chunks) {
+    const long long cn = c + gridDim.x;
+    double dn[4], fn[4];
+    if (cn < chunks) load(cn, dn, fn);
+    unsigned plain = 0u;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) plain |= group(d[q], f[q], q);
+    if (plain) acc = cons_add_groups(acc, plain, d[0], d[1], d[2], d[3], f[0], f[1], f[2], f[3]);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      d[q] = dn[q];
+      f[q] = fn[q];
+    }
+    c = cn;
+  }
+  if (per_row * kConsChunk < w) {
+    for (int r = blockIdx.x; r < rows; r += gridDim.x) {
+      const double* rr = rho + (size_t)(pad + r) * nx + pad;
+      const double* er = e + (size_t)(pad + r) * nx + pad;
+      int j0 = per_row * kConsChunk;
+      for (; j0 + kRedThreads <= w; j0 += kRedThreads) {
+        const double dd = rr[j0 + t], ff = er[j0 + t];
+        if (group(dd, ff, 0)) acc = cons_add_groups(acc, 1u, dd, 0.0, 0.0, 0.0, ff, 0.0, 0.0, 0.0);
+      }
+      if (j0 + t < w) {
+        acc.m0 += rr[j0 + t];
+        acc.e0 = fma(rr[j0 + t], er[j0 + t], acc.e0);
+      }
     }
   }
-  double ms = ms0 + ms1, es = es0 + es1;
+  if (run_n > 0) acc = cons_add_run(acc, run_n, run_r, run_e);
+  double ms = acc.m0 + acc.m1, es = acc.e0 + acc.e1;
   __shared__ double s_m[kRedThreads / 32], s_e[kRedThreads / 32];
   __shared__ bool s_last;
   ms = warp_sum(ms);
@@ -573,6 +668,33 @@ int reduce_blocks(int nx, int ny, int pad, int partials_per_block) {
   return (int)b;
 }
 
+// One wave of resident conservation blocks on the current device (the SM
+// count and the kernel's occupancy, looked up once per device), no more than
+// the chunks and rows to deal out nor the partial slots of reduce_array.
+int conservation_blocks(int nx, int ny, int pad) {
+  constexpr int kMaxDevices = 64;
+  static std::atomic<int> wave[kMaxDevices];
+  int dev = 0;
+  cudaGetDevice(&dev);
+  int b = (dev >= 0 && dev < kMaxDevices) ? wave[dev].load(std::memory_order_relaxed) : 0;
+  if (b == 0) {
+    int sms = 0, per_sm = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_conservation, kRedThreads, 0);
+    b = sms * per_sm > 0 ? sms * per_sm : kMaxReduceBlocks;
+    if (dev >= 0 && dev < kMaxDevices) wave[dev].store(b, std::memory_order_relaxed);
+  }
+  const int w = nx - 2 * pad, rows = ny - 2 * pad;
+  long long work = (long long)rows * (w / kConsChunk);  // whole chunks
+  if (work < rows) work = rows;  // rows of ragged ends
+  const long long cap = ((long long)nx * ny - kRaPartial) / 2;
+  long long g = b;
+  if (g > work) g = work;
+  if (g > cap) g = cap;
+  if (g < 1) g = 1;
+  return (int)g;
+}
+
 void launch_min_timestep(cudaStream_t s, int nx, int ny, int pad, double max_dt,
                          double dt_h, int first_step, const double* Qxx,
                          const double* Qyy, const double* rho, const double* e,
@@ -587,7 +709,7 @@ void launch_conservation(cudaStream_t s, int nx, int ny, int pad,
                          const double* rho, const double* e,
                          double* reduce_array) {
   cudaMemsetAsync(reduce_array + kRaTicket, 0, sizeof(double), s);
-  k_conservation<<<reduce_blocks(nx, ny, pad, 2), kRedThreads, 0, s>>>(
+  k_conservation<<<conservation_blocks(nx, ny, pad), kRedThreads, 0, s>>>(
       nx, ny, pad, rho, e, reduce_array);
 }
 

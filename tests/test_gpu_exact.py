@@ -184,6 +184,24 @@ def test_conservation_totals(fg):
     np.testing.assert_allclose(got, want, rtol=1e-13)
 
 
+@pytest.mark.parametrize("width", [1024 + 256 + 7, 2048, 300])
+def test_conservation_totals_runs_of_equal_cells(fg, width):
+    """Rows wide enough for the full 1024-column chunks, the single 256-column
+    groups and the ragged tail, with runs of equal (rho, e) groups broken by
+    a blast, a changed background and a lone perturbed cell."""
+    rng = np.random.default_rng(4)
+    ny = 37
+    r, e = np.ones((ny, width)), np.full((ny, width), 1e-5)
+    r[10:14, 40:300] = rng.uniform(0.5, 2.0, (4, 260))
+    e[10:14, 40:300] = rng.uniform(1.0, 9.0, (4, 260))
+    r[20:, :] = 1.25  # a second run of equal groups
+    e[25, width // 2] = 3.0  # one cell breaks its group
+    sim, hm, st = make_pair(fg, r, e, 1e-3)
+    got = sim.conservation()
+    want = O.conservation(hm, st)
+    np.testing.assert_allclose(got, want, rtol=1e-13)
+
+
 def test_boundary_fill_bit_exact(fg):
     rng = np.random.default_rng(11)
     sim, hm, st = make_pair(fg, np.ones((9, 14)), np.ones((9, 14)), 1e-3)
