@@ -602,7 +602,7 @@ def run_gpu(args):
         "forms": forms,
         "cpu_baseline": cpu,
         "clocks": clk.summary(),
-        "gpu_launches": 11 * args.steps,  # 10 timestep kernels + the conservation totals
+        "gpu_launches": 12 * args.steps,  # mesh test + 10 timestep kernels + the conservation totals
         "mass": mass, "energy": energy,
     }
     print(json.dumps(line), flush=True)

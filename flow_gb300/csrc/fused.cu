@@ -39,12 +39,16 @@ __global__ void __launch_bounds__(kPow2Threads)
                 const double* celldy, const double* edgedy, unsigned long long* flag) {
   pdl_wait();
   pdl_trigger();
+  // Every test is made (no short circuit), so that a thread's loads are
+  // independent and in flight together.
   bool ok = true;
+#pragma unroll 4
   for (int j = threadIdx.x; j <= nx; j += kPow2Threads) {
-    ok = ok && d_is_pow2(celldx[j]) && d_is_pow2(edgedx[j]);
+    ok &= d_is_pow2(celldx[j]) & d_is_pow2(edgedx[j]);
   }
+#pragma unroll 4
   for (int i = threadIdx.x; i <= ny; i += kPow2Threads) {
-    ok = ok && d_is_pow2(celldy[i]) && d_is_pow2(edgedy[i]);
+    ok &= d_is_pow2(celldy[i]) & d_is_pow2(edgedy[i]);
   }
   ok = __syncthreads_and(ok) != 0;
   if (threadIdx.x == 0) *flag = ok ? 1ull : 0ull;

@@ -127,6 +127,15 @@ __device__ __forceinline__ bool d_is_pow2(double x) {
   const unsigned ex = (unsigned)(b >> 52);  // sign bit lands above the field
   return (b & 0x000fffffffffffffLL) == 0 && ex - 1u < 0x7feu;
 }
+// r * e is exact and r * e / r gives e back: r a positive normal power of
+// two, e a zero or a normal number whose product with r is normal (tests on
+// the bit patterns, no FP64 instruction).
+__device__ __forceinline__ bool d_pow2_product_exact(double r, double e) {
+  const long long eb = dbits(e);
+  const int ee = (int)((eb >> 52) & 0x7ff);
+  const int ex = ee + (int)((dbits(r) >> 52) & 0x7ff) - 1023;
+  return d_is_pow2(r) & (((eb << 1) == 0) | ((ee != 0) & (ee != 0x7ff) & (ex >= 1) & (ex <= 2046)));
+}
 
 // Quotients of powers of two, for the spacing factors of power-of-two
 // meshes: 1/y, x/(2y) and 1/(y*y) with x, y positive normal powers of two.

@@ -864,6 +864,12 @@ struct ColWindow {
     d1 = d2; d2 = d3; d3 = d3n;
     D1 = D2; D2 = D2n;
   }
+  // After a push: the differences shift's would have given, from those of
+  // the window one row before (same operands, same values).
+  __device__ __forceinline__ void advance() {
+    d1 = d2; d2 = d3; d3 = p1 - p0;
+    D1 = D2; D2 = p1 - m1;
+  }
   // mc_face of the window's face (between m1 and p0).
   template <bool kP2>
   __device__ __forceinline__ R face(bool pos, R inv_h, R h, R wdt) const {
@@ -962,23 +968,35 @@ __device__ __forceinline__ void mass_energy_flux(R vm, R v0, R vp, R rm2,
       inv_h, icd, area, dt, dt_h, F_out, eF_out);
 }
 
+// The energy of a cell that takes no flux: the reference's rho_old*e/den
+// round trip, which gives e itself when the product rho_old*e is exact and
+// den is rho_old.  Called (a real branch) by warps whose round trip is not
+// settled by tests on the bit patterns: a short FP64 sequence under a branch
+// is turned into predicated code that still occupies the FP64 pipe.
+template <typename R>
+static __device__ __noinline__ double still_energy(double r_old, double e_in, double den) {
+  const double rho_e = __dmul_rn(r_old, e_in);
+  if (warp_all(d_is_zero(fma(r_old, e_in, -rho_e)) && dbits(den) == dbits(r_old) &&
+               !d_is_zero(den))) {
+    return e_in;
+  }
+  if (d_is_zero(den)) return 0.0;
+  if constexpr (Prec<R>::kMixed) {
+    const double r0 = Prec<R>::to_d(Prec<R>::rcp(Prec<R>::from_d(den)));
+    const double q = rho_e * r0;
+    return fma(r0, fma(-den, q, rho_e), q);
+  } else {
+    return d_div(rho_e, den);
+  }
+}
+
 // Conservative FP64 update of one cell from its two face fluxes (given in
 // bulk precision, converted exactly): vol = celldx*celldy and ivol its
 // reciprocal (in the mixed form ivol is dt_h/vol: the sweeps fold dt_h into
-// their row factors), a0/a1 the face lengths.  den is rho_old in the first sweep of a step and the new
-// density in the second (omp3/flow.c:416-432).  The FP64 form keeps the
-// reference's evaluation order; the mixed form contracts into FMAs.
-// The quotient rho_e / den of an update as a called function, for warps
-// whose cells take no flux but whose energies do not come back exactly: a
-// short FP64 sequence under a branch is turned into predicated code that
-// still occupies the FP64 pipe, while a call is a real branch.
-static __device__ __noinline__ double still_quotient(double n, double d) { return d_div(n, d); }
-template <typename R>
-static __device__ __noinline__ double still_quotient_mixed(double n, double d) {
-  const double r0 = Prec<R>::to_d(Prec<R>::rcp(Prec<R>::from_d(d)));
-  const double q = n * r0;
-  return fma(r0, fma(-d, q, n), q);
-}
+// their row factors), a0/a1 the face lengths.  den is rho_old in the first
+// sweep of a step and the new density in the second (omp3/flow.c:416-432).
+// The FP64 form keeps the reference's evaluation order; the mixed form
+// contracts into FMAs.
 
 // The fluxes arrive widened to FP64 (f0, f1 mass, ef0, ef1 energy; exact
 // for the mixed form's FP32 fluxes), each face's once.
@@ -994,20 +1012,17 @@ __device__ __forceinline__ void mass_energy_update(double r_in, double e_in,
   // updates subtract zeros, the density stays and the energy takes the
   // reference's rho_old*e/den round trip -- which gives e itself when the
   // product rho_old*e is exact and den is rho_old, as in the still background
-  // of a blast.  The FP64 form takes the per-lane skip below otherwise.
+  // of a blast (a power-of-two density: settled without FP64 instructions).
+  // The FP64 form takes the per-lane skip below otherwise.
   const bool none = warp_all(d_is_zero(f0) && d_is_zero(f1) &&
                              (Pr::kMixed || (d_is_zero(ef0) && d_is_zero(ef1))));
   if (none) {
-    const double rho_e = __dmul_rn(r_old, e_in);
     const double den = kFirst ? r_old : r_in;
     *r_out = r_in;
-    if (warp_all(d_is_zero(fma(r_old, e_in, -rho_e)) && dbits(den) == dbits(r_old) &&
-                 !d_is_zero(den))) {
+    if (warp_all(dbits(den) == dbits(r_old) && d_pow2_product_exact(r_old, e_in))) {
       *e_out = e_in;
-    } else if (d_is_zero(den)) {
-      *e_out = 0.0;
     } else {
-      *e_out = Pr::kMixed ? still_quotient_mixed<R>(rho_e, den) : still_quotient(rho_e, den);
+      *e_out = still_energy<R>(r_old, e_in, den);
     }
     return;
   }
@@ -1369,6 +1384,24 @@ __device__ __forceinline__ R momentum_upwind(R wind, R m2, R m1, R p0, R p1,
 // A flux the reference reads from a ghost point is the mirror source's
 // (the reflective fill of the flux arrays, no sign change).
 
+// FP64 form: a face's momentum minus dt_h * (fa - fb) / (hx * h) where the
+// fluxes differ, stored; the momentum is read here unless kVel gave it.  A
+// call, so that the warps which skip it skip its FP64 instructions (if
+// converted to predicated code they would still take their FP64 issue
+// slots).
+template <bool kVel, bool kP2>
+static __device__ __noinline__ double momentum_change(double* mom, double m, double fa, double fb,
+                                                      double dt_h, double hx, double h,
+                                                      double inv_h, double ihx) {
+  using Pr = Prec<double>;
+  const double diff = fa - fb;
+  if (Pr::zero_skip_mem(diff)) return m;
+  if (!kVel) m = *mom;
+  m = Pr::template dsub<kP2>(m, dt_h * diff, hx * h, Pr::template mulp<kP2>(inv_h, ihx));
+  *mom = m;
+  return m;
+}
+
 // The momentum update of one face from its flux difference fa - fb, the
 // velocity recomputed from the post-advection density when kVel (written to
 // vout with its ghost images).  kU: an x-face (rho_u, u) else a y-face.
@@ -1391,11 +1424,15 @@ __device__ __forceinline__ void momentum_face_update(const StepArgs<R>& a, bool 
   // momentum is read only where it is needed.
   R m = kVel ? m_in : R(0);
   if (!warp_same(fa, fb)) {
-    const R diff = fa - fb;
-    if (!Pr::zero_skip_mem(diff)) {
-      if (!kVel) m = *mom;
-      m = Pr::template dsub<kP2>(m, dt_h * diff, hx * h, Pr::template mulp<kP2>(inv_h, ihx));
-      *mom = m;
+    if constexpr (Pr::kMixed) {
+      const R diff = fa - fb;
+      if (!Pr::zero_skip_mem(diff)) {
+        if (!kVel) m = *mom;
+        m = Pr::template dsub<kP2>(m, dt_h * diff, hx * h, Pr::template mulp<kP2>(inv_h, ihx));
+        *mom = m;
+      }
+    } else {
+      m = momentum_change<kVel, kP2>(mom, m, fa, fb, dt_h, hx, h, inv_h, ihx);
     }
   }
   if (kVel) {
@@ -1636,7 +1673,13 @@ __device__ __forceinline__ void tile_mom_y_impl(const StepArgs<R>& a, int bx, in
       fresh = false;  // the window shifts its values alone until mass moves
       return sum_zeros(Fa, Fb);
     }
-    if (!fresh) win.refresh();
+    // The window moves by values alone (a push per row); its differences are
+    // formed here, on the moving path only: shifted from the row before when
+    // that row moved, else all of them.  (A shift per row under a branch
+    // would be predicated code, its FP64 subtractions taking FP64 issue
+    // slots in every warp at rest.)
+    if (fresh) win.advance();
+    else win.refresh();
     fresh = true;
     const R mass = Pr::template mulp<kP2>(Fa + Fb, hcol);
     if (Pr::zero_skip_coarse(mass)) return mass;
@@ -1691,8 +1734,7 @@ __device__ __forceinline__ void tile_mom_y_impl(const StepArgs<R>& a, int bx, in
       const R Fa = Fa_n, Fb = Fb_n, wv = wv_n;
       const int cn = ci + 1;
       if (ii + 1 < i1 && src_row(cn) == cn) load(cn);
-      if (fresh) win.shift(wv);
-      else win.push(wv);
+      win.push(wv);
       ++wrow;
       cur = flux_at(cs, cs - fr0, Fa, Fb);
     }
