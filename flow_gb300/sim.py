@@ -60,6 +60,9 @@ class DeviceSim:
         for k, t in self.mesh_arrays.items():
             setattr(m, k, dptr(t))
         self.mesh = m
+        self._mesh_ref = ctypes.byref(m)
+        self._solve = lib().gb300_solve_hydro_2d
+        self._args = None
         self.tt = 0
         if prob.box_list is not None:
             self.fill_boxes(prob.box_list)
@@ -115,11 +118,16 @@ class DeviceSim:
         check()
 
     def args(self):
-        return [dptr(self.a[f]) for f in SOLVE_ORDER]
+        # The arrays are allocated once, in __init__, and written in place
+        # afterwards, so their pointers are formed once: a ctypes cast per
+        # array per step would keep the GPU waiting on the host after every
+        # step whose totals are read back.
+        if self._args is None:
+            self._args = tuple(dptr(self.a[f]) for f in SOLVE_ORDER)
+        return self._args
 
     def step(self) -> None:
-        L = lib()
-        st = L.gb300_solve_hydro_2d(ctypes.byref(self.mesh), self.tt, *self.args())
+        st = self._solve(self._mesh_ref, self.tt, *self.args())
         if st != GB300_OK:
             check()
         self.tt += 1
