@@ -126,6 +126,28 @@ __device__ __forceinline__ void store_cell(bool edge, double* a64, R* ar, int nx
   }
 }
 
+// Asynchronous copy of one 4- or 8-byte element from global to shared memory
+// (cp.async, through L1); with pred false nothing is read and the element is
+// zero-filled.  A thread that reads back only the elements it copied itself
+// needs no barrier: cp.async.wait_group makes its own copies visible to it.
+template <typename T>
+__device__ __forceinline__ void cp_async_elem(T* smem, const T* gmem, bool pred) {
+  static_assert(sizeof(T) == 4 || sizeof(T) == 8, "4- or 8-byte elements");
+  const unsigned dst = (unsigned)__cvta_generic_to_shared(smem);
+  const int src_bytes = pred ? (int)sizeof(T) : 0;
+  asm volatile("cp.async.ca.shared.global [%0], [%1], %2, %3;\n" ::"r"(dst), "l"(gmem),
+               "n"((int)sizeof(T)), "r"(src_bytes)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+// Waits until at most n of this thread's newest copy groups are in flight.
+template <int n>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(n) : "memory");
+}
+
 // pred holds in every active lane of the warp (a warp-uniform branch
 // condition).
 __device__ __forceinline__ bool warp_all(bool pred) {
@@ -546,8 +568,9 @@ __device__ __forceinline__ void tile_lag_viscous_accel_impl(const StepArgs<R>& a
   }
   const bool col_ok = jj < nx + 1 - pad;
   const int i1 = min(i0 + a.rows, ny + 1 - pad);
-  // The stresses of row ii+1 are loaded before row ii is processed (the
-  // first row's before the barrier that publishes the row tables, kEarly).
+  // kEarly (the fused kernel): the stresses stream through a shared-memory
+  // ring, below.  Otherwise (the batched kernel) row ii+1's are loaded into
+  // registers before row ii is processed.
   R q1_n = R(0), q0_n = R(0), qy_n = R(0), qy_dn = R(0);
   auto load = [&](int ii) {
     const size_t c = cidx(nx, ii, jj);
@@ -559,7 +582,7 @@ __device__ __forceinline__ void tile_lag_viscous_accel_impl(const StepArgs<R>& a
   };
   auto prime = [&]() {
     if (jj < nx - pad) qy_dn = a.Qyy[cidx(nx, i0 - 1, jj)];
-    if (i0 < i1) load(i0);
+    if (!kEarly && i0 < i1) load(i0);
   };
   if (kEarly && col_ok) prime();
   __syncthreads();
@@ -574,10 +597,8 @@ __device__ __forceinline__ void tile_lag_viscous_accel_impl(const StepArgs<R>& a
   const R wx1 = geo_half_ratio<R, kP2>(a.celldx[jj - 1], a.edgedx[jj]);
   const R dt = Pr::from_d(a.dt);
   if (!kEarly) prime();
-  for (int ii = i0; ii < i1; ++ii) {
+  auto row = [&](int ii, R q1, R q0, R qy) {
     const int k = ii - i0;
-    const R q1 = q1_n, q0 = q0_n, qy = qy_n;
-    if (ii + 1 < i1) load(ii + 1);
     if (ii < ny - pad) {
       const size_t f = fidx(nx, ii, jj);
       // No stress gradient: the momentum and the velocity from the pressure
@@ -609,6 +630,44 @@ __device__ __forceinline__ void tile_lag_viscous_accel_impl(const StepArgs<R>& a
         }
       }
       qy_dn = qy;
+    }
+  };
+  if constexpr (kEarly) {
+    // The stresses of rows ii+1 .. ii+kAhead are in flight while row ii is
+    // processed: each thread copies its own column's values into a ring of
+    // shared-memory slots (no registers held for them, no barrier), one copy
+    // group per row.  kAhead + 1 slots: a row's slot is refilled one row
+    // after it was read.
+    constexpr int kAhead = 2, kSlots = kAhead + 1;
+    __shared__ R s_q[kSlots][3][kCols];
+    const int t = threadIdx.x;
+    auto issue = [&](int ii) {
+      const int sl = (ii - i0) % kSlots;
+      const size_t c = cidx(nx, ii, jj);
+      const bool xq = ii < ny - pad, yq = jj < nx - pad;
+      cp_async_elem(&s_q[sl][0][t], xq ? a.Qxx + c : a.Qxx, xq);
+      cp_async_elem(&s_q[sl][1][t], xq ? a.Qxx + c - 1 : a.Qxx, xq);
+      cp_async_elem(&s_q[sl][2][t], yq ? a.Qyy + c : a.Qyy, yq);
+    };
+#pragma unroll
+    for (int d = 0; d < kAhead; ++d) {
+      if (i0 + d < i1) issue(i0 + d);
+      cp_async_commit();
+    }
+    for (int ii = i0; ii < i1; ++ii) {
+      cp_async_wait<kAhead - 1>();  // row ii's group has landed
+      const int sl = (ii - i0) % kSlots;
+      const R q1 = s_q[sl][0][t], q0 = s_q[sl][1][t], qy = s_q[sl][2][t];
+      if (ii + kAhead < i1) issue(ii + kAhead);
+      cp_async_commit();
+      row(ii, q1, q0, qy);
+    }
+    cp_async_wait<0>();
+  } else {
+    for (int ii = i0; ii < i1; ++ii) {
+      const R q1 = q1_n, q0 = q0_n, qy = qy_n;
+      if (ii + 1 < i1) load(ii + 1);
+      row(ii, q1, q0, qy);
     }
   }
 }
