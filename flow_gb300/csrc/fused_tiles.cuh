@@ -1522,12 +1522,19 @@ __device__ __forceinline__ void momentum_face_update(const StepArgs<R>& a, bool 
 //   kV = true (rho_v): thread t holds the vF_x of corner c0 + t (c0 = pad +
 //     127 bx) and, for t < 127, updates y-face c0 + t from corners c0 + t and
 //     c0 + t + 1.
-template <typename R, bool kV, bool kVel, bool kP2>
+template <typename R, bool kV, bool kVel, bool kP2, bool kRing>
 __device__ __forceinline__ void tile_mom_x_impl(const StepArgs<R>& a, int bx, int by) {
   using Pr = Prec<R>;
   __shared__ R s_half[kMaxRows], s_h[kMaxRows], s_row[kMaxRows];
   __shared__ R s_wy0[kMaxRows], s_wy1[kMaxRows];
   __shared__ R sF[kCols];
+  // kVel and kRing (the fused kernels): the update inputs of a face (its
+  // momentum and the densities either side) stream through a per-thread
+  // ring of asynchronous copies, two rows ahead (no registers held for them,
+  // no barrier: each thread reads back only what it copied).
+  constexpr bool kUpdRing = kVel && kRing;
+  constexpr int kAhead = 2, kSlots = kAhead + 1;
+  __shared__ R s_upd[kUpdRing ? kSlots : 1][3][kUpdRing ? kCols : 1];
   const int nx = a.nx, ny = a.ny, pad = a.pad;
   const int t = threadIdx.x;
   const int c0 = (kV ? pad : pad - 1) + bx * (kCols - 1);
@@ -1593,8 +1600,27 @@ __device__ __forceinline__ void tile_mom_x_impl(const StepArgs<R>& a, int bx, in
     }
     load(i0);
   }
+  auto issue_upd = [&](int ii) {
+    const int sl = (ii - i0) % kSlots;
+    const size_t c = cidx(nx, ii, j);
+    const R* mp = kV ? a.rho_v + c : a.rho_u + fidx(nx, ii, j);
+    const R* rbp = kV ? a.rho_r + c - nx : a.rho_r + c - 1;
+    cp_async_elem(&s_upd[sl][0][t], upd ? mp : a.rho_r, upd);
+    cp_async_elem(&s_upd[sl][1][t], upd ? a.rho_r + c : a.rho_r, upd);
+    cp_async_elem(&s_upd[sl][2][t], upd ? rbp : a.rho_r, upd);
+  };
+  if constexpr (kUpdRing) {
+#pragma unroll
+    for (int d = 0; d < kAhead; ++d) {
+      if (i0 + d < i1) issue_upd(i0 + d);
+      cp_async_commit();
+    }
+  }
   __syncthreads();
-  if (i0 >= i1) return;
+  if (i0 >= i1) {
+    if constexpr (kUpdRing) cp_async_wait<0>();
+    return;
+  }
   for (int ii = i0; ii < i1; ++ii) {
     const int k = ii - i0;
     const R Fa = Fa_n, Fb = Fb_n, u0 = u0_n;
@@ -1638,7 +1664,15 @@ __device__ __forceinline__ void tile_mom_x_impl(const StepArgs<R>& a, int bx, in
       const R fb = kV ? sF[t] : sF[t - 1];
       const size_t c = cidx(nx, ii, j);
       R m = R(0), ra = R(0), rb = R(0);
-      if (kVel) {
+      if constexpr (kUpdRing) {
+        cp_async_wait<kAhead - 1>();  // row ii's group has landed
+        const int sl = k % kSlots;
+        m = s_upd[sl][0][t];
+        ra = s_upd[sl][1][t];
+        rb = s_upd[sl][2][t];
+        if (ii + kAhead < i1) issue_upd(ii + kAhead);
+        cp_async_commit();
+      } else if (kVel) {
         m = kV ? a.rho_v[c] : a.rho_u[fidx(nx, ii, j)];
         ra = a.rho_r[c];
         rb = kV ? a.rho_r[c - nx] : a.rho_r[c - 1];
@@ -1649,6 +1683,7 @@ __device__ __forceinline__ void tile_mom_x_impl(const StepArgs<R>& a, int bx, in
     }
     __syncthreads();
   }
+  if constexpr (kUpdRing) cp_async_wait<0>();
 }
 
 // y pairs: each thread marches down its column, carrying the flux of the
@@ -1806,11 +1841,11 @@ __device__ __forceinline__ void tile_mom_y_impl(const StepArgs<R>& a, int bx, in
   }
 }
 
-template <typename R, bool kV, bool kVel>
+template <typename R, bool kV, bool kVel, bool kRing = true>
 __device__ __forceinline__ void tile_mom_x(const StepArgs<R>& a, int bx, int by) {
   FLOW_POW2_DISPATCH(R, a, (kV ? a.pad : a.pad - 1) + bx * (kCols - 1), a.pad + by * a.rows,
-                     (tile_mom_x_impl<R, kV, kVel, true>(a, bx, by)),
-                     (tile_mom_x_impl<R, kV, kVel, false>(a, bx, by)));
+                     (tile_mom_x_impl<R, kV, kVel, true, kRing>(a, bx, by)),
+                     (tile_mom_x_impl<R, kV, kVel, false, kRing>(a, bx, by)));
 }
 template <typename R, bool kV, bool kVel>
 __device__ __forceinline__ void tile_mom_y(const StepArgs<R>& a, int bx, int by) {
