@@ -100,12 +100,12 @@ __device__ __noinline__ void tile_call(const Instance<R>& __restrict__ I, int tx
   switch (kPh) {
     case kPhMomUxV: tile_mom_x<R, false, true, false>(I.a, tx, ty); break;
     case kPhMomUx: tile_mom_x<R, false, false, false>(I.a, tx, ty); break;
-    case kPhMomUyV: tile_mom_y<R, false, true>(I.a, tx, ty); break;
-    case kPhMomUy: tile_mom_y<R, false, false>(I.a, tx, ty); break;
+    case kPhMomUyV: tile_mom_y<R, false, true, false>(I.a, tx, ty); break;
+    case kPhMomUy: tile_mom_y<R, false, false, false>(I.a, tx, ty); break;
     case kPhMomVxV: tile_mom_x<R, true, true, false>(I.a, tx, ty); break;
     case kPhMomVx: tile_mom_x<R, true, false, false>(I.a, tx, ty); break;
-    case kPhMomVyV: tile_mom_y<R, true, true>(I.a, tx, ty); break;
-    default: tile_mom_y<R, true, false>(I.a, tx, ty); break;
+    case kPhMomVyV: tile_mom_y<R, true, true, false>(I.a, tx, ty); break;
+    default: tile_mom_y<R, true, false, false>(I.a, tx, ty); break;
   }
 }
 

@@ -1695,9 +1695,15 @@ __device__ __forceinline__ void tile_mom_x_impl(const StepArgs<R>& a, int bx, in
 //     updates y-faces i0 .. i1-1 from cells ii-1, ii.
 // The windows form their differences only where mass moves in the warp
 // (FP64 form), as the y mass sweep does.
-template <typename R, bool kV, bool kVel, bool kP2>
+template <typename R, bool kV, bool kVel, bool kP2, bool kRing>
 __device__ __forceinline__ void tile_mom_y_impl(const StepArgs<R>& a, int bx, int by) {
   using Pr = Prec<R>;
+  // kVel and kRing (the fused kernels): the update inputs of a face stream
+  // through a per-thread ring of asynchronous copies, two rows ahead (as in
+  // the x pairs).
+  constexpr bool kUpdRing = kVel && kRing;
+  constexpr int kAhead = 2, kSlots = kAhead + 1;
+  __shared__ R s_upd[kUpdRing ? kSlots : 1][3][kUpdRing ? kCols : 1];
   // Flux tables over flux rows q = ci - fr0 (fr0 the first flux row): 1/edgedy
   // of the row, celldy of the row below (s_cy[q]) and of the row (s_cy[q + 1]).
   __shared__ R s_iey[kMaxRows + 2], s_cy[kMaxRows + 3];
@@ -1803,8 +1809,24 @@ __device__ __forceinline__ void tile_mom_y_impl(const StepArgs<R>& a, int bx, in
     rb_n = kV ? ra_n : a.rho_r[c - 1];
     ra_n = a.rho_r[c];
   };
-  if (kVel && kV) ra_n = a.rho_r[cidx(nx, i0 - 1, jj)];
-  load_upd(i0);
+  const int t = threadIdx.x;
+  auto issue_upd = [&](int ii) {
+    const int sl = (ii - i0) % kSlots;
+    const size_t c = cidx(nx, ii, jj);
+    cp_async_elem(&s_upd[sl][0][t], kV ? a.rho_v + c : a.rho_u + fidx(nx, ii, jj), true);
+    cp_async_elem(&s_upd[sl][1][t], a.rho_r + c, true);
+    cp_async_elem(&s_upd[sl][2][t], kV ? a.rho_r + c - nx : a.rho_r + c - 1, true);
+  };
+  if constexpr (kUpdRing) {
+#pragma unroll
+    for (int d = 0; d < kAhead; ++d) {
+      if (i0 + d < i1) issue_upd(i0 + d);
+      cp_async_commit();
+    }
+  } else {
+    if (kVel && kV) ra_n = a.rho_r[cidx(nx, i0 - 1, jj)];
+    load_upd(i0);
+  }
   // A loop row computes its flux row unless that is a ghost row or (bottom
   // wall) the row computed above.
   const bool bottom = kV && fr0 != src_row(fr0);
@@ -1832,13 +1854,27 @@ __device__ __forceinline__ void tile_mom_y_impl(const StepArgs<R>& a, int bx, in
       ++wrow;
       cur = flux_at(cs, cs - fr0, Fa, Fb);
     }
-    const R m = m_n, ra = ra_n, rb = rb_n;
-    if (ii + 1 < i1) load_upd(ii + 1);
+    R m, ra, rb;
+    if constexpr (kUpdRing) {
+      cp_async_wait<kAhead - 1>();  // row ii's group has landed
+      const int sl = k % kSlots;
+      m = s_upd[sl][0][t];
+      ra = s_upd[sl][1][t];
+      rb = s_upd[sl][2][t];
+      if (ii + kAhead < i1) issue_upd(ii + kAhead);
+      cp_async_commit();
+    } else {
+      m = m_n;
+      ra = ra_n;
+      rb = rb_n;
+      if (ii + 1 < i1) load_upd(ii + 1);
+    }
     momentum_face_update<R, !kV, kVel, kP2>(a, edge, ii, jj, cur, prev, dt_h, hx, ihx, s_h[k],
                                             s_row[k], kV ? s_wy0[k] : wx0, kV ? s_wy1[k] : wx1,
                                             m, ra, rb, vout);
     prev = cur;
   }
+  if constexpr (kUpdRing) cp_async_wait<0>();
 }
 
 template <typename R, bool kV, bool kVel, bool kRing = true>
@@ -1847,11 +1883,11 @@ __device__ __forceinline__ void tile_mom_x(const StepArgs<R>& a, int bx, int by)
                      (tile_mom_x_impl<R, kV, kVel, true, kRing>(a, bx, by)),
                      (tile_mom_x_impl<R, kV, kVel, false, kRing>(a, bx, by)));
 }
-template <typename R, bool kV, bool kVel>
+template <typename R, bool kV, bool kVel, bool kRing = true>
 __device__ __forceinline__ void tile_mom_y(const StepArgs<R>& a, int bx, int by) {
   FLOW_POW2_DISPATCH(R, a, a.pad + bx * kCols, a.pad + by * a.rows,
-                     (tile_mom_y_impl<R, kV, kVel, true>(a, bx, by)),
-                     (tile_mom_y_impl<R, kV, kVel, false>(a, bx, by)));
+                     (tile_mom_y_impl<R, kV, kVel, true, kRing>(a, bx, by)),
+                     (tile_mom_y_impl<R, kV, kVel, false, kRing>(a, bx, by)));
 }
 
 }  // namespace tiles
