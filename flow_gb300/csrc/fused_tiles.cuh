@@ -1190,14 +1190,56 @@ __device__ __forceinline__ void tile_mass_sweep_x_impl(const StepArgs<R>& a,
       rold_n = kFirst ? rin_n : a.rho[c];
     }
   };
-  if (kEarly && i0 < i1) load(i0);
+  // kEarly (the fused kernel): the face velocity and the cell's density and
+  // energy stream through a per-thread ring of asynchronous copies instead,
+  // two rows ahead (no registers held for them, no barrier: each thread reads
+  // back only what it copied); the second sweep's old density stays a row
+  // ahead in a register (a third ring plane costs more occupancy of shared
+  // memory than it gains).
+  constexpr int kAhead = 2, kSlots = kAhead + 1;
+  __shared__ R s_ru[kEarly ? kSlots : 1][kEarly ? kCols : 1];
+  __shared__ double s_rd[kEarly ? kSlots : 1][2][kEarly ? kCols : 1];
+  auto issue = [&](int ii) {
+    const int sl = (ii - i0) % kSlots;
+    const size_t c = cidx(nx, ii, jj);
+    cp_async_elem(&s_ru[sl][t], face_ok ? a.u + fidx(nx, ii, jj) : a.u, face_ok);
+    cp_async_elem(&s_rd[sl][0][t], cell_ok ? s.r_in + c : s.r_in, cell_ok);
+    cp_async_elem(&s_rd[sl][1][t], cell_ok ? s.e_in + c : s.e_in, cell_ok);
+  };
+  auto load_old = [&](int ii) {
+    if (!kFirst && cell_ok) rold_n = a.rho[cidx(nx, ii, jj)];
+  };
+  if constexpr (kEarly) {
+#pragma unroll
+    for (int d = 0; d < kAhead; ++d) {
+      if (i0 + d < i1) issue(i0 + d);
+      cp_async_commit();
+    }
+    if (i0 < i1) load_old(i0);
+  }
   __syncthreads();
   if (!kEarly && i0 < i1) load(i0);
   for (int ii = i0; ii < i1; ++ii) {
     const int k = ii - i0;
-    const R u0 = u0_n;
-    const double r_in = rin_n, e_in = ein_n, r_old = rold_n;
-    if (ii + 1 < i1) load(ii + 1);
+    R u0;
+    double r_in, e_in, r_old;
+    if constexpr (kEarly) {
+      cp_async_wait<kAhead - 1>();  // row ii's group has landed
+      const int sl = k % kSlots;
+      u0 = s_ru[sl][t];
+      r_in = s_rd[sl][0][t];
+      e_in = s_rd[sl][1][t];
+      r_old = kFirst ? r_in : rold_n;
+      if (ii + kAhead < i1) issue(ii + kAhead);
+      cp_async_commit();
+      if (ii + 1 < i1) load_old(ii + 1);
+    } else {
+      u0 = u0_n;
+      r_in = rin_n;
+      e_in = ein_n;
+      r_old = rold_n;
+      if (ii + 1 < i1) load(ii + 1);
+    }
     R F = R(0), eF = R(0);
     if (face_ok) {
       const size_t f = fidx(nx, ii, jj);
@@ -1229,6 +1271,7 @@ __device__ __forceinline__ void tile_mass_sweep_x_impl(const StepArgs<R>& a,
     }
     __syncthreads();
   }
+  if constexpr (kEarly) cp_async_wait<0>();
 }
 
 template <typename R, bool kFirst, bool kEarly = true>
