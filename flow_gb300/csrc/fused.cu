@@ -106,7 +106,7 @@ __global__ void __launch_bounds__(kCols, Prec<R>::kMixed ? 8 : 7) k_mass_sweep_x
   tile_mass_sweep_x<R, kFirst>(a, s, blockIdx.x, blockIdx.y);
 }
 template <typename R, bool kFirst>
-__global__ void __launch_bounds__(kCols, Prec<R>::kMixed ? 7 : 5) k_mass_sweep_y(const StepArgs<R> a,
+__global__ void __launch_bounds__(kCols, Prec<R>::kMixed ? 7 : 6) k_mass_sweep_y(const StepArgs<R> a,
                                                         const SweepArgs<R> s) {
   pdl_wait();
   pdl_trigger();

@@ -1355,9 +1355,39 @@ __device__ __forceinline__ void tile_mass_sweep_y_impl(const StepArgs<R>& a,
     rw.m2 = r[0]; rw.m1 = r[1]; rw.p0 = r[2]; rw.p1 = r[3];
     ew.m2 = e[0]; ew.m1 = e[1]; ew.p0 = e[2]; ew.p1 = e[3];
   };
+  // kEarly (the fused kernel): the window values stream through a per-thread
+  // ring of asynchronous copies instead, two rows ahead (no registers held
+  // for them, no barrier: each thread reads back only what it copied), and
+  // the FP64 form takes a cell's update inputs from its windows (the same
+  // arrays: r_in_r and e_in_r alias r_in and e_in), so only the second
+  // sweep's old density (and the mixed form's FP64 inputs) stay a row ahead
+  // in registers.
+  constexpr int kAhead = 2, kSlots = kAhead + 1;
+  __shared__ R s_w[kEarly ? kSlots : 1][3][kEarly ? kCols : 1];
+  const int t = threadIdx.x;
+  auto issue = [&](int ii) {
+    const int sl = (ii - i0) % kSlots;
+    const size_t c = cidx(nx, ii + 2, jj);
+    cp_async_elem(&s_w[sl][0][t], s.r_in_r + c, true);
+    cp_async_elem(&s_w[sl][1][t], s.e_in_r + c, true);
+    cp_async_elem(&s_w[sl][2][t], a.v + c, true);
+  };
+  auto load_upd = [&](int ii) {
+    const size_t c = cidx(nx, ii, jj);
+    if (Pr::kMixed) {
+      rin_n = s.r_in[c];
+      ein_n = s.e_in[c];
+    }
+    if (!kFirst) rold_n = a.rho[c];
+  };
   if (kEarly && col_ok) {
     prime();
-    if (i0 < i1) load(i0);
+#pragma unroll
+    for (int d = 0; d < kAhead; ++d) {
+      if (i0 + d < i1) issue(i0 + d);
+      cp_async_commit();
+    }
+    if (i0 < i1) load_upd(i0);
   }
   __syncthreads();
   if (!col_ok) return;
@@ -1399,9 +1429,34 @@ __device__ __forceinline__ void tile_mass_sweep_y_impl(const StepArgs<R>& a,
   if (!kEarly && i0 < i1) load(i0);
   for (int ii = i0; ii < i1; ++ii) {
     const int k = ii - i0;
-    const R rn = rn_n, en = en_n, vn = vn_n;
-    const double r_in = rin_n, e_in = ein_n, r_old = rold_n;
-    if (ii + 1 < i1) load(ii + 1);
+    R rn, en, vn;
+    double r_in, e_in, r_old;
+    if constexpr (kEarly) {
+      cp_async_wait<kAhead - 1>();  // row ii's group has landed
+      const int sl = k % kSlots;
+      rn = s_w[sl][0][t];
+      en = s_w[sl][1][t];
+      vn = s_w[sl][2][t];
+      if (ii + kAhead < i1) issue(ii + kAhead);
+      cp_async_commit();
+      if constexpr (Pr::kMixed) {
+        r_in = rin_n;
+        e_in = ein_n;
+      } else {
+        r_in = rw.p0;  // cell ii, the window's upper middle value before this row's shift
+        e_in = ew.p0;
+      }
+      r_old = kFirst ? r_in : rold_n;
+      if (ii + 1 < i1) load_upd(ii + 1);
+    } else {
+      rn = rn_n;
+      en = en_n;
+      vn = vn_n;
+      r_in = rin_n;
+      e_in = ein_n;
+      r_old = rold_n;
+      if (ii + 1 < i1) load(ii + 1);
+    }
     R F1 = R(0), eF1 = R(0);
     const bool was_fresh = fresh;
     // Shift the velocity window's values; face row k+1 has velocity vp.
@@ -1446,6 +1501,7 @@ __device__ __forceinline__ void tile_mass_sweep_y_impl(const StepArgs<R>& a,
     f0d = f1d;
     ef0d = ef1d;
   }
+  if constexpr (kEarly) cp_async_wait<0>();
 }
 
 template <typename R, bool kFirst, bool kEarly = true>
