@@ -1803,6 +1803,10 @@ __device__ __forceinline__ void tile_mom_y_impl(const StepArgs<R>& a, int bx, in
   constexpr bool kUpdRing = kVel && kRing;
   constexpr int kAhead = 2, kSlots = kAhead + 1;
   __shared__ R s_upd[kUpdRing ? kSlots : 1][3][kUpdRing ? kCols : 1];
+  // The other pairs (no velocity update): the mass fluxes and window value of
+  // the flux rows stream through the ring instead.
+  constexpr bool kFluxRing = !kVel && kRing;
+  __shared__ R s_flux[kFluxRing ? kSlots : 1][3][kFluxRing ? kCols : 1];
   // Flux tables over flux rows q = ci - fr0 (fr0 the first flux row): 1/edgedy
   // of the row, celldy of the row below (s_cy[q]) and of the row (s_cy[q + 1]).
   __shared__ R s_iey[kMaxRows + 2], s_cy[kMaxRows + 3];
@@ -1895,8 +1899,43 @@ __device__ __forceinline__ void tile_mom_y_impl(const StepArgs<R>& a, int bx, in
     Fb_n = kV ? a.F_y[c + nx] : a.F_y[c - 1];
     wv_n = w[widx(ci + wlo + 3)];
   };
-  load(wrow);
-  R prev = flux_at(wrow, wrow - fr0, Fa_n, Fb_n);
+  // The flux rows a column consumes are consecutive: from the window's first
+  // row to the last row that is not a ghost (kFluxRing: one copy group per
+  // row, in that order).
+  const int w0row = wrow;
+  const int rmax = kV ? min(i1 - 1, ny - pad - 1) : i1;
+  auto issue_flux = [&](int ci) {
+    const int sl = (ci - w0row) % kSlots;
+    const size_t c = cidx(nx, ci, jj);
+    cp_async_elem(&s_flux[sl][0][threadIdx.x], a.F_y + c, true);
+    cp_async_elem(&s_flux[sl][1][threadIdx.x], kV ? a.F_y + c + nx : a.F_y + c - 1, true);
+    cp_async_elem(&s_flux[sl][2][threadIdx.x], w + widx(ci + wlo + 3), true);
+  };
+  // Row ci's values from the ring (its group waited for), the row kAhead
+  // rows on issued.
+  auto take_flux = [&](int ci, R* Fa, R* Fb, R* wv) {
+    cp_async_wait<kAhead - 1>();
+    const int sl = (ci - w0row) % kSlots;
+    *Fa = s_flux[sl][0][threadIdx.x];
+    *Fb = s_flux[sl][1][threadIdx.x];
+    *wv = s_flux[sl][2][threadIdx.x];
+    if (ci + kAhead <= rmax) issue_flux(ci + kAhead);
+    cp_async_commit();
+  };
+  R prev;
+  if constexpr (kFluxRing) {
+#pragma unroll
+    for (int d = 0; d < kAhead; ++d) {
+      if (w0row + d <= rmax) issue_flux(w0row + d);
+      cp_async_commit();
+    }
+    R Fa, Fb, wv;
+    take_flux(wrow, &Fa, &Fb, &wv);
+    prev = flux_at(wrow, wrow - fr0, Fa, Fb);
+  } else {
+    load(wrow);
+    prev = flux_at(wrow, wrow - fr0, Fa_n, Fb_n);
+  }
   const R top = prev;  // rho_v: the flux of the first flux row's mirror source
   // The update inputs of face row ii (momentum and densities, kVel), loaded a
   // row ahead; rho_v's lower density is the row below's upper one.
@@ -1929,7 +1968,10 @@ __device__ __forceinline__ void tile_mom_y_impl(const StepArgs<R>& a, int bx, in
   // A loop row computes its flux row unless that is a ghost row or (bottom
   // wall) the row computed above.
   const bool bottom = kV && fr0 != src_row(fr0);
-  if (i0 < i1 && !(bottom && i0 == src_row(fr0)) && src_row(kV ? i0 : i0 + 1) == (kV ? i0 : i0 + 1)) {
+  if (kFluxRing) {
+    // (the ring holds the next rows already)
+  } else if (i0 < i1 && !(bottom && i0 == src_row(fr0)) &&
+             src_row(kV ? i0 : i0 + 1) == (kV ? i0 : i0 + 1)) {
     load(kV ? i0 : i0 + 1);
   } else if (bottom && i0 + 1 < i1) {
     load(i0 + 1);
@@ -1946,9 +1988,16 @@ __device__ __forceinline__ void tile_mom_y_impl(const StepArgs<R>& a, int bx, in
     } else if (bottom && ci == wrow) {
       cur = top;  // the bottom wall's first interior row: computed already
     } else {
-      const R Fa = Fa_n, Fb = Fb_n, wv = wv_n;
-      const int cn = ci + 1;
-      if (ii + 1 < i1 && src_row(cn) == cn) load(cn);
+      R Fa, Fb, wv;
+      if constexpr (kFluxRing) {
+        take_flux(ci, &Fa, &Fb, &wv);
+      } else {
+        Fa = Fa_n;
+        Fb = Fb_n;
+        wv = wv_n;
+        const int cn = ci + 1;
+        if (ii + 1 < i1 && src_row(cn) == cn) load(cn);
+      }
       win.push(wv);
       ++wrow;
       cur = flux_at(cs, cs - fr0, Fa, Fb);
@@ -1973,7 +2022,7 @@ __device__ __forceinline__ void tile_mom_y_impl(const StepArgs<R>& a, int bx, in
                                             m, ra, rb, vout);
     prev = cur;
   }
-  if constexpr (kUpdRing) cp_async_wait<0>();
+  if constexpr (kUpdRing || kFluxRing) cp_async_wait<0>();
 }
 
 template <typename R, bool kV, bool kVel, bool kRing = true>
