@@ -1634,6 +1634,11 @@ __device__ __forceinline__ void tile_mom_x_impl(const StepArgs<R>& a, int bx, in
   constexpr bool kUpdRing = kVel && kRing;
   constexpr int kAhead = 2, kSlots = kAhead + 1;
   __shared__ R s_upd[kUpdRing ? kSlots : 1][3][kUpdRing ? kCols : 1];
+  // The other pairs (no velocity update), FP64 form: a row's mass fluxes (and
+  // for rho_v the u at the corner) stream through the ring instead.  (The
+  // mixed form measured slower with it.)
+  constexpr bool kFluxRing = !kVel && kRing && !Pr::kMixed;
+  __shared__ R s_flux[kFluxRing ? kSlots : 1][2][kFluxRing ? kCols : 1];
   const int nx = a.nx, ny = a.ny, pad = a.pad;
   const int t = threadIdx.x;
   const int c0 = (kV ? pad : pad - 1) + bx * (kCols - 1);
@@ -1691,13 +1696,27 @@ __device__ __forceinline__ void tile_mom_x_impl(const StepArgs<R>& a, int bx, in
     Fb_n = kV ? R(0) : a.F_x[f + 1];
     if (kV) u0_n = uu[f];
   };
+  auto issue_flux = [&](int ii) {
+    const int sl = (ii - i0) % kSlots;
+    const size_t f = fidx(nx, ii, js);
+    cp_async_elem(&s_flux[sl][0][t], flux_ok ? a.F_x + f : a.F_x, flux_ok);
+    cp_async_elem(&s_flux[sl][1][t], flux_ok ? (kV ? uu + f : a.F_x + f + 1) : a.F_x, flux_ok);
+  };
   if (i0 < i1) {
     if (kV && flux_ok) {
       const size_t f = fidx(nx, i0 - 1, j);
       F_dn = a.F_x[f];
       u_dn = uu[f];
     }
-    load(i0);
+    if constexpr (kFluxRing) {
+#pragma unroll
+      for (int d = 0; d < kAhead; ++d) {
+        if (i0 + d < i1) issue_flux(i0 + d);
+        cp_async_commit();
+      }
+    } else {
+      load(i0);
+    }
   }
   auto issue_upd = [&](int ii) {
     const int sl = (ii - i0) % kSlots;
@@ -1717,13 +1736,26 @@ __device__ __forceinline__ void tile_mom_x_impl(const StepArgs<R>& a, int bx, in
   }
   __syncthreads();
   if (i0 >= i1) {
-    if constexpr (kUpdRing) cp_async_wait<0>();
+    if constexpr (kUpdRing || kFluxRing) cp_async_wait<0>();
     return;
   }
   for (int ii = i0; ii < i1; ++ii) {
     const int k = ii - i0;
-    const R Fa = Fa_n, Fb = Fb_n, u0 = u0_n;
-    if (ii + 1 < i1) load(ii + 1);
+    R Fa, Fb, u0;
+    if constexpr (kFluxRing) {
+      cp_async_wait<kAhead - 1>();  // row ii's group has landed
+      const int sl = k % kSlots;
+      Fa = s_flux[sl][0][t];
+      Fb = kV ? R(0) : s_flux[sl][1][t];
+      u0 = kV ? s_flux[sl][1][t] : R(0);
+      if (ii + kAhead < i1) issue_flux(ii + kAhead);
+      cp_async_commit();
+    } else {
+      Fa = Fa_n;
+      Fb = Fb_n;
+      u0 = u0_n;
+      if (ii + 1 < i1) load(ii + 1);
+    }
     R val = R(0);
     if (flux_ok) {
       const size_t f = fidx(nx, ii, js);
@@ -1782,7 +1814,7 @@ __device__ __forceinline__ void tile_mom_x_impl(const StepArgs<R>& a, int bx, in
     }
     __syncthreads();
   }
-  if constexpr (kUpdRing) cp_async_wait<0>();
+  if constexpr (kUpdRing || kFluxRing) cp_async_wait<0>();
 }
 
 // y pairs: each thread marches down its column, carrying the flux of the
