@@ -61,16 +61,16 @@ KERNEL_BYTES_PER_CELL = {
 # Sedov blast at the benchmark size, 4096^2, after five timesteps; scaled to a
 # launch by its cell count.
 NCU_TRAFFIC_BYTES_PER_CELL = {
-    "lag_pressure": 62.5,
-    "lag_viscosity": 38.8,
-    "lag_viscous_accel": 16.1,
-    "lag_energy_dt": 48.6,
-    "mass_sweep_x": 53.3,
-    "mass_sweep_y": 45.4,
-    "mom_uFx": 30.7,             # the launch that recomputes u
-    "mom_uFy": 16.1,
-    "mom_vFx": 39.8,             # the launch that recomputes v
-    "mom_vFy": 16.1,
+    "lag_pressure": 62.2,
+    "lag_viscosity": 38.7,
+    "lag_viscous_accel": 16.0,
+    "lag_energy_dt": 48.4,
+    "mass_sweep_x": 53.1,
+    "mass_sweep_y": 45.7,
+    "mom_uFx": 30.6,             # the launch that recomputes u
+    "mom_uFy": 16.0,
+    "mom_vFx": 39.1,             # the launch that recomputes v
+    "mom_vFy": 16.0,
 }
 
 
