@@ -147,6 +147,16 @@ template <int n>
 __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;\n" ::"n"(n) : "memory");
 }
+// The shared-memory slots of an asynchronous-copy ring, [slots][planes][cols]
+// of T.  Declared here rather than in the tile: a tile's power-of-two and
+// general variants are both compiled into its kernel, and shared arrays
+// declared in each would be allocated twice; this function's array is one
+// allocation per kernel for each (T, shape, tag).
+template <typename T, int kSlotsN, int kPlanes, int kColsN, int kTag>
+__device__ __forceinline__ T (*ring_slots())[kPlanes][kColsN] {
+  __shared__ T buf[kSlotsN][kPlanes][kColsN];
+  return buf;
+}
 
 // pred holds in every active lane of the warp (a warp-uniform branch
 // condition).
@@ -639,7 +649,7 @@ __device__ __forceinline__ void tile_lag_viscous_accel_impl(const StepArgs<R>& a
     // group per row.  kAhead + 1 slots: a row's slot is refilled one row
     // after it was read.
     constexpr int kAhead = 2, kSlots = kAhead + 1;
-    __shared__ R s_q[kSlots][3][kCols];
+    auto s_q = ring_slots<R, kSlots, 3, kCols, 1>();
     const int t = threadIdx.x;
     auto issue = [&](int ii) {
       const int sl = (ii - i0) % kSlots;
@@ -1197,12 +1207,12 @@ __device__ __forceinline__ void tile_mass_sweep_x_impl(const StepArgs<R>& a,
   // ahead in a register (a third ring plane costs more occupancy of shared
   // memory than it gains).
   constexpr int kAhead = 2, kSlots = kAhead + 1;
-  __shared__ R s_ru[kEarly ? kSlots : 1][kEarly ? kCols : 1];
-  __shared__ double s_rd[kEarly ? kSlots : 1][2][kEarly ? kCols : 1];
+  auto s_ru = ring_slots<R, kEarly ? kSlots : 1, 1, kEarly ? kCols : 1, 6>();
+  auto s_rd = ring_slots<double, kEarly ? kSlots : 1, 2, kEarly ? kCols : 1, 7>();
   auto issue = [&](int ii) {
     const int sl = (ii - i0) % kSlots;
     const size_t c = cidx(nx, ii, jj);
-    cp_async_elem(&s_ru[sl][t], face_ok ? a.u + fidx(nx, ii, jj) : a.u, face_ok);
+    cp_async_elem(&s_ru[sl][0][t], face_ok ? a.u + fidx(nx, ii, jj) : a.u, face_ok);
     cp_async_elem(&s_rd[sl][0][t], cell_ok ? s.r_in + c : s.r_in, cell_ok);
     cp_async_elem(&s_rd[sl][1][t], cell_ok ? s.e_in + c : s.e_in, cell_ok);
   };
@@ -1226,7 +1236,7 @@ __device__ __forceinline__ void tile_mass_sweep_x_impl(const StepArgs<R>& a,
     if constexpr (kEarly) {
       cp_async_wait<kAhead - 1>();  // row ii's group has landed
       const int sl = k % kSlots;
-      u0 = s_ru[sl][t];
+      u0 = s_ru[sl][0][t];
       r_in = s_rd[sl][0][t];
       e_in = s_rd[sl][1][t];
       r_old = kFirst ? r_in : rold_n;
@@ -1363,7 +1373,7 @@ __device__ __forceinline__ void tile_mass_sweep_y_impl(const StepArgs<R>& a,
   // sweep's old density (and the mixed form's FP64 inputs) stay a row ahead
   // in registers.
   constexpr int kAhead = 2, kSlots = kAhead + 1;
-  __shared__ R s_w[kEarly ? kSlots : 1][3][kEarly ? kCols : 1];
+  auto s_w = ring_slots<R, kEarly ? kSlots : 1, 3, kEarly ? kCols : 1, 8>();
   const int t = threadIdx.x;
   auto issue = [&](int ii) {
     const int sl = (ii - i0) % kSlots;
@@ -1633,12 +1643,12 @@ __device__ __forceinline__ void tile_mom_x_impl(const StepArgs<R>& a, int bx, in
   // no barrier: each thread reads back only what it copied).
   constexpr bool kUpdRing = kVel && kRing;
   constexpr int kAhead = 2, kSlots = kAhead + 1;
-  __shared__ R s_upd[kUpdRing ? kSlots : 1][3][kUpdRing ? kCols : 1];
+  auto s_upd = ring_slots<R, kUpdRing ? kSlots : 1, 3, kUpdRing ? kCols : 1, 2>();
   // The other pairs (no velocity update), FP64 form: a row's mass fluxes (and
   // for rho_v the u at the corner) stream through the ring instead.  (The
   // mixed form measured slower with it.)
   constexpr bool kFluxRing = !kVel && kRing && !Pr::kMixed;
-  __shared__ R s_flux[kFluxRing ? kSlots : 1][2][kFluxRing ? kCols : 1];
+  auto s_flux = ring_slots<R, kFluxRing ? kSlots : 1, 2, kFluxRing ? kCols : 1, 3>();
   const int nx = a.nx, ny = a.ny, pad = a.pad;
   const int t = threadIdx.x;
   const int c0 = (kV ? pad : pad - 1) + bx * (kCols - 1);
@@ -1834,11 +1844,11 @@ __device__ __forceinline__ void tile_mom_y_impl(const StepArgs<R>& a, int bx, in
   // the x pairs).
   constexpr bool kUpdRing = kVel && kRing;
   constexpr int kAhead = 2, kSlots = kAhead + 1;
-  __shared__ R s_upd[kUpdRing ? kSlots : 1][3][kUpdRing ? kCols : 1];
+  auto s_upd = ring_slots<R, kUpdRing ? kSlots : 1, 3, kUpdRing ? kCols : 1, 4>();
   // The other pairs (no velocity update): the mass fluxes and window value of
   // the flux rows stream through the ring instead.
   constexpr bool kFluxRing = !kVel && kRing;
-  __shared__ R s_flux[kFluxRing ? kSlots : 1][3][kFluxRing ? kCols : 1];
+  auto s_flux = ring_slots<R, kFluxRing ? kSlots : 1, 3, kFluxRing ? kCols : 1, 5>();
   // Flux tables over flux rows q = ci - fr0 (fr0 the first flux row): 1/edgedy
   // of the row, celldy of the row below (s_cy[q]) and of the row (s_cy[q + 1]).
   __shared__ R s_iey[kMaxRows + 2], s_cy[kMaxRows + 3];
