@@ -648,7 +648,7 @@ __device__ __forceinline__ void tile_lag_viscous_accel_impl(const StepArgs<R>& a
     // shared-memory slots (no registers held for them, no barrier), one copy
     // group per row.  kAhead + 1 slots: a row's slot is refilled one row
     // after it was read.
-    constexpr int kAhead = 2, kSlots = kAhead + 1;
+    constexpr int kAhead = Pr::kMixed ? 2 : 3, kSlots = kAhead + 1;
     auto s_q = ring_slots<R, kSlots, 3, kCols, 1>();
     const int t = threadIdx.x;
     auto issue = [&](int ii) {
@@ -1202,11 +1202,10 @@ __device__ __forceinline__ void tile_mass_sweep_x_impl(const StepArgs<R>& a,
   };
   // kEarly (the fused kernel): the face velocity and the cell's density and
   // energy stream through a per-thread ring of asynchronous copies instead,
-  // two rows ahead (no registers held for them, no barrier: each thread reads
-  // back only what it copied); the second sweep's old density stays a row
-  // ahead in a register (a third ring plane costs more occupancy of shared
-  // memory than it gains).
-  constexpr int kAhead = 2, kSlots = kAhead + 1;
+  // kAhead rows ahead: no registers held for them, no barrier (each thread
+  // reads back only what it copied).  The second sweep's old density stays a
+  // row ahead in a register (a third ring plane cost more than it gained).
+  constexpr int kAhead = Pr::kMixed ? 2 : 3, kSlots = kAhead + 1;
   auto s_ru = ring_slots<R, kEarly ? kSlots : 1, 1, kEarly ? kCols : 1, 6>();
   auto s_rd = ring_slots<double, kEarly ? kSlots : 1, 2, kEarly ? kCols : 1, 7>();
   auto issue = [&](int ii) {
@@ -1366,13 +1365,13 @@ __device__ __forceinline__ void tile_mass_sweep_y_impl(const StepArgs<R>& a,
     ew.m2 = e[0]; ew.m1 = e[1]; ew.p0 = e[2]; ew.p1 = e[3];
   };
   // kEarly (the fused kernel): the window values stream through a per-thread
-  // ring of asynchronous copies instead, two rows ahead (no registers held
+  // ring of asynchronous copies instead, kAhead rows ahead (no registers held
   // for them, no barrier: each thread reads back only what it copied), and
   // the FP64 form takes a cell's update inputs from its windows (the same
   // arrays: r_in_r and e_in_r alias r_in and e_in), so only the second
   // sweep's old density (and the mixed form's FP64 inputs) stay a row ahead
   // in registers.
-  constexpr int kAhead = 2, kSlots = kAhead + 1;
+  constexpr int kAhead = Pr::kMixed ? 2 : 3, kSlots = kAhead + 1;
   auto s_w = ring_slots<R, kEarly ? kSlots : 1, 3, kEarly ? kCols : 1, 8>();
   const int t = threadIdx.x;
   auto issue = [&](int ii) {
@@ -1639,10 +1638,12 @@ __device__ __forceinline__ void tile_mom_x_impl(const StepArgs<R>& a, int bx, in
   __shared__ R sF[kCols];
   // kVel and kRing (the fused kernels): the update inputs of a face (its
   // momentum and the densities either side) stream through a per-thread
-  // ring of asynchronous copies, two rows ahead (no registers held for them,
-  // no barrier: each thread reads back only what it copied).
+  // ring of asynchronous copies, kAhead rows ahead (no registers held for
+  // them, no barrier: each thread reads back only what it copied).  Three
+  // rows in the FP64 form, two in the mixed form (which measured slower with
+  // three), as in every ring of the fused tiles.
   constexpr bool kUpdRing = kVel && kRing;
-  constexpr int kAhead = 2, kSlots = kAhead + 1;
+  constexpr int kAhead = Pr::kMixed ? 2 : 3, kSlots = kAhead + 1;
   auto s_upd = ring_slots<R, kUpdRing ? kSlots : 1, 3, kUpdRing ? kCols : 1, 2>();
   // The other pairs (no velocity update), FP64 form: a row's mass fluxes (and
   // for rho_v the u at the corner) stream through the ring instead.  (The
@@ -1840,10 +1841,10 @@ template <typename R, bool kV, bool kVel, bool kP2, bool kRing>
 __device__ __forceinline__ void tile_mom_y_impl(const StepArgs<R>& a, int bx, int by) {
   using Pr = Prec<R>;
   // kVel and kRing (the fused kernels): the update inputs of a face stream
-  // through a per-thread ring of asynchronous copies, two rows ahead (as in
-  // the x pairs).
+  // through a per-thread ring of asynchronous copies, kAhead rows ahead (as
+  // in the x pairs).
   constexpr bool kUpdRing = kVel && kRing;
-  constexpr int kAhead = 2, kSlots = kAhead + 1;
+  constexpr int kAhead = Pr::kMixed ? 2 : 3, kSlots = kAhead + 1;
   auto s_upd = ring_slots<R, kUpdRing ? kSlots : 1, 3, kUpdRing ? kCols : 1, 4>();
   // The other pairs (no velocity update): the mass fluxes and window value of
   // the flux rows stream through the ring instead.
