@@ -115,7 +115,7 @@ __device__ __forceinline__ void run_tile(int ph, const Instance<R>& I, int tx, i
     case kPhPressure: tile_lag_pressure(I.a, tx, ty); break;
     case kPhViscosity: tile_lag_viscosity(I.a, tx, ty); break;
     case kPhAccel: tile_lag_viscous_accel<R, false>(I.a, tx, ty); break;
-    case kPhEnergy: tile_lag_energy_dt(I.a, tx, ty); break;
+    case kPhEnergy: tile_lag_energy_dt<R, false>(I.a, tx, ty); break;
     case kPhSweepX1: tile_mass_sweep_x<R, true, false>(I.a, I.first, tx, ty); break;
     case kPhSweepY1: tile_mass_sweep_y<R, true, false>(I.a, I.first, tx, ty); break;
     case kPhSweepX2: tile_mass_sweep_x<R, false, false>(I.a, I.second, tx, ty); break;

@@ -703,7 +703,7 @@ __device__ __forceinline__ unsigned long long warp_min_u64(unsigned long long x)
 // block on the FP64 bit pattern of its smallest candidate; the last block to
 // finish applies the leapfrog dt/dt_h rule (finish_dt).  In the mixed form
 // the FP32 energy change is added to the FP64 energy.
-template <typename R, bool kP2>
+template <typename R, bool kP2, bool kRing>
 __device__ __forceinline__ void tile_lag_energy_dt_impl(const StepArgs<R>& a, int bx, int by) {
   using Pr = Prec<R>;
   __shared__ R s_icy[kMaxRows], s_cy[kMaxRows];
@@ -734,9 +734,15 @@ __device__ __forceinline__ void tile_lag_energy_dt_impl(const StepArgs<R>& a, in
     const int i1 = min(i0 + a.rows, ny - pad);
     R v0 = a.v[cidx(nx, i0, jj)];
     // Mixed form: row ii+1's inputs are loaded before row ii is processed.
-    // (The FP64 form, at 64 registers without it, loses more occupancy than
-    // it gains.)  The FP64 pressure is read only where a cell is compressed.
+    // The FP64 form (at 64 registers without that, which loses more
+    // occupancy than it gains) streams them through a per-thread ring of
+    // asynchronous copies instead when kRing (the fused kernel), kEAhead rows
+    // ahead.  The FP64 pressure is read only where a cell is compressed.
     constexpr bool kAhead = Pr::kMixed;
+    constexpr bool kERing = kRing && !Pr::kMixed;
+    constexpr int kEAhead = 2, kESlots = kEAhead + 1;
+    auto s_in = ring_slots<R, kERing ? kESlots : 1, 7, kERing ? kCols : 1, 9>();
+    const int t = threadIdx.x;
     R v1_n = R(0), r_n = R(0), er_n = R(0), qx_n = R(0), qy_n = R(0), u0_n = R(0), u1_n = R(0);
     auto load = [&](int ii) {
       const size_t c = cidx(nx, ii, jj);
@@ -749,11 +755,44 @@ __device__ __forceinline__ void tile_lag_energy_dt_impl(const StepArgs<R>& a, in
       u0_n = a.u[f];
       u1_n = a.u[f + 1];
     };
+    auto issue = [&](int ii) {
+      const int sl = (ii - i0) % kESlots;
+      const size_t c = cidx(nx, ii, jj);
+      const size_t f = c + (size_t)ii;  // fidx(nx, ii, jj)
+      cp_async_elem(&s_in[sl][0][t], a.v + c + nx, true);
+      cp_async_elem(&s_in[sl][1][t], a.rho_r + c, true);
+      cp_async_elem(&s_in[sl][2][t], a.e_r + c, true);
+      cp_async_elem(&s_in[sl][3][t], a.Qxx + c, true);
+      cp_async_elem(&s_in[sl][4][t], a.Qyy + c, true);
+      cp_async_elem(&s_in[sl][5][t], a.u + f, true);
+      cp_async_elem(&s_in[sl][6][t], a.u + f + 1, true);
+    };
+    if constexpr (kERing) {
+#pragma unroll
+      for (int d = 0; d < kEAhead; ++d) {
+        if (i0 + d < i1) issue(i0 + d);
+        cp_async_commit();
+      }
+    }
     if (kAhead && i0 < i1) load(i0);
     for (int ii = i0; ii < i1; ++ii) {
       const int k = ii - i0;
       const size_t c = cidx(nx, ii, jj);
-      if (!kAhead) load(ii);
+      if constexpr (kERing) {
+        cp_async_wait<kEAhead - 1>();  // row ii's group has landed
+        const int sl = k % kESlots;
+        v1_n = s_in[sl][0][t];
+        r_n = s_in[sl][1][t];
+        er_n = s_in[sl][2][t];
+        qx_n = s_in[sl][3][t];
+        qy_n = s_in[sl][4][t];
+        u0_n = s_in[sl][5][t];
+        u1_n = s_in[sl][6][t];
+        if (ii + kEAhead < i1) issue(ii + kEAhead);
+        cp_async_commit();
+      } else if (!kAhead) {
+        load(ii);
+      }
       const R v1 = v1_n, r = r_n, er = er_n, qx = qx_n, qy = qy_n, u0f = u0_n, u1f = u1_n;
       if (kAhead && ii + 1 < i1) load(ii + 1);
       const bool rz = Pr::is_zero(r);
@@ -838,6 +877,7 @@ __device__ __forceinline__ void tile_lag_energy_dt_impl(const StepArgs<R>& a, in
       }
       v0 = v1;
     }
+    if constexpr (kERing) cp_async_wait<0>();
   }
   if (!Pr::kMixed && kbest >= 0) best = (unsigned long long)dbits(c_best * d_rsqrt(s_best));
   best = warp_min_u64(best);
@@ -850,11 +890,11 @@ __device__ __forceinline__ void tile_lag_energy_dt_impl(const StepArgs<R>& a, in
   }
 }
 
-template <typename R>
+template <typename R, bool kRing = true>
 __device__ __forceinline__ void tile_lag_energy_dt(const StepArgs<R>& a, int bx, int by) {
   FLOW_POW2_DISPATCH(R, a, a.pad + bx * kCols, a.pad + by * a.rows,
-                     (tile_lag_energy_dt_impl<R, true>(a, bx, by)),
-                     (tile_lag_energy_dt_impl<R, false>(a, bx, by)));
+                     (tile_lag_energy_dt_impl<R, true, kRing>(a, bx, by)),
+                     (tile_lag_energy_dt_impl<R, false, kRing>(a, bx, by)));
 }
 
 // The leapfrog dt/dt_h rule of omp3/flow.c:103-105 applied to the finished
