@@ -43,7 +43,7 @@ KERNEL_BYTES_PER_CELL = {
     "lag_pressure": 8 * 8,       # rho, e, rho_u, rho_v in; P, rho_old, u, v out
     "lag_viscosity": 8 * 5,      # u, v, rho in; Qxx, Qyy out
     "lag_viscous_accel": 8 * 2,  # Qxx, Qyy in (momenta, densities, velocities where a stress gradient acts)
-    "lag_energy_dt": 8 * 7,      # rho, P, e, Qxx, Qyy, u, v in (e out where the cell is compressed)
+    "lag_energy_dt": 8 * 6,      # rho, e, Qxx, Qyy, u, v in (P in, e out where the cell is compressed)
     "mass_sweep_x": 8 * 6,       # rho, e, u in; rho, e, F_x out
     "mass_sweep_y": 8 * 6,
     # Momentum pairs (flux fused with its update), one launch per step each;
