@@ -1241,22 +1241,22 @@ __device__ __forceinline__ void tile_mass_sweep_x_impl(const StepArgs<R>& a,
     }
   };
   // kEarly (the fused kernel): the face velocity and the cell's density and
-  // energy stream through a per-thread ring of asynchronous copies instead,
-  // kAhead rows ahead: no registers held for them, no barrier (each thread
-  // reads back only what it copied).  The second sweep's old density stays a
-  // row ahead in a register (a third ring plane cost more than it gained).
+  // energy (and in the second sweep its old density) stream through a
+  // per-thread ring of asynchronous copies instead, kAhead rows ahead: no
+  // registers held for them, no barrier (each thread reads back only what it
+  // copied).
   constexpr int kAhead = Pr::kMixed ? 2 : 3, kSlots = kAhead + 1;
   auto s_ru = ring_slots<R, kEarly ? kSlots : 1, 1, kEarly ? kCols : 1, 6>();
-  auto s_rd = ring_slots<double, kEarly ? kSlots : 1, 2, kEarly ? kCols : 1, 7>();
+  auto s_rd = ring_slots<double, kEarly ? kSlots : 1, kFirst ? 2 : 3, kEarly ? kCols : 1, 7>();
   auto issue = [&](int ii) {
     const int sl = (ii - i0) % kSlots;
     const size_t c = cidx(nx, ii, jj);
     cp_async_elem(&s_ru[sl][0][t], face_ok ? a.u + fidx(nx, ii, jj) : a.u, face_ok);
     cp_async_elem(&s_rd[sl][0][t], cell_ok ? s.r_in + c : s.r_in, cell_ok);
     cp_async_elem(&s_rd[sl][1][t], cell_ok ? s.e_in + c : s.e_in, cell_ok);
-  };
-  auto load_old = [&](int ii) {
-    if (!kFirst && cell_ok) rold_n = a.rho[cidx(nx, ii, jj)];
+    if constexpr (!kFirst) {
+      cp_async_elem(&s_rd[sl][kFirst ? 1 : 2][t], cell_ok ? a.rho + c : a.rho, cell_ok);
+    }
   };
   if constexpr (kEarly) {
 #pragma unroll
@@ -1264,7 +1264,6 @@ __device__ __forceinline__ void tile_mass_sweep_x_impl(const StepArgs<R>& a,
       if (i0 + d < i1) issue(i0 + d);
       cp_async_commit();
     }
-    if (i0 < i1) load_old(i0);
   }
   __syncthreads();
   if (!kEarly && i0 < i1) load(i0);
@@ -1278,10 +1277,9 @@ __device__ __forceinline__ void tile_mass_sweep_x_impl(const StepArgs<R>& a,
       u0 = s_ru[sl][0][t];
       r_in = s_rd[sl][0][t];
       e_in = s_rd[sl][1][t];
-      r_old = kFirst ? r_in : rold_n;
+      r_old = kFirst ? r_in : s_rd[sl][kFirst ? 1 : 2][t];
       if (ii + kAhead < i1) issue(ii + kAhead);
       cp_async_commit();
-      if (ii + 1 < i1) load_old(ii + 1);
     } else {
       u0 = u0_n;
       r_in = rin_n;
