@@ -64,9 +64,9 @@ NCU_TRAFFIC_BYTES_PER_CELL = {
     "lag_pressure": 62.2,
     "lag_viscosity": 38.7,
     "lag_viscous_accel": 16.0,
-    "lag_energy_dt": 48.4,
-    "mass_sweep_x": 53.1,
-    "mass_sweep_y": 45.7,
+    "lag_energy_dt": 48.2,
+    "mass_sweep_x": 53.0,
+    "mass_sweep_y": 45.4,
     "mom_uFx": 30.6,             # the launch that recomputes u
     "mom_uFy": 16.0,
     "mom_vFx": 39.1,             # the launch that recomputes v
