@@ -1410,7 +1410,10 @@ __device__ __forceinline__ void tile_mass_sweep_y_impl(const StepArgs<R>& a,
   // sweep's old density (and the mixed form's FP64 inputs) stay a row ahead
   // in registers.
   constexpr int kAhead = Pr::kMixed ? 2 : 3, kSlots = kAhead + 1;
-  auto s_w = ring_slots<R, kEarly ? kSlots : 1, 3, kEarly ? kCols : 1, 8>();
+  // The FP64 second sweep's old density of row ii rides in the same group (a
+  // fourth plane).
+  constexpr bool kOldRing = !kFirst && !Pr::kMixed;
+  auto s_w = ring_slots<R, kEarly ? kSlots : 1, kOldRing ? 4 : 3, kEarly ? kCols : 1, 8>();
   const int t = threadIdx.x;
   auto issue = [&](int ii) {
     const int sl = (ii - i0) % kSlots;
@@ -1418,6 +1421,7 @@ __device__ __forceinline__ void tile_mass_sweep_y_impl(const StepArgs<R>& a,
     cp_async_elem(&s_w[sl][0][t], s.r_in_r + c, true);
     cp_async_elem(&s_w[sl][1][t], s.e_in_r + c, true);
     cp_async_elem(&s_w[sl][2][t], a.v + c, true);
+    if constexpr (kOldRing) cp_async_elem(&s_w[sl][3][t], a.rho + cidx(nx, ii, jj), true);
   };
   auto load_upd = [&](int ii) {
     const size_t c = cidx(nx, ii, jj);
@@ -1425,7 +1429,7 @@ __device__ __forceinline__ void tile_mass_sweep_y_impl(const StepArgs<R>& a,
       rin_n = s.r_in[c];
       ein_n = s.e_in[c];
     }
-    if (!kFirst) rold_n = a.rho[c];
+    if (!kFirst && !kOldRing) rold_n = a.rho[c];
   };
   if (kEarly && col_ok) {
     prime();
@@ -1493,7 +1497,11 @@ __device__ __forceinline__ void tile_mass_sweep_y_impl(const StepArgs<R>& a,
         r_in = rw.p0;  // cell ii, the window's upper middle value before this row's shift
         e_in = ew.p0;
       }
-      r_old = kFirst ? r_in : rold_n;
+      if constexpr (kOldRing) {
+        r_old = s_w[sl][3][t];
+      } else {
+        r_old = kFirst ? r_in : rold_n;
+      }
       if (ii + 1 < i1) load_upd(ii + 1);
     } else {
       rn = rn_n;
