@@ -737,7 +737,9 @@ __device__ __forceinline__ void tile_lag_energy_dt_impl(const StepArgs<R>& a, in
     // The FP64 form (at 64 registers without that, which loses more
     // occupancy than it gains) streams them through a per-thread ring of
     // asynchronous copies instead when kRing (the fused kernel), kEAhead rows
-    // ahead.  The FP64 pressure is read only where a cell is compressed.
+    // ahead (seven planes: three rows ahead, 30 KB of shared memory per CTA,
+    // cost more in the overlap between kernels than it hid).  The FP64
+    // pressure is read only where a cell is compressed.
     constexpr bool kAhead = Pr::kMixed;
     constexpr bool kERing = kRing && !Pr::kMixed;
     constexpr int kEAhead = 2, kESlots = kEAhead + 1;
