@@ -5,21 +5,30 @@ Workload (one "step" = one timestep, solve_hydro_2d + the conservation totals
 the reference driver computes every iteration, main.c:82-91): a Sedov-type
 blast on a 4096^2 uniform mesh, FP64, gamma 1.4, density 1, specific energy
 1e-5 with a central 4x4-cell square at 1e4, zero velocity, reflective walls,
-the params dt set to the CFL estimate of the initial state.  Synthetic data.
-The state (17 arrays of 4100^2 doubles, 2.3 GB) is larger than L2, so no L2
-flush is needed between steps.
+the params dt set to the CFL estimate of the initial state, 500 iterations.
+Synthetic data.  The state (15 arrays of 4100^2 doubles, 2 GB) is larger than
+L2, so no L2 flush is needed between steps.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
-Prints one JSON line on rank 0.  With --impl reference the same workload runs
-on the host cores through the CPU oracle (a C restatement of the reference
-omp3 kernel set, bit-exact with it), since the reference has no GPU path that
-builds here.  Under torchrun (N > 1) every rank advances its own independent
-replica (the single-mesh timestep does not shard without a halo exchange).
+Prints one JSON line on rank 0.  Besides the timed FP64 line it reports:
+  parity        per-field maxima of the fused step against the oracle (the C
+                restatement of the reference omp3 set, strict IEEE) after the
+                workload's full 500 steps;
+  forms         the mixed-precision form (blast, 8192^2 Sod, a field in
+                motion everywhere) and the batched forms at their stated
+                lengths (200 and 1000 steps), with their errors;
+  cpu_baseline  the oracle built with the reference's flags on the host cores.
+With --impl reference the same workload runs on the host cores through the
+oracle, which the tests hold bit-identical to the reference's own omp3 code
+(the reference has no GPU path that builds on this machine).  Under torchrun
+(N > 1) every rank advances its own replica (replicas only; the single-mesh
+step is not decomposed across GPUs here).
 """
 from __future__ import annotations
 
 import argparse
+import hashlib
 import json
 import os
 import statistics
@@ -33,17 +42,21 @@ sys.path.insert(0, ROOT)
 METRIC = "cell-steps/s, % HBM peak: FP64 vs mixed/batched at stated L1 err"
 UNIT = "cell-steps/s"
 N_CELLS_SIDE = 4096
-B_ALG_FP64 = 64  # bytes/cell-step: rho, e, rho_u, rho_v read + written once
+CONFIG_STEPS = 500   # the blast workload's stated length
+B_ALG_FP64 = 64      # bytes/cell-step: rho, e, rho_u, rho_v read + written once
+B_ALG_MIXED = 48     # rho, e (FP64) and rho_u, rho_v (FP32), each read + written
 
 # Algorithmic bytes per interior cell of each fused kernel: the arrays it must
 # read and write once (8 bytes each) on every cell.  Arrays that change only
 # where the flow moves (momenta, energy) are counted as read; their writes on
 # moving cells come on top.  Used for the per-kernel HBM roofline.
 KERNEL_BYTES_PER_CELL = {
-    "lag_pressure": 8 * 8,       # rho, e, rho_u, rho_v in; P, rho_old, u, v out
+    "lag_pressure": 8 * 7,       # rho, e, rho_u, rho_v in; P, u, v out
     "lag_viscosity": 8 * 5,      # u, v, rho in; Qxx, Qyy out
     "lag_viscous_accel": 8 * 2,  # Qxx, Qyy in (momenta, densities, velocities where a stress gradient acts)
     "lag_energy_dt": 8 * 6,      # rho, e, Qxx, Qyy, u, v in (P in, e out where the cell is compressed)
+    "lag_fused": 8 * 6,          # one-kernel Lagrangian phase: rho, e, rho_u, rho_v in; u, v out
+    "lag_apply": 0,              # changed values only
     "mass_sweep_x": 8 * 6,       # rho, e, u in; rho, e, F_x out
     "mass_sweep_y": 8 * 6,
     # Momentum pairs (flux fused with its update), one launch per step each;
@@ -56,40 +69,33 @@ KERNEL_BYTES_PER_CELL = {
     "mesh_pow2": 0,              # the step's one-block mesh test (spacings only)
 }
 
-# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per interior cell of
-# one launch, from an ncu capture (one pass) of the FP64 fused kernels on the
-# Sedov blast at the benchmark size, 4096^2, after five timesteps; scaled to a
-# launch by its cell count.
-NCU_TRAFFIC_BYTES_PER_CELL = {
-    "lag_pressure": 62.2,
-    "lag_viscosity": 38.7,
-    "lag_viscous_accel": 16.0,
-    "lag_energy_dt": 48.2,
-    "mass_sweep_x": 53.0,
-    "mass_sweep_y": 45.4,
-    "mom_uFx": 30.6,             # the launch that recomputes u
-    "mom_uFy": 16.0,
-    "mom_vFx": 39.1,             # the launch that recomputes v
-    "mom_vFy": 16.0,
-}
+# ncu figures (DRAM bytes per cell of each kernel on the blast workload, FP64
+# instructions per cell-step on a field in motion) with the fingerprint of the
+# kernel sources they were measured on; used only while the sources match.
+PROFILE_FIGURES = os.path.join(ROOT, "profiles", "ncu_figures_fused_fp64.json")
 
 
 def parse_args():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=500)
+    p.add_argument("--steps", type=int, default=CONFIG_STEPS)
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--size", type=int, default=N_CELLS_SIDE)
     p.add_argument("--workload", default="sedov", choices=["sedov", "smooth"],
                    help="the FP64 line's problem: the blast (default) or a field in "
                         "motion everywhere")
-    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-cpu-baseline", action="store_true",
+                   help="skip the host-core legs (CPU baseline and oracle checks)")
     p.add_argument("--fp64-only", action="store_true", help="skip the mixed/batched forms")
     p.add_argument("--sod-size", type=int, default=8192,
                    help="side of the Sod tube of the mixed form (0 skips it)")
-    p.add_argument("--batch-steps", type=int, default=20,
-                   help="timed steps of each batched form (a sample of its 200/1000)")
+    p.add_argument("--parity-steps", type=int, default=CONFIG_STEPS,
+                   help="steps of the per-cell oracle comparison (0 skips it)")
+    p.add_argument("--batch-fp64-steps", type=int, default=200,
+                   help="timed steps of the batched FP64 ensemble (its stated length)")
+    p.add_argument("--batch-mixed-steps", type=int, default=1000,
+                   help="timed steps of the batched mixed ensemble (its stated length)")
     return p.parse_args()
 
 
@@ -106,6 +112,27 @@ def measured_peaks():
         return float(d["hbm_gbs"]), "measured"
     except (OSError, KeyError, ValueError):
         return 6800.0, "fallback"
+
+
+def source_fingerprint() -> str:
+    """sha256 (16 hex digits) of the kernel sources, in name order."""
+    h = hashlib.sha256()
+    csrc = os.path.join(ROOT, "flow_gb300", "csrc")
+    for name in sorted(os.listdir(csrc)):
+        if name.endswith((".cu", ".cuh", ".h")):
+            with open(os.path.join(csrc, name), "rb") as f:
+                h.update(name.encode() + b"\0" + f.read())
+    return h.hexdigest()[:16]
+
+
+def profile_figures():
+    """The committed ncu figures when they were measured on these sources."""
+    try:
+        with open(PROFILE_FIGURES) as f:
+            d = json.load(f)
+    except (OSError, ValueError):
+        return None
+    return d if d.get("source_fingerprint") == source_fingerprint() else None
 
 
 class ClockSampler:
@@ -161,7 +188,9 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------------------
-# CPU side: the oracle (C restatement of the reference omp3 set).
+# Host-core leg: the oracle (C restatement of the reference omp3 set) as the
+# timed CPU baseline and as the checker of the GPU results.  Nothing here is
+# on the GPU path.
 
 def _omp_env():
     ncpu = os.cpu_count() or 1
@@ -180,9 +209,23 @@ def main_problem(problems, workload: str, n: int):
     return problems.sedov(n)
 
 
+def oracle_start(prob):
+    """Host mesh and state of a problem, after the driver's initial
+    set_timestep (main.c:64-66)."""
+    from oracle import oracle as O
+    hm = O.HostMesh(prob.gnx, prob.gny, width=prob.width, height=prob.height,
+                    dt=prob.dt_param)
+    st = O.HostState(hm)
+    O.fill_fields(hm, st, prob.interior(prob.rho), prob.interior(prob.e))
+    O.initial_timestep(hm, st)
+    return hm, st
+
+
 def cpu_run(n: int, steps: int, warmup: int, budget_s: float, workload: str = "sedov"):
-    """Times the oracle on the same workload; returns (cell-steps/s, steps
-    timed, threads).  Times at most ~budget_s seconds of steps."""
+    """Times the oracle, built with the reference's flags (-O3 -march=native
+    -fopenmp, Makefile:15), on the same workload; returns (cell-steps/s,
+    steps timed, threads).  Times all `steps` steps unless that would take
+    more than about budget_s seconds."""
     threads = _omp_env()
     from flow_gb300 import problems
     from oracle import oracle as O
@@ -214,14 +257,47 @@ def cpu_run(n: int, steps: int, warmup: int, budget_s: float, workload: str = "s
     return n * n * timed / el, timed, threads
 
 
+def oracle_compare(fields: dict, prob, steps: int, dt_pair=None):
+    """Advances the oracle (strict IEEE build) `steps` steps from the problem's
+    initial state and compares the given GPU fields (interior arrays by name)
+    per cell: the largest |a-b| / max(|b|, 1e-3 max|b|) (the tests'
+    tolerance measure), the L1 error sum|a-b| / sum|b| and the count of cells
+    that differ at all."""
+    import numpy as np
+    from oracle import oracle as O
+    _omp_env()
+    hm, st = oracle_start(prob)
+    O.run(hm, st, steps)
+    out = {}
+    for k, got in fields.items():
+        want = st.interior(k)
+        got = np.asarray(got, dtype=np.float64)
+        scale = float(np.abs(want).max()) if want.size else 0.0
+        d = np.abs(got - want)
+        if scale == 0.0:
+            out[k] = {"max_abs": float(d.max()), "cells_differing": int(np.count_nonzero(d))}
+            continue
+        rel = d / np.maximum(np.abs(want), 1e-3 * scale)
+        out[k] = {"max_cell_rel": float(rel.max()),
+                  "l1": float(d.sum() / np.abs(want).sum()),
+                  "linf": float(d.max() / scale),
+                  "cells_differing": int(np.count_nonzero(got != want))}
+    if dt_pair is not None:
+        out["dt"] = {"rel": abs(dt_pair[0] - hm.mesh.dt) / hm.mesh.dt,
+                     "dt_h_rel": abs(dt_pair[1] - hm.mesh.dt_h) / hm.mesh.dt_h}
+    return out
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return
     value, timed, threads = cpu_run(args.size, args.steps, args.warmup, budget_s=150.0,
                                     workload=args.workload)
-    sample = (f"{args.workload} {args.size}^2 FP64 timesteps on {threads} host threads: "
-              f"{timed} of {args.steps} requested steps timed after {args.warmup} warm-up")
+    sample = (f"{args.workload} {args.size}^2 FP64 timesteps + conservation totals on "
+              f"{threads} host threads (the oracle, -O3 -march=native -fopenmp as the "
+              f"reference's Makefile:15): {timed} of {args.steps} requested steps timed "
+              f"after {args.warmup} warm-up")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
@@ -238,9 +314,6 @@ def run_reference(args):
 
 # ---------------------------------------------------------------------------
 # GPU side.
-
-B_ALG_MIXED = 48  # rho, e (FP64) and rho_u, rho_v (FP32), each read + written
-
 
 def field_errors(fg, got, want, names=("rho", "e")):
     """L1 (sum|d| / sum|want|) and L-infinity (max|d| / max|want|) per field."""
@@ -259,9 +332,9 @@ def field_errors(fg, got, want, names=("rho", "e")):
 
 
 def batch_problems(problems, kind: str):
-    """Config 3 (kind "two_region"): 256 two-region instances with sides drawn
-    from {128, 192, ..., 1024}; config 4 (kind "smooth"): 64 instances of
-    2048^2 smooth random fields.  Seeded."""
+    """The batched FP64 ensemble (kind "two_region"): 256 two-region instances
+    with sides drawn from {128, 192, ..., 1024}; the batched mixed ensemble
+    (kind "smooth"): 64 instances of 2048^2 smooth random fields.  Seeded."""
     import numpy as np
     if kind == "two_region":
         rng = np.random.default_rng(20261203)
@@ -271,9 +344,11 @@ def batch_problems(problems, kind: str):
     return [problems.smooth_random(2048, rng) for _ in range(64)]
 
 
-def run_batched_form(fg, problems, torch, device, kind, precision, steps, warmup):
-    """Times one batched ensemble (autotuned, graph-replayed) and measures its
-    error on two sampled instances against the single-problem FP64 step."""
+def run_batched_form(fg, problems, torch, device, kind, precision, steps, warmup, oracle_samples):
+    """Times one batched ensemble (autotuned, graph-replayed) for `steps`
+    steps and measures its error on sampled instances at the final step
+    against the single-problem FP64 step on the GPU and, for the first
+    `oracle_samples` of them, against the oracle on the host cores."""
     import numpy as np
     from flow_gb300.replicas import max_over_ranks, shard_instances, sum_over_ranks
     rank, world, _ = dist_env()
@@ -298,31 +373,37 @@ def run_batched_form(fg, problems, torch, device, kind, precision, steps, warmup
     value = cells * steps / (ms * 1e-3)
     total_steps = b.steps_done
     samples = [0, len(probs) // 2]
-    errs = {}
+    errs, finals = {}, {}
     for i in samples:
         rho, e, dt, _ = b.state(i)
         ref = fg.DeviceSim(probs[i], device)
         ref.initial_timestep()
         ref.run(total_steps)
         rr, er = ref.interior("rho"), ref.interior("e")
-        errs[f"instance_{i}_{probs[i].gnx}x{probs[i].gny}"] = {
-            "rho_l1": float(np.abs(rho - rr).sum() / np.abs(rr).sum()),
-            "e_l1": float(np.abs(e - er).sum() / np.abs(er).sum()),
-            "rho_linf": float(np.abs(rho - rr).max() / np.abs(rr).max()),
-            "max_abs_diff": float(max(np.abs(rho - rr).max(), np.abs(e - er).max()))}
+        name = f"instance_{i}_{probs[i].gnx}x{probs[i].gny}"
+        errs[name] = {
+            "vs_fp64_gpu": {
+                "rho_l1": float(np.abs(rho - rr).sum() / np.abs(rr).sum()),
+                "e_l1": float(np.abs(e - er).sum() / np.abs(er).sum()),
+                "rho_linf": float(np.abs(rho - rr).max() / np.abs(rr).max()),
+                "max_abs_diff": float(max(np.abs(rho - rr).max(), np.abs(e - er).max()))}}
+        finals[name] = (probs[i], {"rho": rho, "e": e})
         del ref
     del b
     torch.cuda.empty_cache()
     seq = run_sequential_ensemble(fg, torch, device, probs, precision, warmup=1, steps=2)
     b_alg = B_ALG_FP64 if precision == 0 else B_ALG_MIXED
-    return {"workload": f"batch_{kind}_{'fp64' if precision == 0 else 'mixed'}",
-            "instances": len(probs), "cells": cells, "value": value, "unit": UNIT,
-            "ms_per_step": ms / steps, "steps_timed": steps, "steps_total": total_steps,
-            "graph": True, "tuning": tune,
-            "hbm_fraction_of_step": value * b_alg / (measured_peaks()[0] * 1e9),
-            "errors_vs_fp64_single_problem": errs,
-            "sequential_same_ensemble": seq,
-            "speedup_vs_sequential": value / seq["value"]}
+    out = {"workload": f"batch_{kind}_{'fp64' if precision == 0 else 'mixed'}",
+           "instances": len(probs), "cells": cells, "value": value, "unit": UNIT,
+           "ms_per_step": ms / steps, "steps_timed": steps, "steps_total": total_steps,
+           "graph": True, "tuning": tune,
+           "hbm_fraction_of_step": value * b_alg / (measured_peaks()[0] * 1e9),
+           "errors": errs,
+           "sequential_same_ensemble": seq,
+           "speedup_vs_sequential": value / seq["value"]}
+    # The first sampled instances against the oracle (host cores).
+    oracle_todo = list(finals.items())[:oracle_samples]
+    return out, total_steps, oracle_todo
 
 
 def run_sequential_ensemble(fg, torch, device, probs, precision, warmup, steps):
@@ -352,51 +433,85 @@ def run_sequential_ensemble(fg, torch, device, probs, precision, warmup, steps):
             "what": "per-instance single-problem steps, host-timed (each step reads dt back)"}
 
 
-def run_fp64_smooth(fg, problems, torch, device, n, steps, warmup):
+def timed_run(torch, sim, steps, warmup):
+    for _ in range(warmup):
+        sim.step()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        sim.step()
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1)
+
+
+def smooth_problem(problems, n):
+    import numpy as np
+    return problems.smooth_random(n, np.random.default_rng(20261205))
+
+
+def run_fp64_smooth(fg, problems, torch, device, n, steps, warmup, figures, fma_rate):
     """The FP64 step on a field with structure everywhere (density and energy
     1 + a 16-mode smooth random field, seed 20261205): no flat regions, so
     every slope and limiter is live -- the general-case rate next to the
-    blast problem, most of whose mesh is still at rest."""
-    import numpy as np
-    sim = fg.DeviceSim(problems.smooth_random(n, np.random.default_rng(20261205)), device)
+    blast problem, most of whose mesh is still at rest.  Bound by the FP64
+    pipe: its fraction is the FP64 instructions per cell-step (ncu) times the
+    cell-steps/s over the measured FP64 issue rate."""
+    sim = fg.DeviceSim(smooth_problem(problems, n), device)
     sim.initial_timestep()
-    for _ in range(warmup):
-        sim.step()
-    torch.cuda.synchronize()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    e0.record()
-    for _ in range(steps):
-        sim.step()
-    e1.record()
-    torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1)
+    ms = timed_run(torch, sim, steps, warmup)
     del sim
     torch.cuda.empty_cache()
-    return {"workload": f"smooth_{n}_fp64", "value": n * n * steps / (ms * 1e-3), "unit": UNIT,
-            "ms_per_step": ms / steps, "steps": steps, "warmup": warmup}
-
-
-def run_mixed_form(fg, problems, torch, device, n, steps, warmup, ref_state=None, workload="sedov"):
-    """Times the mixed form on the same workload; returns its result dict and
-    the final simulation object."""
-    prob = problems.sedov(n) if workload == "sedov" else problems.sod(n)
-    sim = fg.MixedSim(prob, device)
-    for _ in range(warmup):
-        sim.step()
-    torch.cuda.synchronize()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    e0.record()
-    for _ in range(steps):
-        sim.step()
-    e1.record()
-    torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1)
     value = n * n * steps / (ms * 1e-3)
-    return {"workload": f"{workload}_{n}_mixed", "value": value, "unit": UNIT,
-            "ms_per_step": ms / steps, "steps": steps, "warmup": warmup,
-            "hbm_fraction_of_step_48B": value * B_ALG_MIXED / (measured_peaks()[0] * 1e9)}, sim
+    out = {"workload": f"smooth_{n}_fp64", "value": value, "unit": UNIT,
+           "ms_per_step": ms / steps, "steps": steps, "warmup": warmup,
+           "hbm_fraction_of_step": value * B_ALG_FP64 / (measured_peaks()[0] * 1e9)}
+    per_cell = (figures or {}).get("fp64_inst_per_cell_step_moving")
+    if per_cell and fma_rate > 0:
+        out["fp64_pipe"] = {"fp64_inst_per_cell_step": per_cell,
+                            "fraction_of_measured_fp64_rate": per_cell * value / fma_rate}
+    return out
+
+
+def mixed_problem(problems, workload, n):
+    if workload == "sedov":
+        return problems.sedov(n)
+    if workload == "sod":
+        return problems.sod(n)
+    return smooth_problem(problems, n)
+
+
+def run_mixed_form(fg, problems, torch, device, workload, n, steps, warmup):
+    """Times the mixed form on a workload and measures it against the FP64
+    path after the same steps from the same initial state (the FP64 path is
+    held to the oracle per cell): L1/Linf per field and the mass/energy
+    drift.  Also times the FP64 path on that workload for the speed-up."""
+    sim = fg.MixedSim(mixed_problem(problems, workload, n), device)
+    ms = timed_run(torch, sim, steps, warmup)
+    value = n * n * steps / (ms * 1e-3)
+    ref = fg.DeviceSim(mixed_problem(problems, workload, n), device)
+    ref.initial_timestep()
+    ms_ref = timed_run(torch, ref, steps, warmup)
+    fp64_value = n * n * steps / (ms_ref * 1e-3)
+    out = {"workload": f"{workload}_{n}_mixed", "value": value, "unit": UNIT,
+           "ms_per_step": ms / steps, "steps": steps, "warmup": warmup,
+           "hbm_fraction_of_step_48B": value * B_ALG_MIXED / (measured_peaks()[0] * 1e9),
+           "errors_vs_fp64": field_errors(fg, sim, ref,
+                                          names=("rho", "e", "u", "v", "rho_u", "rho_v"))}
+    cm, cr = sim.conservation(), ref.conservation()
+    out["mass_drift"] = abs(cm[0] - cr[0]) / cr[0]
+    out["energy_drift"] = abs(cm[1] - cr[1]) / cr[1]
+    out["fp64_value_same_workload"] = fp64_value
+    out["speedup_vs_fp64"] = value / fp64_value
+    del sim, ref
+    torch.cuda.empty_cache()
+    return out
+
+
+STATE = ("rho", "e", "u", "v", "rho_u", "rho_v")
+
 
 def run_gpu(args):
     rank, world, local = dist_env()
@@ -415,6 +530,7 @@ def run_gpu(args):
     fg.set_stream(torch.cuda.current_stream())
     fg.set_mode(fg.MODE_FUSED)
     n = args.size
+    figures = profile_figures()
 
     from flow_gb300.replicas import barrier, job_throughput, max_over_ranks
 
@@ -424,6 +540,7 @@ def run_gpu(args):
     out2 = (fg.ctypes.c_double * 2)()
     out2p = fg.ctypes.cast(out2, fg.ctypes.POINTER(fg.ctypes.c_double))
     nx, ny = sim.nx, sim.ny
+
     def step():
         sim.step()
         # The pointers of the totals' arrays, formed once per sim (kept on it).
@@ -448,11 +565,13 @@ def run_gpu(args):
     with ClockSampler(local) as clk:
         barrier()
         torch.cuda.synchronize()
+        launches0 = L.gb300_launch_count()
         e0.record()
         for _ in range(args.steps):
             step()
         e1.record()
         torch.cuda.synchronize()
+        launches = L.gb300_launch_count() - launches0
         barrier()
     # The job's time is its slowest replica's.
     ms = max_over_ranks(e0.elapsed_time(e1), device)
@@ -478,11 +597,11 @@ def run_gpu(args):
 
     kernels = []
     buf = fg.ctypes.create_string_buffer(64)
-    launches = fg.ctypes.c_longlong()
+    nlaunch = fg.ctypes.c_longlong()
     tot = fg.ctypes.c_double()
     for i in range(L.gb300_profile_count()):
-        L.gb300_profile_entry(i, buf, 64, fg.ctypes.byref(launches), fg.ctypes.byref(tot))
-        kernels.append((buf.value.decode(), launches.value, tot.value))
+        L.gb300_profile_entry(i, buf, 64, fg.ctypes.byref(nlaunch), fg.ctypes.byref(tot))
+        kernels.append((buf.value.decode(), nlaunch.value, tot.value))
     kernels.sort(key=lambda k: -k[2])
 
     # ---- end to end through the C ABI with host buffers ----
@@ -510,71 +629,88 @@ def run_gpu(args):
     h2d = sum(host_in[f].numel() * 8 for f in fields)
     d2h = sum(host_out[f].numel() * 8 for f in fields)
     e2e_value = job_throughput(n * n * args.steps, world, e2e_s)
-    del host_in, host_out
+    del host_in, host_out, sim, sim2
+    torch.cuda.empty_cache()
 
-    # ---- the mixed-precision form on the same workload ----
-    forms = {}
-    if not args.fp64_only:
-        del sim, sim2
+    # ---- parity of the timed path on the full workload (rank 0) ----
+    parity = None
+    host_legs = rank == 0 and not args.no_cpu_baseline
+    if host_legs and args.parity_steps > 0:
+        psim = fg.DeviceSim(main_problem(problems, args.workload, n), device)
+        psim.initial_timestep()
+        psim.run(args.parity_steps)
+        got = {k: psim.interior(k) for k in STATE}
+        pair = (psim.mesh.dt, psim.mesh.dt_h)
+        del psim
         torch.cuda.empty_cache()
+        parity = {"steps": args.parity_steps,
+                  "against": "oracle: C restatement of the reference omp3 set, strict IEEE "
+                             "(bit-identical to the reference compiled from its sources)",
+                  "measure": "max_cell_rel = max |a-b| / max(|b|, 1e-3 max|b|)",
+                  "tolerance": 1e-12,
+                  "fields": oracle_compare(got, main_problem(problems, args.workload, n),
+                                           args.parity_steps, pair)}
+        parity["within_tolerance"] = all(
+            v.get("max_cell_rel", 0.0) <= 1e-12 for k, v in parity["fields"].items() if k != "dt")
+
+    fma_rate = fg.ctypes.c_double()
+    L.gb300_measure_fp64_fma_rate(fg.ctypes.byref(fma_rate))
+
+    # ---- the mixed-precision and batched forms ----
+    forms = {}
+    oracle_checks = []
+    if not args.fp64_only:
         if args.workload != "smooth":
             forms["fp64_smooth"] = run_fp64_smooth(fg, problems, torch, device, n,
-                                                   min(args.steps, 100), args.warmup)
-        # The mixed form on the FP64 workload, then on the 8192^2 Sod tube.
-        for workload, size in (("sedov", n), ("sod", args.sod_size)):
+                                                   min(args.steps, 100), args.warmup, figures,
+                                                   fma_rate.value)
+        for workload, size in (("sedov", n), ("sod", args.sod_size), ("smooth", n)):
             if size <= 0:
                 continue
-            mixed, msim = run_mixed_form(fg, problems, torch, device, size, args.steps,
-                                         args.warmup, workload=workload)
-            # Error against the FP64 path after the same number of steps from
-            # the same initial state (the FP64 path itself matches the CPU
-            # oracle to ~1e-13 per cell).
-            prob_ref = problems.sedov(size) if workload == "sedov" else problems.sod(size)
-            ref = fg.DeviceSim(prob_ref, device)
-            ref.initial_timestep()
-            t0 = torch.cuda.Event(enable_timing=True)
-            t1 = torch.cuda.Event(enable_timing=True)
-            t0.record()
-            ref.run(args.steps + args.warmup)
-            t1.record()
-            torch.cuda.synchronize()
-            fp64_value = size * size * (args.steps + args.warmup) / (t0.elapsed_time(t1) * 1e-3)
-            mixed["errors_vs_fp64"] = field_errors(fg, msim, ref,
-                                                   names=("rho", "e", "u", "v", "rho_u", "rho_v"))
-            cm, cr = msim.conservation(), ref.conservation()
-            mixed["mass_drift"] = abs(cm[0] - cr[0]) / cr[0]
-            mixed["energy_drift"] = abs(cm[1] - cr[1]) / cr[1]
-            mixed["fp64_value_same_workload"] = fp64_value
-            mixed["speedup_vs_fp64"] = mixed["value"] / fp64_value
-            forms["mixed" if workload == "sedov" else f"mixed_sod_{size}"] = mixed
-            del msim, ref
-            torch.cuda.empty_cache()
-        bsteps = min(args.steps, args.batch_steps)
-        forms["batched_fp64"] = run_batched_form(fg, problems, torch, device, "two_region", 0,
-                                                 bsteps, args.warmup)
-        forms["batched_mixed"] = run_batched_form(fg, problems, torch, device, "smooth", 1,
-                                                  bsteps, args.warmup)
+            name = {"sedov": "mixed", "sod": f"mixed_sod_{size}", "smooth": "mixed_smooth"}[workload]
+            forms[name] = run_mixed_form(fg, problems, torch, device, workload, size,
+                                         args.steps if workload != "smooth" else min(args.steps, 100),
+                                         args.warmup)
+        for key, kind, prec, steps, nsamp in (
+                ("batched_fp64", "two_region", 0, args.batch_fp64_steps, 2),
+                ("batched_mixed", "smooth", 1, args.batch_mixed_steps, 1)):
+            if steps <= 0:
+                continue
+            res, total, todo = run_batched_form(fg, problems, torch, device, kind, prec, steps,
+                                                args.warmup, nsamp)
+            forms[key] = res
+            oracle_checks += [(key, name, p, f, total) for name, (p, f) in todo]
 
     if rank != 0:
         return
 
-    # ---- roofline of the dominant kernel and of the FP64 pipe ----
+    # Batched instances against the oracle at their final step (host cores).
+    if host_legs:
+        for key, name, p, f, total in oracle_checks:
+            res = oracle_compare(f, p, total)
+            forms[key]["errors"][name]["vs_oracle"] = {
+                k: {m: v[m] for m in ("l1", "linf", "max_cell_rel") if m in v}
+                for k, v in res.items()}
+
+    # ---- roofline of the dominant kernel and of the whole step ----
     peak, peak_kind = measured_peaks()
     name, nl, total = kernels[0] if kernels else ("none", 1, float("nan"))
     cells = (nx - 4) * (ny - 4)
     bytes_launch = KERNEL_BYTES_PER_CELL.get(name, B_ALG_FP64) * cells
     achieved = bytes_launch / (total / nl * 1e-3) / 1e9
-    tb = NCU_TRAFFIC_BYTES_PER_CELL.get(name)
+    tb = ((figures or {}).get("dram_bytes_per_cell") or {}).get(name)
     traffic = tb * cells if tb is not None else None
-    fma_rate = fg.ctypes.c_double()
-    L.gb300_measure_fp64_fma_rate(fg.ctypes.byref(fma_rate))
+    step_gbs = value / world * B_ALG_FP64 / 1e9
 
     cpu = None
-    if not args.no_cpu_baseline:
-        cv, timed, threads = cpu_run(n, 64, 1, budget_s=20.0, workload=args.workload)
+    if host_legs:
+        cv, timed, threads = cpu_run(n, args.steps, 1, budget_s=60.0, workload=args.workload)
         cpu = {"value": cv, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": f"{args.workload} {n}^2 FP64, {timed} timesteps on {threads} host threads "
-                         "(C restatement of the reference omp3 set, OpenMP)"}
+               "sample": f"{args.workload} {n}^2 FP64 timesteps + conservation totals, {timed} "
+                         f"of the GPU arm's {args.steps} steps, on {threads} host threads (the "
+                         "oracle, a C restatement of the reference omp3 set that the tests hold "
+                         "bit-identical to it, built -O3 -march=native -fopenmp as the "
+                         "reference's Makefile:15)"}
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
@@ -582,7 +718,7 @@ def run_gpu(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic",
         "config": {"workload": f"{args.workload}_{n}_fp64", "nx": n, "ny": n, "form": "fp64",
-                   "iterations_timed": args.steps, "l2": "inputs larger than L2 (2.3 GB state)",
+                   "iterations_timed": args.steps, "l2": "inputs larger than L2 (2 GB state)",
                    "parallelism": "replicas" if world > 1 else "single GPU",
                    "hbm_fraction_of_step": value / world * B_ALG_FP64 / (peak * 1e9)},
         "e2e": {"value": e2e_value, "unit": UNIT,
@@ -591,9 +727,15 @@ def run_gpu(args):
                         "through the C ABI, final state D2H"},
         "roofline": {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
-                     "peak_kind": peak_kind},
+                     "peak_kind": peak_kind,
+                     "step": {"what": "cell-steps/s x 64 B (rho, e, rho_u, rho_v read and "
+                                      "written once per step) over the measured copy bandwidth",
+                              "achieved": step_gbs, "frac": step_gbs / peak,
+                              "dram_bytes_per_cell_step": (figures or {}).get(
+                                  "dram_bytes_per_cell_step")}},
         "fp64_pipe": {"fma_per_s_peak": fma_rate.value,
-                      "note": "FP64 issue rate measured on this GPU; the FP64 timestep is bound here"},
+                      "note": "FP64 issue rate measured on this GPU; bounds the FP64 step on "
+                              "fields in motion (forms.fp64_smooth.fp64_pipe)"},
         # Per kernel: launches, total ms, share of the step, and its achieved
         # GB/s on its algorithmic bytes (KERNEL_BYTES_PER_CELL) with the
         # fraction of the measured HBM copy bandwidth.
@@ -602,11 +744,13 @@ def run_gpu(args):
                      "alg_frac": KERNEL_BYTES_PER_CELL.get(k, B_ALG_FP64) * cells
                                  / (t / c * 1e-3) / 1e9 / peak}
                     for k, c, t in kernels],
+        "parity": parity,
         "forms": forms,
         "cpu_baseline": cpu,
         "clocks": clk.summary(),
-        "gpu_launches": 12 * args.steps,  # mesh test + 10 timestep kernels + the conservation totals
+        "gpu_launches": launches,
         "mass": mass, "energy": energy,
+        "kernel_sources": source_fingerprint(),
     }
     print(json.dumps(line), flush=True)
 

@@ -27,6 +27,7 @@ LIB_PATH = os.path.join(_HERE, "libflow_gb300.so")
 GB300_OK = 0
 MODE_EXACT = 0
 MODE_FUSED = 1
+MODE_FUSED_LAG = 2
 
 _dp = ctypes.POINTER(ctypes.c_double)
 
@@ -98,6 +99,7 @@ def _declare(L: ctypes.CDLL) -> None:
         "gb300_last_error": [],
         "gb300_set_stream": [V],
         "gb300_set_mode": [I],
+        "gb300_set_lagrangian_rows": [I],
         "gb300_get_mode": [],
         "gb300_set_verbose": [I],
         "gb300_synchronize": [],
@@ -122,6 +124,7 @@ def _declare(L: ctypes.CDLL) -> None:
     L.gb300_last_error_message.argtypes, L.gb300_last_error_message.restype = [], ctypes.c_char_p
     L.gb300_clear_error.argtypes, L.gb300_clear_error.restype = [], None
     L.gb300_get_stream.argtypes, L.gb300_get_stream.restype = [], ctypes.c_void_p
+    L.gb300_launch_count.argtypes, L.gb300_launch_count.restype = [], ctypes.c_ulonglong
     L.gb300_mixed_workspace_bytes.argtypes = [I, I]
     L.gb300_mixed_workspace_bytes.restype = ctypes.c_size_t
     L.gb300_mixed_workspace_offset.argtypes = [I, I, I]

@@ -303,7 +303,6 @@ InstLayout inst_layout(int nx, int ny, int precision) {
   L.vF_y = take(nf * 8);  // also the FP64 first-sweep energy
   if (precision == 0) {
     L.P = take(nc * 8);
-    L.rho_old = take(nc * 8);
   } else {
     L.rho_r = take(nc * 4);
     L.e_r = take(nc * 4);
@@ -360,7 +359,7 @@ Instance<R> make_instance(const BatchImpl& B, int i) {
     a.rho_r = reinterpret_cast<R*>(a.rho);
     a.e_r = reinterpret_cast<R*>(a.e);
     a.P = D(L.P);
-    a.rho_old = D(L.rho_old);
+    a.rho_old = nullptr;
     I.first = SweepArgs<R>{a.rho, a.e, a.rho_r, a.e_r, D(L.uF_x), D(L.vF_y),
                            Rp(L.uF_x), Rp(L.vF_y)};
     I.second = SweepArgs<R>{D(L.uF_x), D(L.vF_y), Rp(L.uF_x), Rp(L.vF_y), a.rho,

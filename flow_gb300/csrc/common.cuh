@@ -27,6 +27,11 @@ constexpr double kCT = 0.3;
 //   [2] ticket                block-completion counter (uint64 bits)
 //   [3] mass, [4] energy      conservation totals of the last reduction
 //   [5] status                error word of the fused kernels (uint64 bits)
+//   [6] CFL minimum           running minimum of the fused step's CFL
+//                             candidates (uint64 bits of a non-negative
+//                             double: bit order = value order)
+//   [7] mesh power-of-two     1 when every mesh spacing is a power of two
+//                             (formed on the device at the start of a step)
 //   [8 ...]                   per-block partials (2 doubles per block)
 enum : int {
   kRaDt = 0,
@@ -35,6 +40,8 @@ enum : int {
   kRaMass = 3,
   kRaEnergy = 4,
   kRaStatus = 5,
+  kRaMinBits = 6,
+  kRaMeshPow2 = 7,
   kRaPartial = 8,
 };
 constexpr int kMaxReduceBlocks = 1024;

@@ -6,18 +6,13 @@
 #include "../../include/flow_gb300.h"
 #include "fused.h"
 #include "fused_tiles.cuh"
+#include "lag_fused.cuh"
 #include "profile.h"
 
 namespace flow {
 namespace {
 
 using namespace tiles;
-
-// reduce_array slot holding the running CFL minimum of the fused step (uint64
-// bits; all candidates are non-negative, so bit order = value order).
-constexpr int kRaMinBits = 6;
-// reduce_array slot holding the whole-mesh power-of-two flag of the step.
-constexpr int kRaMeshPow2 = 7;
 
 // Programmatic dependent launch: every kernel of the step is launched with
 // programmatic stream serialisation, lets the next kernel launch as soon as
@@ -34,11 +29,18 @@ __device__ __forceinline__ void pdl_trigger() {
 // ny) is a positive normal power of two: one block, the first kernel of the
 // step.  The tiles then skip their own spacing tests (block_mesh_pow2).
 constexpr int kPow2Threads = 1024;
+// It also clears the CFL minimum slot and the block ticket for the step's
+// Lagrangian kernels.
 __global__ void __launch_bounds__(kPow2Threads)
     k_mesh_pow2(int nx, int ny, const double* celldx, const double* edgedx,
-                const double* celldy, const double* edgedy, unsigned long long* flag) {
+                const double* celldy, const double* edgedy, unsigned long long* flag,
+                double* ra) {
   pdl_wait();
   pdl_trigger();
+  if (threadIdx.x == 0) {
+    *reinterpret_cast<unsigned long long*>(ra + kRaTicket) = 0ull;
+    *reinterpret_cast<unsigned long long*>(ra + kRaMinBits) = ~0ull;
+  }
   // Every test is made (no short circuit), so that a thread's loads are
   // independent and in flight together.
   bool ok = true;
@@ -127,6 +129,124 @@ __global__ void __launch_bounds__(kCols) k_mom_y(const StepArgs<R> a) {
   tile_mom_y<R, kV, kVel>(a, blockIdx.x, blockIdx.y);
 }
 
+// The whole Lagrangian phase of the FP64 step in one kernel (lag_fused.cuh):
+// pressure, viscosity, viscous acceleration, shock heating and the CFL
+// minimum; the last block to finish (ticket in reduce_array) applies the dt
+// rule.  A tile whose row copies were lost records GB300_ERR_TIMEOUT in the
+// status word and leaves the dt pair unchanged.
+__global__ void __launch_bounds__(lagf::kT, 4) k_lag_fused(const lagf::LagArgs a) {
+  __shared__ lagf::LagSmem sm;
+  __shared__ unsigned long long s_warp[lagf::kWarps];
+  __shared__ bool s_last;
+  pdl_wait();
+  pdl_trigger();
+  lagf::CflBest cfl;
+  const lagf::TileGeom g = lagf::tile_geom(a, blockIdx.x, blockIdx.y);
+  const bool ok = lagf::tile_pow2(a, g)
+                      ? lagf::lag_tile<true>(a, sm, blockIdx.x, blockIdx.y, cfl)
+                      : lagf::lag_tile<false>(a, sm, blockIdx.x, blockIdx.y, cfl);
+  if (!ok) {
+    if (threadIdx.x == 0) {
+      atomicExch(reinterpret_cast<unsigned long long*>(a.ra + kRaStatus),
+                 (unsigned long long)GB300_ERR_TIMEOUT);
+    }
+    return;
+  }
+  unsigned long long best = ~0ull;
+  if (cfl.kbest >= 0) best = (unsigned long long)dbits(cfl.c_best * d_rsqrt(cfl.s_best));
+  best = warp_min_u64(best);
+  if ((threadIdx.x & 31) == 0) s_warp[threadIdx.x >> 5] = best;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long b = s_warp[0];
+    for (int w = 1; w < lagf::kWarps; ++w) b = (s_warp[w] < b) ? s_warp[w] : b;
+    atomicMin(a.min_slot, b);
+    __threadfence();
+    unsigned long long* ticket = reinterpret_cast<unsigned long long*>(a.ra + kRaTicket);
+    s_last = (atomicAdd(ticket, 1ull) == (unsigned long long)gridDim.x * gridDim.y - 1);
+  }
+  __syncthreads();
+  if (s_last && threadIdx.x == 0) {
+    __threadfence();
+    // The leapfrog dt/dt_h rule of omp3/flow.c:103-105 (finish_dt).
+    const unsigned long long gmin = atomicExch(a.min_slot, ~0ull);
+    const double cflv = d_min_pos(a.max_dt, dfrom((long long)gmin));
+    const double limited = dmin(cflv, __dmul_rn(FLOW_C_M, a.dt_h));
+    const double dt = __dmul_rn(0.5, __dadd_rn(__dmul_rn(kCT, limited), a.dt_h));
+    a.dt_slot[0] = dt;
+    a.dt_slot[1] = a.first_step ? dt : __dmul_rn(kCT, limited);
+    *reinterpret_cast<unsigned long long*>(a.ra + kRaTicket) = 0ull;
+  }
+}
+
+// Copies the changed energies (with their ghost images) and momenta of the
+// fused Lagrangian kernel into the state arrays.  Each thread reads the three
+// change masks of one (mask row, tile) pair -- 48 contiguous bytes, so the
+// scan is one coalesced pass over the masks -- and the warp then copies the
+// flagged values of each non-empty pair together, one lane per column.
+constexpr int kApplyThreads = 256;
+__global__ void __launch_bounds__(kApplyThreads)
+    k_lag_apply(const lagf::LagArgs a, double* e, double* rho_u, double* rho_v) {
+  pdl_wait();
+  pdl_trigger();
+  const int nx = a.nx, ny = a.ny, pad = a.pad;
+  const int lane = threadIdx.x & 31;
+  const int pairs = (ny + 1) * a.ntx;
+  const int stride = gridDim.x * blockDim.x;
+  for (int base = blockIdx.x * blockDim.x; base < pairs; base += stride) {
+    const int k = base + (int)threadIdx.x;
+    uint4 m[lagf::kMaskFields] = {};
+    bool any = false;
+    if (k < pairs) {
+      const int row = k / a.ntx;
+      // Mask rows the tiles write: cells and x faces pad .. ny-pad-1, y faces
+      // pad .. ny-pad.
+      if (row >= pad && row <= ny - pad) {
+        const uint4* mk = reinterpret_cast<const uint4*>(a.masks) + (size_t)k * lagf::kMaskFields;
+#pragma unroll
+        for (int f = 0; f < lagf::kMaskFields; ++f) {
+          if (f != lagf::kMaskRhoV && row == ny - pad) continue;
+          m[f] = mk[f];
+          any |= (m[f].x | m[f].y | m[f].z | m[f].w) != 0u;
+        }
+      }
+    }
+    unsigned todo = __ballot_sync(0xffffffffu, any);
+    while (todo) {
+      const int src = __ffs(todo) - 1;
+      todo &= todo - 1;
+      const int kk = __shfl_sync(0xffffffffu, k, src);
+      const int row = kk / a.ntx;
+      const int c0 = pad + (kk - row * a.ntx) * lagf::kW - lagf::kHalo;
+#pragma unroll
+      for (int f = 0; f < lagf::kMaskFields; ++f) {
+        const unsigned w0 = __shfl_sync(0xffffffffu, m[f].x, src);
+        const unsigned w1 = __shfl_sync(0xffffffffu, m[f].y, src);
+        const unsigned w2 = __shfl_sync(0xffffffffu, m[f].z, src);
+        const unsigned w3 = __shfl_sync(0xffffffffu, m[f].w, src);
+        const unsigned words[lagf::kWarps] = {w0, w1, w2, w3};
+#pragma unroll
+        for (int w = 0; w < lagf::kWarps; ++w) {
+          if (!((words[w] >> lane) & 1u)) continue;
+          const int col = c0 + 32 * w + lane;
+          if (f == lagf::kMaskE) {
+            const size_t ci = cidx(nx, row, col);
+            const double val = a.e_new[ci];
+            e[ci] = val;
+            mirror(true, e, nx, ny, pad, row, col, val, false, false);
+          } else if (f == lagf::kMaskRhoU) {
+            const size_t fi = fidx(nx, row, col);
+            rho_u[fi] = a.rho_u_new[fi];
+          } else {
+            const size_t ci = cidx(nx, row, col);
+            rho_v[ci] = a.rho_v_new[ci];
+          }
+        }
+      }
+    }
+  }
+}
+
 // Launches kernel k with programmatic stream serialisation (see pdl_wait).
 template <typename... KArgs, typename... Args>
 void launch_pdl_block(void (*k)(KArgs...), dim3 grid, dim3 block, cudaStream_t s,
@@ -142,6 +262,7 @@ void launch_pdl_block(void (*k)(KArgs...), dim3 grid, dim3 block, cudaStream_t s
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   cudaLaunchKernelEx(&cfg, k, args...);
+  count_launches(1);
 }
 template <typename... KArgs, typename... Args>
 void launch_pdl(void (*k)(KArgs...), dim3 grid, cudaStream_t s, Args... args) {
@@ -184,25 +305,47 @@ void launch_mass(cudaStream_t s, const StepArgs<R>& a, bool dir_y, bool first,
   }
 }
 
+// Blocks of k_lag_apply: one thread per (mask row, tile) pair, at most 8
+// blocks per SM (a grid-stride loop covers the rest).
+inline int apply_blocks(const lagf::LagArgs& l) {
+  const int pairs = (l.ny + 1) * l.ntx;
+  const int need = (pairs + kApplyThreads - 1) / kApplyThreads;
+  return need < 8 * num_sms() ? need : 8 * num_sms();
+}
+
 // One timestep of either form; first/second are the two mass sweeps' buffers.
+// lag: the FP64 form's one-kernel Lagrangian phase (k_lag_fused +
+// k_lag_apply), or null for the four separate Lagrangian kernels.
 template <typename R>
 void launch_step(cudaStream_t s, const StepArgs<R>& a, int tt,
                  const SweepArgs<R>& first, const SweepArgs<R>& second,
-                 StepProfiler& prof) {
+                 StepProfiler& prof, const lagf::LagArgs* lag = nullptr) {
   const int nx = a.nx, ny = a.ny, pad = a.pad;
   // The whole-mesh spacing test the tiles read (the mesh may change between
   // calls, so it is formed every step; one block, a few microseconds).
   prof.mark("mesh_pow2");
   launch_pdl_block(k_mesh_pow2, dim3(1), dim3(kPow2Threads), s, nx, ny, a.celldx, a.edgedx,
-                   a.celldy, a.edgedy, const_cast<unsigned long long*>(a.mesh_pow2));
-  prof.mark("lag_pressure");
-  launch_pdl(k_lag_pressure<R>, strip_grid(nx, ny, a.rows), s, a);
-  prof.mark("lag_viscosity");
-  launch_pdl(k_lag_viscosity<R>, strip_grid(nx - 2 * pad, ny - 2 * pad, a.rows), s, a);
-  prof.mark("lag_viscous_accel");
-  launch_pdl(k_lag_viscous_accel<R>, strip_grid(nx + 1 - 2 * pad, ny + 1 - 2 * pad, a.rows), s, a);
-  prof.mark("lag_energy_dt");
-  launch_pdl(k_lag_energy_dt<R>, strip_grid(nx - 2 * pad, ny - 2 * pad, a.rows), s, a);
+                   a.celldy, a.edgedy, const_cast<unsigned long long*>(a.mesh_pow2), a.ra);
+  if (lag) {
+    const int nty = (ny - 2 * pad + lag->rows - 1) / lag->rows;
+    prof.mark("lag_fused");
+    launch_pdl_block(k_lag_fused, dim3((unsigned)lag->ntx, (unsigned)nty), dim3(lagf::kT), s,
+                     *lag);
+    prof.mark("lag_apply");
+    launch_pdl_block(k_lag_apply, dim3((unsigned)apply_blocks(*lag)), dim3(kApplyThreads), s,
+                     *lag, const_cast<double*>(lag->e), const_cast<double*>(lag->rho_u),
+                     const_cast<double*>(lag->rho_v));
+  } else {
+    prof.mark("lag_pressure");
+    launch_pdl(k_lag_pressure<R>, strip_grid(nx, ny, a.rows), s, a);
+    prof.mark("lag_viscosity");
+    launch_pdl(k_lag_viscosity<R>, strip_grid(nx - 2 * pad, ny - 2 * pad, a.rows), s, a);
+    prof.mark("lag_viscous_accel");
+    launch_pdl(k_lag_viscous_accel<R>, strip_grid(nx + 1 - 2 * pad, ny + 1 - 2 * pad, a.rows), s,
+               a);
+    prof.mark("lag_energy_dt");
+    launch_pdl(k_lag_energy_dt<R>, strip_grid(nx - 2 * pad, ny - 2 * pad, a.rows), s, a);
+  }
 
   const bool x_first = (tt % 2 == 0);
   prof.mark(x_first ? "mass_sweep_x" : "mass_sweep_y");
@@ -239,13 +382,22 @@ int finish_step(cudaStream_t s, Mesh* mesh, double* ra, StepProfiler& prof,
     const int st = check_launch(where);
     if (st != GB300_OK) return st;
   }
-  double pair[2];
-  cudaMemcpyAsync(pair, ra + kRaDt, sizeof(pair), cudaMemcpyDeviceToHost, s);
+  // dt, dt_h (slots 0, 1) and the status word (slot 5) in one copy.
+  double head[kRaStatus + 1];
+  cudaMemcpyAsync(head, ra + kRaDt, sizeof(head), cudaMemcpyDeviceToHost, s);
   const cudaError_t err = cudaStreamSynchronize(s);
   if (err != cudaSuccess) {
     return record_error(GB300_ERR_CUDA, "%s: %s", where, cudaGetErrorString(err));
   }
   prof.end();
+  unsigned long long status;
+  memcpy(&status, &head[kRaStatus], sizeof(status));
+  if (status != 0ull) {
+    cudaMemsetAsync(ra + kRaStatus, 0, sizeof(double), s);
+    return record_error(GB300_ERR_TIMEOUT,
+                        "%s: a row copy of the Lagrangian kernel did not arrive", where);
+  }
+  const double pair[2] = {head[kRaDt], head[kRaDtH]};
   mesh->dt = pair[0];
   mesh->dt_h = pair[1];
   return GB300_OK;
@@ -321,11 +473,25 @@ __global__ void k_make_shadows(size_t n, const double* rho, const double* e,
 
 }  // namespace
 
+namespace {
+// Output rows per CTA of the one-kernel Lagrangian phase.
+int g_lag_rows = lagf::kDefaultRows;
+}  // namespace
+
+int set_lagrangian_rows(int rows) {
+  if (rows < 1 || rows > lagf::kMaxRows) {
+    return record_error(GB300_ERR_ARG, "gb300_set_lagrangian_rows: %d not in 1 .. %d", rows,
+                        lagf::kMaxRows);
+  }
+  g_lag_rows = rows;
+  return GB300_OK;
+}
+
 int fused_solve(Mesh* mesh, int tt, double* P, double* rho, double* rho_old,
                 double* e, double* u, double* v, double* rho_u, double* rho_v,
                 double* Qxx, double* Qyy, double* F_x, double* F_y,
                 double* uF_x, double* uF_y, double* vF_x, double* vF_y,
-                double* reduce_array) {
+                double* reduce_array, bool one_kernel_lagrangian) {
   if (!reduce_array) return record_error(GB300_ERR_ARG, "solve_hydro_2d: reduce_array is NULL");
   cudaStream_t s = current_stream();
   StepArgs<double> a;
@@ -343,9 +509,41 @@ int fused_solve(Mesh* mesh, int tt, double* P, double* rho, double* rho_old,
   // into rho/e, so neither sweep updates its own input.
   const SweepArgs<double> first{rho, e, rho, e, uF_x, vF_y, uF_x, vF_y};
   const SweepArgs<double> second{uF_x, vF_y, uF_x, vF_y, rho, e, rho, e};
+  // The one-kernel Lagrangian phase when asked for and the arrays suit it: it
+  // stages rows with 16-byte TMA copies and
+  // keeps its change masks in rho_old (the reference's pre-advection density,
+  // which the fused sweeps do not read).
+  lagf::LagArgs lag{};
+  const lagf::LagArgs* lagp = nullptr;
+  if (one_kernel_lagrangian) {
+    lag.nx = a.nx;
+    lag.ny = a.ny;
+    lag.pad = a.pad;
+    lag.rows = g_lag_rows;
+    lag.ntx = (a.nx - 2 * a.pad + 1 + lagf::kW - 1) / lagf::kW;
+    const size_t mask_bytes = (size_t)(a.ny + 1) * lag.ntx * lagf::kMaskFields * lagf::kWarps * 4;
+    auto al16 = [](const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; };
+    if (al16(rho) && al16(e) && al16(rho_u) && al16(rho_v) && al16(rho_old) && a.pad == 2 &&
+        mask_bytes <= (size_t)a.nx * a.ny * sizeof(double)) {
+      lag.edgedx = a.edgedx; lag.edgedy = a.edgedy; lag.celldx = a.celldx; lag.celldy = a.celldy;
+      lag.rho = rho; lag.e = e; lag.rho_u = rho_u; lag.rho_v = rho_v;
+      lag.u = a.u; lag.v = a.v;
+      // Scratch for the changed values: arrays the step writes only later
+      // (P is not used by this form; F_x, F_y are the sweeps' outputs).
+      lag.e_new = P; lag.rho_u_new = F_x; lag.rho_v_new = F_y;
+      lag.masks = reinterpret_cast<unsigned*>(rho_old);
+      lag.ra = reduce_array;
+      lag.min_slot = a.min_slot;
+      lag.mesh_pow2 = a.mesh_pow2;
+      lag.dt_slot = a.dt_slot;
+      lag.dt = a.dt; lag.dt_h = a.dt_h; lag.max_dt = a.max_dt;
+      lag.first_step = a.first_step;
+      lagp = &lag;
+    }
+  }
   StepProfiler prof;
   prof.begin(s);
-  launch_step(s, a, tt, first, second, prof);
+  launch_step(s, a, tt, first, second, prof, lagp);
   return finish_step(s, mesh, reduce_array, prof, "solve_hydro_2d (fused)");
 }
 

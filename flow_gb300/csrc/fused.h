@@ -14,13 +14,23 @@ int check_sizes(int nx, int ny, int pad, const char* where);
 cudaStream_t current_stream();
 int verbose();
 
+// SMs of the current device (cached per device).
+int num_sms();
+// Kernel launches issued by this library (the fused step's kernels and the
+// conservation totals), for gb300_launch_count.
+void count_launches(unsigned n);
+
 // One full timestep with the fused kernels; dt/dt_h stay on the device inside
 // the step and are copied to mesh->dt/dt_h before returning.
+// one_kernel_lagrangian: the Lagrangian phase as one kernel (lag_fused.cuh)
+// instead of the four kernels the mixed and batched steps share.
 int fused_solve(Mesh* mesh, int tt, double* P, double* rho, double* rho_old,
                 double* e, double* u, double* v, double* rho_u, double* rho_v,
                 double* Qxx, double* Qyy, double* F_x, double* F_y,
                 double* uF_x, double* uF_y, double* vF_x, double* vF_y,
-                double* reduce_array);
+                double* reduce_array, bool one_kernel_lagrangian);
+// Output rows per CTA of the one-kernel Lagrangian phase (1 .. 64).
+int set_lagrangian_rows(int rows);
 
 // Mixed form: FP32 bulk arithmetic, FP64 density/energy and their
 // conservative updates.  The workspace holds every intermediate array.

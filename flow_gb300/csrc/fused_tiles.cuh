@@ -57,8 +57,8 @@ struct StepArgs {
   double* e;
   R* rho_r;         // the same fields in bulk precision (aliases for FP64)
   R* e_r;
-  double* P;        // FP64 form only: the reference's P and rho_old outputs
-  double* rho_old;
+  double* P;        // FP64 form: the pressures, for the shock-heating kernel
+  double* rho_old;  // unused: the first mass sweep reads the density itself
   R* u;             // velocities of the Lagrangian phase and the mass sweeps
   R* v;
   R* u_out;         // the caller's velocity arrays: the advected velocities
@@ -339,9 +339,10 @@ __device__ __forceinline__ R face_average(R a, R wa, R b, R wb) {
 // Lagrangian phase.
 
 // Pressure (EOS on the fly) -> face momenta -> velocities.  Covers every cell
-// (the FP64 form writes P and rho_old for ghosts too, as equation_of_state and
-// the rho_old copy of the reference do) and every interior x/y face.
-// omp3/flow.c:55-70, 110-158.
+// (the FP64 form stores P for ghosts too, as equation_of_state does; the
+// shock-heating kernel reads it where a cell is compressed) and every interior
+// x/y face.  The reference's rho_old copy is not made: the first mass sweep
+// reads the density itself.  omp3/flow.c:55-70, 110-158.
 template <typename R, bool kP2>
 __device__ __forceinline__ void tile_lag_pressure_impl(const StepArgs<R>& a, int bx, int by) {
   using Pr = Prec<R>;
@@ -406,13 +407,9 @@ __device__ __forceinline__ void tile_lag_pressure_impl(const StepArgs<R>& a, int
     if (k + 1 < a.rows && ii + 1 < ny) load(ii + 1);
     R Pc = R(0), rc = R(0);
     if (jj < nx) {
-      const size_t c = cidx(nx, ii, jj);
       rc = rc_l;
       Pc = g1 * rc * ec_l;
-      if (!Pr::kMixed) {
-        a.P[c] = double(Pc);
-        a.rho_old[c] = double(rc);
-      }
+      if (!Pr::kMixed) a.P[cidx(nx, ii, jj)] = double(Pc);
     }
     sP[t + 1] = Pc;
     sR[t + 1] = rc;

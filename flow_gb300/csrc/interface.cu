@@ -3,6 +3,7 @@
 // stages.cu and the fused timestep of fused.cu, plus error/stream control.
 #include <cstdarg>
 #include <cstdio>
+#include <atomic>
 #include <cstring>
 
 #include "../../include/flow_gb300.h"
@@ -40,6 +41,27 @@ int check_launch(const char* where) {
 }
 
 cudaStream_t current_stream() { return t_stream; }
+
+namespace {
+std::atomic<unsigned long long> g_launches{0};
+}  // namespace
+
+void count_launches(unsigned n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+int num_sms() {
+  static int cached[64] = {0};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) dev = 0;
+  if (cached[dev] <= 0) {
+    int n = 0;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) {
+      n = 1;
+    }
+    cached[dev] = n;
+  }
+  return cached[dev];
+}
 int verbose() { return g_verbose; }
 
 // Sizes the kernels support: one rank, pad >= 2, >= 2 interior cells per axis
@@ -359,7 +381,8 @@ int gb300_solve_hydro_2d(Mesh* mesh, int tt, double* P, double* rho,
   }
   FLOW_TRY(check_mesh(mesh, mesh->local_nx, mesh->local_ny, "solve_hydro_2d"));
   return fused_solve(mesh, tt, P, rho, rho_old, e, u, v, rho_u, rho_v, Qxx, Qyy,
-                     F_x, F_y, uF_x, uF_y, vF_x, vF_y, reduce_array);
+                     F_x, F_y, uF_x, uF_y, vF_x, vF_y, reduce_array,
+                     t_mode == GB300_MODE_FUSED_LAG);
 }
 
 void solve_hydro_2d(Mesh* mesh, int tt, double* P, double* rho,
@@ -551,13 +574,15 @@ int gb300_set_stream(void* stream) {
 }
 void* gb300_get_stream(void) { return t_stream; }
 int gb300_set_mode(int mode) {
-  if (mode != GB300_MODE_EXACT && mode != GB300_MODE_FUSED) {
+  if (mode != GB300_MODE_EXACT && mode != GB300_MODE_FUSED && mode != GB300_MODE_FUSED_LAG) {
     return record_error(GB300_ERR_ARG, "gb300_set_mode: unknown mode %d", mode);
   }
   t_mode = mode;
   return GB300_OK;
 }
 int gb300_get_mode(void) { return t_mode; }
+int gb300_set_lagrangian_rows(int rows) { return set_lagrangian_rows(rows); }
+unsigned long long gb300_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
 int gb300_set_verbose(int v) {
   g_verbose = v;
   return GB300_OK;

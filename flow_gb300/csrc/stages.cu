@@ -711,6 +711,7 @@ void launch_conservation(cudaStream_t s, int nx, int ny, int pad,
   cudaMemsetAsync(reduce_array + kRaTicket, 0, sizeof(double), s);
   k_conservation<<<conservation_blocks(nx, ny, pad), kRedThreads, 0, s>>>(
       nx, ny, pad, rho, e, reduce_array);
+  count_launches(1);
 }
 
 void launch_mass_energy_flux(cudaStream_t s, bool dir_y, int nx, int ny,

@@ -35,6 +35,9 @@ void launch_min_timestep(cudaStream_t s, int nx, int ny, int pad, double max_dt,
                          const double* Qyy, const double* rho, const double* e,
                          const MeshView& m, double* reduce_array);
 // Writes interior sum(rho), sum(rho e) to reduce_array[3..4].
+// Counts kernel launches for gb300_launch_count (interface.cu).
+void count_launches(unsigned n);
+
 void launch_conservation(cudaStream_t s, int nx, int ny, int pad,
                          const double* rho, const double* e,
                          double* reduce_array);

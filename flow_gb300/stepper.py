@@ -8,8 +8,9 @@ steps, CUDA events on the current stream) and, unless --no-profile, the time
 of each kernel of the step from the library's per-kernel event profile.
 Workloads: "sedov" (the blast of the benchmark), "sod" (a tube split at
 x = 0.5), "smooth" (density and energy 1 + a 16-mode smooth random field,
-seed 20261205).  Forms: "fp64" (solve_hydro_2d in the fused mode) and
-"mixed" (gb300_mixed_solve).  Small runs of this module are what the ncu
+seed 20261205).  Forms: "fp64" (solve_hydro_2d in the fused mode),
+"fp64lag" (the same with the one-kernel Lagrangian phase) and "mixed"
+(gb300_mixed_solve).  Small runs of this module are what the ncu
 captures of the kernels profile.
 """
 from __future__ import annotations
@@ -32,7 +33,7 @@ def main(argv=None) -> None:
     p = argparse.ArgumentParser(description=__doc__.splitlines()[0])
     p.add_argument("--size", type=int, default=4096)
     p.add_argument("--workload", choices=["sedov", "sod", "smooth"], default="sedov")
-    p.add_argument("--form", choices=["fp64", "mixed"], default="fp64")
+    p.add_argument("--form", choices=["fp64", "fp64lag", "mixed"], default="fp64")
     p.add_argument("--steps", type=int, default=100)
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--no-profile", action="store_true")
@@ -45,7 +46,7 @@ def main(argv=None) -> None:
 
     L = fg.lib()
     fg.set_stream(torch.cuda.current_stream())
-    fg.set_mode(fg.MODE_FUSED)
+    fg.set_mode(fg.MODE_FUSED_LAG if args.form == "fp64lag" else fg.MODE_FUSED)
     prob = make_problem(problems, args.workload, args.size)
     if args.form == "mixed":
         sim = fg.MixedSim(prob, "cuda:0")

@@ -145,10 +145,14 @@ enum {
 
 /* Timestep implementations selectable for solve_hydro_2d. */
 enum {
-  GB300_MODE_EXACT = 0, /* the stage entry points in sequence; bit-exact
-                           with the reference omp3 set */
-  GB300_MODE_FUSED = 1  /* fused kernels, FP64, within 1e-12 of the
-                           reference; the default */
+  GB300_MODE_EXACT = 0,      /* the stage entry points in sequence; bit-exact
+                                with the reference omp3 set */
+  GB300_MODE_FUSED = 1,      /* fused kernels, FP64, within 1e-12 of the
+                                reference; the default */
+  GB300_MODE_FUSED_LAG = 2   /* the same step with the Lagrangian phase
+                                (omp3/flow.c:22-38) as one kernel (TMA-staged,
+                                ~43 B/cell of DRAM traffic instead of ~165);
+                                the same numbers bit for bit */
 };
 
 int gb300_last_error(void);
@@ -161,6 +165,16 @@ void* gb300_get_stream(void);
 
 int gb300_set_mode(int mode);
 int gb300_get_mode(void);
+
+/* Output rows per CTA of the one-kernel Lagrangian phase of
+ * GB300_MODE_FUSED_LAG (1 .. 64, default 32): a tuning knob; every value gives
+ * the same numbers.  No reference counterpart (the reference has no tiles). */
+int gb300_set_lagrangian_rows(int rows);
+
+/* Kernel launches this library has issued for the fused timestep and the
+ * conservation totals since it was loaded (a counter a benchmark reads around
+ * its timed region).  No reference counterpart. */
+unsigned long long gb300_launch_count(void);
 
 /* 1 (default): print dt and conservation totals as the reference does
  * (omp3/flow.c:18-20, 991-994); 0: silent. */
