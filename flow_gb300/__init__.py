@@ -25,6 +25,10 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "libflow_gb300.so")
 
 GB300_OK = 0
+GB300_ERR_CUDA = 1
+GB300_ERR_ARG = 2
+GB300_ERR_TIMEOUT = 3
+GB300_ERR_STATE = 4
 MODE_EXACT = 0
 MODE_FUSED = 1
 MODE_FUSED_LAG = 2
@@ -139,6 +143,7 @@ def _declare(L: ctypes.CDLL) -> None:
         "gb300_batch_get_tuning": [V, IP, IP, IP, IP],
         "gb300_batch_step": [V, I, I],
         "gb300_batch_status": [V],
+        "gb300_batch_set_spin_limit": [V, ctypes.c_longlong],
         "gb300_batch_get_state": [V, I, P, P, P, P],
     }
     for name, args in batch.items():

@@ -78,6 +78,17 @@ class Batch:
             check()
         self.steps_done += steps
 
+    def set_spin_limit(self, spins: int) -> None:
+        """Bound of each grid-barrier wait, in 64 ns naps (default 2**25)."""
+        if lib().gb300_batch_set_spin_limit(self.handle, spins) != GB300_OK:
+            check()
+
+    def status_code(self) -> int:
+        """The status word after the steps so far (synchronises): GB300_OK,
+        or GB300_ERR_TIMEOUT when a grid barrier ran out (the barrier state is
+        then cleared, so the batch can be stepped again)."""
+        return int(lib().gb300_batch_status(self.handle))
+
     def status(self) -> None:
         if lib().gb300_batch_status(self.handle) != GB300_OK:
             check()

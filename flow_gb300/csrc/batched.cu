@@ -75,6 +75,7 @@ struct BatchDev {
   const int* prefix;    // [kNumShapes][n+1]
   Status* status;
   int n;
+  long long spin_limit;  // naps a barrier waits before it reports a timeout
 };
 
 __device__ __forceinline__ int shape_of(int ph) {
@@ -131,9 +132,11 @@ __device__ __forceinline__ void run_tile(int ph, const Instance<R>& I, int tx, i
   }
 }
 
-// Grid-wide barrier with a bounded wait.  Returns false (for every block) once
-// any block has timed out, so that all blocks leave the kernel.
-__device__ bool grid_sync(Status* st) {
+// Grid-wide barrier with a bounded wait of spin_limit 64 ns naps.  Returns
+// false (for every block) once any block has timed out, so that all blocks
+// leave the kernel: a waiting block also leaves as soon as another block has
+// recorded a timeout.
+__device__ bool grid_sync(Status* st, long long spin_limit) {
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -147,8 +150,9 @@ __device__ bool grid_sync(Status* st) {
       atomicAdd(&st->generation, 1u);
     } else {
       long long spins = 0;
-      while (*gen == g) {
-        if (++spins > kSpinLimit) {
+      volatile int* err = &st->error;
+      while (*gen == g && *err == 0) {
+        if (++spins > spin_limit) {
           atomicExch(&st->error, GB300_ERR_TIMEOUT);
           break;
         }
@@ -223,7 +227,7 @@ __global__ void __launch_bounds__(kCols, kBatchMinCtas<R>) k_batch_step(const Ba
       run_tile(ph[p], s_inst, local % tx_n[i], local / tx_n[i]);
       __syncthreads();
     }
-    if (!grid_sync(b.status)) return;
+    if (!grid_sync(b.status, b.spin_limit)) return;
     if (ph[p] == kPhEnergy) {
       // Every tile of every instance has added its CFL candidate: apply the
       // dt rule per instance.
@@ -235,7 +239,7 @@ __global__ void __launch_bounds__(kCols, kBatchMinCtas<R>) k_batch_step(const Ba
         a.first_step = first_step;
         finish_dt(a);
       }
-      if (!grid_sync(b.status)) return;
+      if (!grid_sync(b.status, b.spin_limit)) return;
       if (threadIdx.x == 0) s_cur = -1;  // reload dt into the cached instance
     }
   }
@@ -265,6 +269,7 @@ struct BatchImpl {
   int order = 0;        // 0 largest first, 1 input order
   int grid = 0;
   int tt = 0;
+  long long spin_limit = kSpinLimit;
   cudaGraphExec_t graph = nullptr;
   int graph_tt_parity = -1;
   std::vector<int> perm;  // instance order in the work list
@@ -403,7 +408,7 @@ int upload_tables(BatchImpl& B) {
 template <typename R>
 int launch_batch_step(BatchImpl& B, cudaStream_t s, int tt) {
   BatchDev<R> b{static_cast<const Instance<R>*>(B.d_inst), B.d_tiles_x, B.d_prefix,
-                B.d_status, B.n};
+                B.d_status, B.n, B.spin_limit};
   int first = (tt == 0) ? 1 : 0;
   void* args[] = {&b, &tt, &first};
   cudaLaunchConfig_t cfg{};
@@ -729,7 +734,10 @@ int gb300_batch_step(GB300Batch* b, int steps, int use_graph) {
 }
 
 // Status word of the batched kernel (GB300_ERR_TIMEOUT after a barrier ran
-// out of iterations); synchronises the stream.
+// out of iterations); synchronises the stream.  After reporting a timeout it
+// clears the barrier state (counter, generation, error), so the batch can be
+// stepped again; the instances' fields are then those of a step that stopped
+// part-way.
 int gb300_batch_status(GB300Batch* b) {
   using namespace flow;
   if (!b || !b->impl.pool) return GB300_ERR_ARG;
@@ -740,7 +748,29 @@ int gb300_batch_status(GB300Batch* b) {
     return record_error(GB300_ERR_CUDA, "gb300_batch_status: %s", cudaGetErrorString(err));
   }
   if (st.error != 0) {
+    cudaMemsetAsync(b->impl.d_status, 0, sizeof(Status), current_stream());
+    const cudaError_t e2 = cudaStreamSynchronize(current_stream());
+    if (e2 != cudaSuccess) {
+      return record_error(GB300_ERR_CUDA, "gb300_batch_status: %s", cudaGetErrorString(e2));
+    }
     return record_error(st.error, "gb300_batch: a grid barrier timed out");
+  }
+  return GB300_OK;
+}
+
+// Barrier wait bound of the batched kernel, in 64 ns naps (default 2^25,
+// about 2 s).  A captured step graph holds the old bound, so it is dropped
+// and captured again on the next graph step.
+int gb300_batch_set_spin_limit(GB300Batch* b, long long spins) {
+  using namespace flow;
+  if (!b || spins < 0) {
+    return record_error(GB300_ERR_ARG, "gb300_batch_set_spin_limit: bad arguments");
+  }
+  BatchImpl& B = b->impl;
+  B.spin_limit = spins;
+  if (B.graph) {
+    cudaGraphExecDestroy(B.graph);
+    B.graph = nullptr;
   }
   return GB300_OK;
 }

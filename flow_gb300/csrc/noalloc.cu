@@ -9,8 +9,6 @@
 // pattern.  The result does not depend on the grid, so repeated calls on the
 // same state return identical totals; it differs from gb300_conservation only
 // by the order of the additions.
-#include <mutex>
-
 #include "../../include/flow_gb300.h"
 #include "fused.h"
 
@@ -19,7 +17,6 @@ namespace {
 
 constexpr int kNoAllocMaxRows = GB300_NOALLOC_MAX_ROWS;
 constexpr int kNoAllocThreads = 256;
-constexpr int kNoAllocMaxDevices = 64;
 
 // Header (in doubles): [0] ticket (u64), [1] mass total, [2] energy total;
 // the row partials start at kRowBase, two per row.
@@ -94,11 +91,10 @@ __global__ void __launch_bounds__(kNoAllocThreads)
   }
 }
 
-std::mutex g_symbol_lock;
-double* g_symbol_addr[kNoAllocMaxDevices] = {};
-
-// Device address of the scratch on the current device, looked up once per
-// device with cudaGetSymbolAddress.
+// Device address of the scratch on the current device.  Looked up on every
+// call (cudaGetSymbolAddress allocates nothing): an address kept from an
+// earlier call would be stale after a device reset re-creates the context
+// and reloads the module.
 int scratch_address(double** out) {
   int dev = -1;
   cudaError_t err = cudaGetDevice(&dev);
@@ -106,21 +102,14 @@ int scratch_address(double** out) {
     return record_error(GB300_ERR_CUDA, "conservation_noalloc: cudaGetDevice: %s",
                         cudaGetErrorString(err));
   }
-  if (dev < 0 || dev >= kNoAllocMaxDevices) {
-    return record_error(GB300_ERR_ARG, "conservation_noalloc: device %d out of range", dev);
+  void* p = nullptr;
+  err = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (err != cudaSuccess || !p) {
+    return record_error(GB300_ERR_CUDA,
+                        "conservation_noalloc: cudaGetSymbolAddress on device %d: %s", dev,
+                        cudaGetErrorString(err));
   }
-  std::lock_guard<std::mutex> guard(g_symbol_lock);
-  if (!g_symbol_addr[dev]) {
-    void* p = nullptr;
-    err = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (err != cudaSuccess || !p) {
-      return record_error(GB300_ERR_CUDA,
-                          "conservation_noalloc: cudaGetSymbolAddress on device %d: %s", dev,
-                          cudaGetErrorString(err));
-    }
-    g_symbol_addr[dev] = static_cast<double*>(p);
-  }
-  *out = g_symbol_addr[dev];
+  *out = static_cast<double*>(p);
   return GB300_OK;
 }
 
@@ -158,7 +147,7 @@ extern "C" int gb300_conservation_noalloc(int nx, int ny, int pad, const double*
     return record_error(GB300_ERR_CUDA, "conservation_noalloc: %s", cudaGetErrorString(err));
   }
   int blocks = (rows + kNoAllocThreads / 32 - 1) / (kNoAllocThreads / 32);
-  if (blocks > 8 * 152) blocks = 8 * 152;
+  if (blocks > 8 * num_sms()) blocks = 8 * num_sms();  // 8 resident blocks per SM
   k_conservation_rows<<<blocks, kNoAllocThreads, 0, s>>>(nx, ny, pad, rho, e, scratch);
   const int lst = check_launch("conservation_noalloc");
   if (lst != GB300_OK) return lst;

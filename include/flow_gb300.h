@@ -198,7 +198,7 @@ int gb300_conservation(int nx, int ny, int pad, const double* rho,
 
 /* No counterpart in the reference.  The same interior totals as
  * gb300_conservation (out[0] = sum rho, out[1] = sum rho*e, host array,
- * synchronous on the current stream), for callers that hold only the density
+ * synchronous on the stream set with gb300_set_stream), for callers that hold only the density
  * and energy arrays and must not allocate device memory: a monitoring or
  * validation hook between timesteps (cudaMalloc/cudaFree would synchronise
  * the whole device and stall other streams' work), or a run whose ensemble
@@ -206,9 +206,11 @@ int gb300_conservation(int nx, int ny, int pad, const double* rho,
  * __device__ array inside libflow_gb300.so, holding one pair of partial sums
  * per interior row, so meshes with more than GB300_NOALLOC_MAX_ROWS interior
  * rows are rejected with GB300_ERR_ARG.
- *   - The first call on each device looks up the scratch address with
- *     cudaGetSymbolAddress (with that device current); make that first call
- *     before any stream capture begins.
+ *   - Every call looks up the scratch address of the current device with
+ *     cudaGetSymbolAddress, so it stays right across a device reset.
+ *   - Never call it while its stream is capturing a CUDA graph: it copies the
+ *     totals to host memory and synchronises the stream, neither of which a
+ *     capture allows.
  *   - The scratch's ticket counter must be zero when the kernel starts: it is
  *     zero at load, every call clears it on the stream before launching, and
  *     the kernel leaves it at zero.
@@ -313,6 +315,11 @@ int gb300_batch_get_tuning(const GB300Batch* batch, int* rows,
 int gb300_batch_step(GB300Batch* batch, int steps, int use_graph);
 /* Synchronises and returns GB300_ERR_TIMEOUT if a grid barrier ran out. */
 int gb300_batch_status(GB300Batch* batch);
+/* Bound of each grid-barrier wait of the batched kernel, in 64 ns naps
+ * (default 2^25, about 2 s): past it the kernel records GB300_ERR_TIMEOUT and
+ * every block returns.  No reference counterpart (the reference aborts on a
+ * CUDA error, cuda/flow.cu:24). */
+int gb300_batch_set_spin_limit(GB300Batch* batch, long long spins);
 /* Interior fields (host, optional), dt/dt_h pair and interior totals of rho
  * and rho*e of instance i. */
 int gb300_batch_get_state(GB300Batch* batch, int i, double* rho, double* e,

@@ -51,11 +51,15 @@ _lock = threading.Lock()
 _libs: dict[str, ctypes.CDLL] = {}
 
 
+# The reference's source tree, where present (FLOW_REF_DIR overrides).
+REF_DIR = os.environ.get("FLOW_REF_DIR", "/root/reference")
+
+
 def build() -> None:
     """Compiles the C restatement (and the reference, where its sources exist)."""
     subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
-    if os.path.isdir("/root/reference"):
-        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+    if os.path.isdir(REF_DIR):
+        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF_DIR={REF_DIR}"], check=True)
 
 
 def _load(name: str) -> ctypes.CDLL:

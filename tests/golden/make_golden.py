@@ -103,7 +103,7 @@ def write_reference_case():
              "iterations    100", "visit_dump    0"]
     with open(os.path.join(HERE, "flow.params"), "w") as f:
         f.write("\n".join(lines) + "\n")
-    with open("/root/reference/flow.tests") as f:
+    with open(os.path.join(O.REF_DIR, "flow.tests")) as f:
         golden = f.read().strip()
     with open(os.path.join(HERE, "flow.tests"), "w") as f:
         f.write(golden + "\n")

@@ -93,3 +93,33 @@ def test_batch_rejects_bad_arguments(fg):
     assert L.gb300_batch_create(1, one, one, None, None, 0, ctypes.byref(h)) == 2
     L.gb300_batch_clear = None
     fg.lib().gb300_clear_error()
+
+
+@pytest.mark.parametrize("use_graph", [False, True])
+def test_bounded_barrier_runs_out_and_recovers(fg, use_graph):
+    """A grid barrier of the persistent kernel whose wait bound is zero naps
+    runs out in every block that is not the last to arrive: the kernel records
+    GB300_ERR_TIMEOUT in its status word and every block returns (no hang, no
+    fault), the status call reports the timeout and re-arms the barrier, and
+    with the default bound restored the same batch steps again and reports
+    GB300_OK; a fresh batch from the same problems then still matches the
+    single-problem step."""
+    probs = ensemble()
+    b = fg.Batch(probs, precision=0)
+    b.set_spin_limit(0)
+    b.step(2, use_graph=use_graph)
+    assert b.status_code() == fg.GB300_ERR_TIMEOUT
+    assert "timed out" in fg.lib().gb300_last_error_message().decode()
+    fg.lib().gb300_clear_error()
+    b.set_spin_limit(1 << 25)
+    b.step(2, use_graph=use_graph)
+    assert b.status_code() == fg.GB300_OK
+    # The context is usable: a new batch advances exactly like the
+    # single-problem step.
+    b2 = fg.Batch(probs, precision=0)
+    b2.step(3, use_graph=use_graph)
+    b2.status()
+    for i, p in enumerate(probs):
+        rho, e, _, _ = b2.state(i)
+        ref = single(fg, p, 3, 0)
+        assert np.array_equal(rho, ref.interior("rho")) and np.array_equal(e, ref.interior("e"))

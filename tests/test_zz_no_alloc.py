@@ -99,3 +99,23 @@ def test_noalloc_rejects_more_rows_than_its_scratch(fg):
     # A valid call right after the rejections.
     assert L.gb300_conservation_noalloc(nx, ny - 1, pad, fg.dptr(rho), fg.dptr(e), outp) == 0
     assert out[0] == MAX_ROWS * (nx - 2 * pad) and out[1] == out[0]
+
+
+def test_noalloc_on_a_non_default_stream(fg):
+    """Both entry points routed to a caller's own stream (gb300_set_stream):
+    two no-allocation calls in a row give the totals gb300_conservation gives
+    on that stream.  The default stream is restored afterwards."""
+    import torch
+    from flow_gb300 import problems
+    L = fg.lib()
+    sim = fg.DeviceSim(problems.sedov(256))
+    sim.initial_timestep()
+    sim.run(4)
+    torch.cuda.synchronize()
+    stream = torch.cuda.Stream()
+    try:
+        assert L.gb300_set_stream(ctypes.c_void_p(stream.cuda_stream)) == 0
+        ref, got = totals_pair(fg, sim.nx, sim.ny, 2, sim.a["rho"], sim.a["e"], sim.a["reduce"])
+    finally:
+        L.gb300_set_stream(None)
+    check_pair(ref, got)
