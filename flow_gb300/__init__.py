@@ -144,6 +144,8 @@ def _declare(L: ctypes.CDLL) -> None:
         "gb300_batch_step": [V, I, I],
         "gb300_batch_status": [V],
         "gb300_batch_set_spin_limit": [V, ctypes.c_longlong],
+        "gb300_batch_set_schedule": [V, I],
+        "gb300_batch_get_schedule": [V],
         "gb300_batch_get_state": [V, I, P, P, P, P],
     }
     for name, args in batch.items():

@@ -2,7 +2,9 @@
 
 A Batch owns one device pool (a PyTorch byte tensor) into which the library
 lays out every instance's arrays; instances of different sizes advance
-together, each with its own dt, one persistent kernel launch per timestep.
+together, each with its own dt: one launch per phase of the timestep over
+every instance's tiles, or one persistent kernel launch per timestep
+(set_schedule), captured two steps at a time as a CUDA graph.
 """
 from __future__ import annotations
 
@@ -15,6 +17,9 @@ import numpy as np
 
 from . import GB300_OK, FlowError, check, lib
 from .problems import Problem
+
+BATCH_PHASES = 0      # include/flow_gb300.h GB300_BATCH_PHASES
+BATCH_PERSISTENT = 1  # GB300_BATCH_PERSISTENT
 
 _TUNE_CACHE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_tuning_cache.json")
 
@@ -73,6 +78,16 @@ class Batch:
         if lib().gb300_batch_set_tuning(self.handle, rows, ctas_per_sm, order) != GB300_OK:
             check()
 
+    def set_schedule(self, schedule: int) -> None:
+        """BATCH_PHASES (one launch per phase over every instance's tiles) or
+        BATCH_PERSISTENT (one cooperative launch per step)."""
+        if lib().gb300_batch_set_schedule(self.handle, schedule) != GB300_OK:
+            check()
+
+    @property
+    def schedule(self) -> int:
+        return int(lib().gb300_batch_get_schedule(self.handle))
+
     def step(self, steps: int = 1, use_graph: bool = True) -> None:
         if lib().gb300_batch_step(self.handle, steps, int(use_graph)) != GB300_OK:
             check()
@@ -106,37 +121,44 @@ class Batch:
         return rho, e, (dt[0], dt[1]), (tot[0], tot[1])
 
     def autotune(self, candidates=None, steps: int = 2, cache: bool = True) -> dict:
-        """Times each (rows, ctas_per_sm, order) candidate for `steps`
-        timesteps (these steps advance the ensemble, like warm-up steps) and
-        keeps the fastest; the choice is cached per GPU and batch signature."""
+        """Times each (schedule, rows, ctas_per_sm, order) candidate for
+        `steps` timesteps (these steps advance the ensemble, like warm-up
+        steps) and keeps the fastest; the choice is cached per GPU and batch
+        signature.  ctas_per_sm only applies to the persistent schedule."""
         torch = self.torch
         key = self._signature()
         if cache and os.path.exists(_TUNE_CACHE):
             try:
                 with open(_TUNE_CACHE) as f:
                     got = json.load(f).get(key)
-                if got:
+                if got and "schedule" in got:
+                    self.set_schedule(got["schedule"])
                     self.set_tuning(got["rows"], got["ctas_per_sm"], got["order"])
                     return {"cached": True, **got}
             except (OSError, ValueError):
                 pass
-        candidates = candidates or [(r, c, o) for r in (8, 16, 32) for c in (0, 2) for o in (0, 1)]
+        candidates = candidates or (
+            [(BATCH_PHASES, r, 0, o) for r in (8, 16, 32) for o in (0, 1)]
+            + [(BATCH_PERSISTENT, r, c, o) for r in (8, 16, 32) for c in (0, 2) for o in (0, 1)])
         results = []
-        for (r, c, o) in candidates:
+        for (sc, r, c, o) in candidates:
+            self.set_schedule(sc)
             self.set_tuning(r, c, o)
             self.step(2, use_graph=False)  # warm the variant
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             self.step(steps, use_graph=False)
             torch.cuda.synchronize()
-            results.append((time.perf_counter() - t0, r, c, o))
+            results.append((time.perf_counter() - t0, sc, r, c, o))
         results.sort()
-        _, r, c, o = results[0]
+        _, sc, r, c, o = results[0]
+        self.set_schedule(sc)
         self.set_tuning(r, c, o)
-        best = {"rows": r, "ctas_per_sm": c, "order": o,
+        best = {"schedule": sc, "rows": r, "ctas_per_sm": c, "order": o,
                 "ms_per_step": results[0][0] / steps * 1e3,
-                "tried": [{"rows": rr, "ctas_per_sm": cc, "order": oo, "ms_per_step": t / steps * 1e3}
-                          for (t, rr, cc, oo) in results]}
+                "tried": [{"schedule": ss, "rows": rr, "ctas_per_sm": cc, "order": oo,
+                           "ms_per_step": t / steps * 1e3}
+                          for (t, ss, rr, cc, oo) in results]}
         if cache:
             data = {}
             if os.path.exists(_TUNE_CACHE):

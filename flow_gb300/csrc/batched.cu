@@ -168,7 +168,7 @@ __device__ bool grid_sync(Status* st, long long spin_limit) {
 
 // Phase list of one step: the reference order (omp3/flow.c:22-51), with the
 // sweep order and the momentum order set by the step parity.
-__device__ __forceinline__ int phase_list(int tt, int* ph) {
+__host__ __device__ __forceinline__ int phase_list(int tt, int* ph) {
   int n = 0;
   ph[n++] = kPhPressure;
   ph[n++] = kPhViscosity;
@@ -245,6 +245,133 @@ __global__ void __launch_bounds__(kCols, kBatchMinCtas<R>) k_batch_step(const Ba
   }
 }
 
+// ---------------------------------------------------------------------------
+// Phase launches (the "phases" schedule): one kernel per phase over the work
+// items of every instance.  The kernel boundaries order the phases instead of
+// grid barriers, so each phase is compiled on its own, with the register
+// budget and asynchronous-copy rings of the single-problem kernel of that
+// phase (fused.cu) -- the persistent kernel holds every phase, and its
+// registers are the maximum over them.  Launches are chained with
+// programmatic dependent launch and captured, two steps at a time, in a CUDA
+// graph like the persistent launches.
+
+__device__ __forceinline__ void batch_pdl_wait() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+__device__ __forceinline__ void batch_pdl_trigger() {
+  asm volatile("griddepcontrol.launch_dependents;" :::);
+}
+
+template <int kPh>
+__host__ __device__ constexpr int phase_shape() {
+  return kPh == kPhPressure ? kShCells
+       : kPh == kPhAccel ? kShFaces
+       : (kPh == kPhSweepX1 || kPh == kPhSweepX2 || kPh == kPhMomUxV || kPh == kPhMomUx)
+           ? kShSweepX
+       : (kPh == kPhMomUyV || kPh == kPhMomUy) ? kShFaceU
+       : (kPh == kPhMomVyV || kPh == kPhMomVy) ? kShFaceV
+       : (kPh == kPhMomVxV || kPh == kPhMomVx) ? kShMomXV
+       : kShInterior;
+}
+
+// The tile function of one phase, in the form the single-problem kernels use
+// (copy rings and early first loads on).
+template <typename R, int kPh>
+__device__ __forceinline__ void phase_tile(const Instance<R>& I, int tx, int ty) {
+  if constexpr (kPh == kPhPressure) tile_lag_pressure(I.a, tx, ty);
+  else if constexpr (kPh == kPhViscosity) tile_lag_viscosity(I.a, tx, ty);
+  else if constexpr (kPh == kPhAccel) tile_lag_viscous_accel<R, true>(I.a, tx, ty);
+  else if constexpr (kPh == kPhEnergy) tile_lag_energy_dt<R, true>(I.a, tx, ty);
+  else if constexpr (kPh == kPhSweepX1) tile_mass_sweep_x<R, true, true>(I.a, I.first, tx, ty);
+  else if constexpr (kPh == kPhSweepY1) tile_mass_sweep_y<R, true, true>(I.a, I.first, tx, ty);
+  else if constexpr (kPh == kPhSweepX2) tile_mass_sweep_x<R, false, true>(I.a, I.second, tx, ty);
+  else if constexpr (kPh == kPhSweepY2) tile_mass_sweep_y<R, false, true>(I.a, I.second, tx, ty);
+  else if constexpr (kPh == kPhMomUxV) tile_mom_x<R, false, true, true>(I.a, tx, ty);
+  else if constexpr (kPh == kPhMomUx) tile_mom_x<R, false, false, true>(I.a, tx, ty);
+  else if constexpr (kPh == kPhMomUyV) tile_mom_y<R, false, true, true>(I.a, tx, ty);
+  else if constexpr (kPh == kPhMomUy) tile_mom_y<R, false, false, true>(I.a, tx, ty);
+  else if constexpr (kPh == kPhMomVxV) tile_mom_x<R, true, true, true>(I.a, tx, ty);
+  else if constexpr (kPh == kPhMomVx) tile_mom_x<R, true, false, true>(I.a, tx, ty);
+  else if constexpr (kPh == kPhMomVyV) tile_mom_y<R, true, true, true>(I.a, tx, ty);
+  else tile_mom_y<R, true, false, true>(I.a, tx, ty);
+}
+
+// Resident CTAs per SM of each phase kernel: those of the single-problem
+// kernels (fused.cu), which only the sweeps set -- one fewer for the y sweeps,
+// whose tile spills at the single-problem budget once the instance lookup
+// takes its registers (60-70 bytes per thread, measured with -Xptxas -v).
+template <typename R, int kPh>
+__host__ __device__ constexpr int phase_min_ctas() {
+  return (kPh == kPhSweepX1 || kPh == kPhSweepX2) ? (Prec<R>::kMixed ? 8 : 7)
+       : (kPh == kPhSweepY1 || kPh == kPhSweepY2) ? (Prec<R>::kMixed ? 6 : 5)
+       : 1;
+}
+
+template <typename R, int kPh>
+__global__ void __launch_bounds__(kCols, (phase_min_ctas<R, kPh>()))
+    k_batch_phase(const BatchDev<R> b, int first_step) {
+  // One work item per CTA (the grid is the phase's item count).
+  __shared__ Instance<R> s_inst;
+  batch_pdl_wait();
+  batch_pdl_trigger();
+  constexpr int shape = phase_shape<kPh>();
+  const int* pre = b.prefix + shape * (b.n + 1);
+  const int w = blockIdx.x;
+  // Instance of work item w: the last prefix entry <= w.
+  int lo = 0, hi = b.n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (pre[mid] <= w) lo = mid; else hi = mid - 1;
+  }
+  const int i = lo;
+  const int local = w - pre[i];
+  const int tx = b.tiles_x[shape * b.n + i];
+  // The instance's arguments, copied into shared memory by the whole block,
+  // with the dt pair the previous step left (Lagrangian phases).
+  static_assert(sizeof(Instance<R>) % 8 == 0, "8-byte words");
+  const unsigned long long* src = reinterpret_cast<const unsigned long long*>(b.inst + i);
+  unsigned long long* dst = reinterpret_cast<unsigned long long*>(&s_inst);
+  for (int k = threadIdx.x; k < (int)(sizeof(Instance<R>) / 8); k += blockDim.x) dst[k] = src[k];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    s_inst.a.dt = s_inst.a.dt_slot[0];
+    s_inst.a.dt_h = s_inst.a.dt_slot[1];
+    s_inst.a.first_step = first_step;
+  }
+  __syncthreads();
+  phase_tile<R, kPh>(s_inst, local % tx, local / tx);
+}
+
+// After the energy phase: the dt rule per instance (omp3/flow.c:103-105).
+template <typename R>
+__global__ void k_batch_finish_dt(const BatchDev<R> b, int first_step) {
+  batch_pdl_wait();
+  batch_pdl_trigger();
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < b.n; i += gridDim.x * blockDim.x) {
+    StepArgs<R> a = b.inst[i].a;
+    a.dt = a.dt_slot[0];
+    a.dt_h = a.dt_slot[1];
+    a.first_step = first_step;
+    finish_dt(a);
+  }
+}
+
+// Whether every spacing of an instance's mesh is a positive normal power of
+// two, one block per instance, into the flag its tiles read (mesh_pow2).
+template <typename R>
+__global__ void __launch_bounds__(256) k_batch_mesh_pow2(const BatchDev<R> b) {
+  const StepArgs<R>& a = b.inst[blockIdx.x].a;
+  bool ok = true;
+  for (int j = threadIdx.x; j <= a.nx; j += blockDim.x) {
+    ok = ok && d_is_pow2(a.celldx[j]) && d_is_pow2(a.edgedx[j]);
+  }
+  for (int j = threadIdx.x; j <= a.ny; j += blockDim.x) {
+    ok = ok && d_is_pow2(a.celldy[j]) && d_is_pow2(a.edgedy[j]);
+  }
+  ok = __syncthreads_and(ok) != 0;
+  if (threadIdx.x == 0) *const_cast<unsigned long long*>(a.mesh_pow2) = ok ? 1ull : 0ull;
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -269,6 +396,8 @@ struct BatchImpl {
   int order = 0;        // 0 largest first, 1 input order
   int grid = 0;
   int tt = 0;
+  int schedule = GB300_BATCH_PHASES;  // phase launches, or one persistent launch
+  std::vector<int> shape_total;       // work items per grid shape
   long long spin_limit = kSpinLimit;
   cudaGraphExec_t graph = nullptr;
   int graph_tt_parity = -1;
@@ -357,6 +486,7 @@ Instance<R> make_instance(const BatchImpl& B, int i) {
   a.uF_x = Rp(L.uF_x); a.uF_y = Rp(L.uF_y); a.vF_x = Rp(L.vF_x); a.vF_y = Rp(L.vF_y);
   a.ra = D(L.ra);
   a.min_slot = reinterpret_cast<unsigned long long*>(D(L.ra) + kRaMinSlot);
+  a.mesh_pow2 = reinterpret_cast<const unsigned long long*>(D(L.ra) + kRaMeshPow2);
   a.dt_slot = D(L.ra) + kRaDt;
   a.max_dt = 10.0;
   a.rows = B.rows;
@@ -396,6 +526,8 @@ int upload_tables(BatchImpl& B) {
       pre[s * (n + 1) + k + 1] = pre[s * (n + 1) + k] + cnt;
     }
   }
+  B.shape_total.assign(kNumShapes, 0);
+  for (int s = 0; s < kNumShapes; ++s) B.shape_total[s] = pre[s * (n + 1) + n];
   std::vector<Instance<R>> inst(n);
   for (int k = 0; k < n; ++k) inst[k] = make_instance<R>(B, B.perm[k]);
   cudaMemcpy(B.d_tiles_x, tx.data(), tx.size() * sizeof(int), cudaMemcpyHostToDevice);
@@ -405,10 +537,96 @@ int upload_tables(BatchImpl& B) {
   return check_launch("gb300_batch: table upload");
 }
 
+// Launches kernel k with programmatic stream serialisation: it may start as
+// soon as its predecessor's CTAs have all started, and waits on the device
+// (griddepcontrol.wait) for its predecessor's writes.
+template <typename... KArgs, typename... Args>
+cudaError_t launch_pdl(void (*k)(KArgs...), unsigned grid, unsigned block, cudaStream_t s,
+                       Args... args) {
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(block);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, k, args...);
+}
+
+template <typename R>
+BatchDev<R> batch_dev(const BatchImpl& B) {
+  return BatchDev<R>{static_cast<const Instance<R>*>(B.d_inst), B.d_tiles_x, B.d_prefix,
+                     B.d_status, B.n, B.spin_limit};
+}
+
+template <typename R, int kPh>
+cudaError_t launch_phase_k(const BatchImpl& B, const BatchDev<R>& b, int first, cudaStream_t s) {
+  const int items = B.shape_total[phase_shape<kPh>()];
+  if (items <= 0) return cudaSuccess;
+  count_launches(1);
+  return launch_pdl(k_batch_phase<R, kPh>, (unsigned)items, (unsigned)kCols, s, b, first);
+}
+
+template <typename R>
+cudaError_t launch_phase(const BatchImpl& B, const BatchDev<R>& b, int ph, int first,
+                         cudaStream_t s) {
+  switch (ph) {
+    case kPhPressure: return launch_phase_k<R, kPhPressure>(B, b, first, s);
+    case kPhViscosity: return launch_phase_k<R, kPhViscosity>(B, b, first, s);
+    case kPhAccel: return launch_phase_k<R, kPhAccel>(B, b, first, s);
+    case kPhEnergy: return launch_phase_k<R, kPhEnergy>(B, b, first, s);
+    case kPhSweepX1: return launch_phase_k<R, kPhSweepX1>(B, b, first, s);
+    case kPhSweepY1: return launch_phase_k<R, kPhSweepY1>(B, b, first, s);
+    case kPhSweepX2: return launch_phase_k<R, kPhSweepX2>(B, b, first, s);
+    case kPhSweepY2: return launch_phase_k<R, kPhSweepY2>(B, b, first, s);
+    case kPhMomUxV: return launch_phase_k<R, kPhMomUxV>(B, b, first, s);
+    case kPhMomUx: return launch_phase_k<R, kPhMomUx>(B, b, first, s);
+    case kPhMomUyV: return launch_phase_k<R, kPhMomUyV>(B, b, first, s);
+    case kPhMomUy: return launch_phase_k<R, kPhMomUy>(B, b, first, s);
+    case kPhMomVxV: return launch_phase_k<R, kPhMomVxV>(B, b, first, s);
+    case kPhMomVx: return launch_phase_k<R, kPhMomVx>(B, b, first, s);
+    case kPhMomVyV: return launch_phase_k<R, kPhMomVyV>(B, b, first, s);
+    default: return launch_phase_k<R, kPhMomVy>(B, b, first, s);
+  }
+}
+
+// One step as phase launches: the step's phases in the reference order, the
+// per-instance dt rule after the energy phase.
+template <typename R>
+int launch_batch_phases(BatchImpl& B, cudaStream_t s, int tt) {
+  const BatchDev<R> b = batch_dev<R>(B);
+  const int first = (tt == 0) ? 1 : 0;
+  int ph[20];
+  const int nph = phase_list(tt, ph);
+  for (int p = 0; p < nph; ++p) {
+    cudaError_t err = launch_phase<R>(B, b, ph[p], first, s);
+    if (err == cudaSuccess && ph[p] == kPhEnergy) {
+      count_launches(1);
+      err = launch_pdl(k_batch_finish_dt<R>, (unsigned)((B.n + 127) / 128), 128u, s, b, first);
+    }
+    if (err != cudaSuccess) {
+      return record_error(GB300_ERR_CUDA, "gb300_batch_step: %s", cudaGetErrorString(err));
+    }
+  }
+  return GB300_OK;
+}
+
+// The per-instance mesh test, once per gb300_batch_step call (the meshes do
+// not change during the steps of a call).
+template <typename R>
+int launch_batch_mesh_test(BatchImpl& B, cudaStream_t s) {
+  k_batch_mesh_pow2<R><<<(unsigned)B.n, 256, 0, s>>>(batch_dev<R>(B));
+  count_launches(1);
+  return check_launch("gb300_batch_step: mesh test");
+}
+
 template <typename R>
 int launch_batch_step(BatchImpl& B, cudaStream_t s, int tt) {
-  BatchDev<R> b{static_cast<const Instance<R>*>(B.d_inst), B.d_tiles_x, B.d_prefix,
-                B.d_status, B.n, B.spin_limit};
+  if (B.schedule == GB300_BATCH_PHASES) return launch_batch_phases<R>(B, s, tt);
+  BatchDev<R> b = batch_dev<R>(B);
   int first = (tt == 0) ? 1 : 0;
   void* args[] = {&b, &tt, &first};
   cudaLaunchConfig_t cfg{};
@@ -422,6 +640,7 @@ int launch_batch_step(BatchImpl& B, cudaStream_t s, int tt) {
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   const cudaError_t err = cudaLaunchKernelExC(&cfg, (const void*)k_batch_step<R>, args);
+  count_launches(1);
   if (err != cudaSuccess) {
     return record_error(GB300_ERR_CUDA, "gb300_batch_step: %s", cudaGetErrorString(err));
   }
@@ -677,6 +896,11 @@ int gb300_batch_step(GB300Batch* b, int steps, int use_graph) {
   auto launch = [&](int tt) {
     return B.precision ? launch_batch_step<float>(B, s, tt) : launch_batch_step<double>(B, s, tt);
   };
+  if (steps > 0) {
+    const int mst = B.precision ? launch_batch_mesh_test<float>(B, s)
+                                : launch_batch_mesh_test<double>(B, s);
+    if (mst != GB300_OK) return mst;
+  }
   int done = 0;
   // Step 0 (first_step = 1) and any odd leftover run as plain launches.
   while (done < steps && (B.tt == 0 || !use_graph || (B.tt % 2) != 0 || steps - done < 2)) {
@@ -756,6 +980,27 @@ int gb300_batch_status(GB300Batch* b) {
     return record_error(st.error, "gb300_batch: a grid barrier timed out");
   }
   return GB300_OK;
+}
+
+// Schedule of a step: GB300_BATCH_PHASES (one launch per phase over every
+// instance's tiles) or GB300_BATCH_PERSISTENT (one cooperative launch per
+// step, grid barriers between the phases).  A captured step graph is dropped.
+int gb300_batch_set_schedule(GB300Batch* b, int schedule) {
+  using namespace flow;
+  if (!b || (schedule != GB300_BATCH_PHASES && schedule != GB300_BATCH_PERSISTENT)) {
+    return record_error(GB300_ERR_ARG, "gb300_batch_set_schedule: bad arguments");
+  }
+  BatchImpl& B = b->impl;
+  B.schedule = schedule;
+  if (B.graph) {
+    cudaGraphExecDestroy(B.graph);
+    B.graph = nullptr;
+  }
+  return GB300_OK;
+}
+
+int gb300_batch_get_schedule(const GB300Batch* b) {
+  return b ? b->impl.schedule : -1;
 }
 
 // Barrier wait bound of the batched kernel, in 64 ns naps (default 2^25,

@@ -320,6 +320,18 @@ int gb300_batch_status(GB300Batch* batch);
  * every block returns.  No reference counterpart (the reference aborts on a
  * CUDA error, cuda/flow.cu:24). */
 int gb300_batch_set_spin_limit(GB300Batch* batch, long long spins);
+/* How a batched step is launched.  GB300_BATCH_PHASES (the default): one
+ * launch per phase of the step (pressure, viscosity, viscous acceleration,
+ * shock heating + CFL, the two sweeps, the four momentum pairs) over the tiles
+ * of every instance, plus the per-instance dt rule; each phase kernel has the
+ * register budget and copy rings of the single-problem kernel of that phase.
+ * GB300_BATCH_PERSISTENT: one cooperative launch per step running every phase
+ * with grid barriers between them.  Both give the single-problem numbers bit
+ * for bit; both are captured two steps at a time as a CUDA graph.  No
+ * reference counterpart. */
+enum { GB300_BATCH_PHASES = 0, GB300_BATCH_PERSISTENT = 1 };
+int gb300_batch_set_schedule(GB300Batch* batch, int schedule);
+int gb300_batch_get_schedule(const GB300Batch* batch);
 /* Interior fields (host, optional), dt/dt_h pair and interior totals of rho
  * and rho*e of instance i. */
 int gb300_batch_get_state(GB300Batch* batch, int i, double* rho, double* e,

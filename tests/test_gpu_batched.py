@@ -1,9 +1,10 @@
-"""The batched form (one persistent cooperative launch per timestep over many
-instances of different sizes, each with its own dt) against the
-single-problem fused step: every instance must match it bit for bit, in both
-precision forms, with or without the captured CUDA graph and for every tile
-shape; the FP64 instances must also match the oracle (1e-12 per cell for
-density and energy)."""
+"""The batched form (many instances of different sizes, each with its own dt,
+advanced by one launch per phase over every instance's tiles or by one
+persistent cooperative launch per timestep) against the single-problem fused
+step: every instance must match it bit for bit, in both precision forms, both
+schedules, with or without the captured CUDA graph and for every tile shape;
+the FP64 instances must also match the oracle (1e-12 per cell for density and
+energy)."""
 import numpy as np
 import pytest
 
@@ -38,10 +39,12 @@ def single(fg, prob, steps, precision):
 
 @pytest.mark.parametrize("precision", [0, 1])
 @pytest.mark.parametrize("use_graph", [False, True])
-def test_batch_matches_single_problem_step(fg, precision, use_graph):
+@pytest.mark.parametrize("schedule", [0, 1], ids=["phases", "persistent"])
+def test_batch_matches_single_problem_step(fg, precision, use_graph, schedule):
     probs = ensemble()
     steps = 9
     b = fg.Batch(probs, precision=precision)
+    b.set_schedule(schedule)
     b.step(steps, use_graph=use_graph)
     b.status()
     for i, p in enumerate(probs):
@@ -52,13 +55,15 @@ def test_batch_matches_single_problem_step(fg, precision, use_graph):
         assert dt[0] == sim.mesh.dt and dt[1] == sim.mesh.dt_h, i
 
 
-@pytest.mark.parametrize("tuning", [(8, 0, 0), (32, 1, 1), (16, 2, 0)])
+@pytest.mark.parametrize("tuning", [(0, 8, 0, 0), (0, 32, 0, 1), (1, 8, 0, 0), (1, 32, 1, 1),
+                                    (1, 16, 2, 0)])
 def test_batch_tile_shapes_give_identical_results(fg, tuning):
     probs = ensemble()[:3]
     ref = fg.Batch(probs, precision=0)
     ref.step(6)
     b = fg.Batch(probs, precision=0)
-    b.set_tuning(*tuning)
+    b.set_schedule(tuning[0])
+    b.set_tuning(*tuning[1:])
     b.step(6)
     b.status()
     for i in range(len(probs)):
@@ -106,6 +111,7 @@ def test_bounded_barrier_runs_out_and_recovers(fg, use_graph):
     single-problem step."""
     probs = ensemble()
     b = fg.Batch(probs, precision=0)
+    b.set_schedule(1)  # the persistent schedule (the one with grid barriers)
     b.set_spin_limit(0)
     b.step(2, use_graph=use_graph)
     assert b.status_code() == fg.GB300_ERR_TIMEOUT
