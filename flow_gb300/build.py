@@ -100,7 +100,7 @@ def _build_driver(verbose: bool) -> None:
         # The arch layer's problem set-up calls the kernel set's device
         # rasteriser (gb300_fill_boxes).
         cmd = ["gcc", "-O2", "-std=gnu99", "-fPIC", "-shared", *inc, arch_src, "-o", ARCH_LIB,
-               "-L" + PKG, "-lflow_gb300", "-Wl,-rpath,$ORIGIN", *link_cuda]
+               "-L" + PKG, "-lflow_gb300", "-Wl,-rpath,$ORIGIN", *link_cuda, "-pthread"]
         if verbose:
             print(" ".join(cmd), flush=True)
         subprocess.run(cmd, check=True)

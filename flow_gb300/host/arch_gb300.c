@@ -6,6 +6,7 @@
  * libflow_gb300_arch.so, which links libflow_gb300.so.
  */
 #include <cuda_runtime.h>
+#include <pthread.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -265,6 +266,90 @@ int within_tolerance(const double expected, const double actual,
   return (d < 0 ? -d : d) <= tolerance * scale;
 }
 
+/* ---- VisIt dump ----------------------------------------------------------
+ *
+ * write_all_ranks_to_visit (main.c:108-114, 129-135) without stalling the
+ * timestep: the interior rows are staged device-to-device on the timestep
+ * stream (so the next step may overwrite the field at once), copied from the
+ * staging block to page-locked host memory on a side stream, and a writer
+ * thread waits for that copy and writes <name><tt>.dat (the interior as
+ * little-endian doubles, row by row) and <name><tt>.bov (its VisIt header).
+ * kDumpSlots dumps may be in flight; a further call waits on the host for the
+ * oldest to be written.  write_all_ranks_flush() waits for every pending dump
+ * (it also runs at exit). */
+
+enum { kDumpSlots = 2 };
+enum { kSlotFree = 0, kSlotClaimed = 1, kSlotQueued = 2 };
+
+struct DumpSlot {
+  int state;               /* kSlotFree, kSlotClaimed or kSlotQueued */
+  int device;
+  double* d_stage;         /* interior block on the device */
+  double* h_buf;           /* page-locked host copy */
+  size_t cap;              /* doubles either buffer holds */
+  size_t w, h;             /* interior width and height */
+  cudaEvent_t staged, copied;
+  char dat[256], bov[256], var[64];
+  double time;
+  unsigned long long seq;  /* order of the call */
+};
+
+static struct DumpSlot g_dump[kDumpSlots];
+static pthread_mutex_t g_dump_lock = PTHREAD_MUTEX_INITIALIZER;
+static pthread_cond_t g_dump_cond = PTHREAD_COND_INITIALIZER;
+static pthread_t g_dump_thread;
+static int g_dump_started = 0;
+static cudaStream_t g_dump_stream = NULL;
+static unsigned long long g_dump_seq = 0, g_dump_done = 0;
+
+static void dump_write_files(struct DumpSlot* d) {
+  FILE* fp = fopen(d->dat, "wb");
+  if (!fp) TERMINATE("could not open %s\n", d->dat);
+  if (fwrite(d->h_buf, sizeof(double), d->w * d->h, fp) != d->w * d->h) {
+    TERMINATE("short write to %s\n", d->dat);
+  }
+  fclose(fp);
+  fp = fopen(d->bov, "w");
+  if (!fp) TERMINATE("could not open %s\n", d->bov);
+  const char* base = strrchr(d->dat, '/');
+  fprintf(fp, "TIME: %.12e\nDATA_FILE: %s\nDATA_SIZE: %zu %zu 1\n"
+              "DATA_FORMAT: DOUBLE\nVARIABLE: %s\nDATA_ENDIAN: LITTLE\n"
+              "CENTERING: zonal\nBRICK_ORIGIN: 0. 0. 0.\nBRICK_SIZE: %zu %zu 1\n",
+          d->time, base ? base + 1 : d->dat, d->w, d->h, d->var, d->w, d->h);
+  fclose(fp);
+}
+
+/* Writer thread: takes the queued slots in call order. */
+static void* dump_writer(void* arg) {
+  (void)arg;
+  pthread_mutex_lock(&g_dump_lock);
+  for (;;) {
+    struct DumpSlot* next = NULL;
+    while (!next) {
+      for (int k = 0; k < kDumpSlots; ++k) {
+        if (g_dump[k].state == kSlotQueued && g_dump[k].seq == g_dump_done) next = &g_dump[k];
+      }
+      if (!next) pthread_cond_wait(&g_dump_cond, &g_dump_lock);
+    }
+    pthread_mutex_unlock(&g_dump_lock);
+    cuda_or_die(cudaSetDevice(next->device), "visit dump: cudaSetDevice");
+    cuda_or_die(cudaEventSynchronize(next->copied), "visit dump copy");
+    dump_write_files(next);
+    pthread_mutex_lock(&g_dump_lock);
+    next->state = kSlotFree;
+    ++g_dump_done;
+    pthread_cond_broadcast(&g_dump_cond);
+  }
+  return NULL;
+}
+
+void write_all_ranks_flush(void) {
+  if (!g_dump_started) return;
+  pthread_mutex_lock(&g_dump_lock);
+  while (g_dump_done != g_dump_seq) pthread_cond_wait(&g_dump_cond, &g_dump_lock);
+  pthread_mutex_unlock(&g_dump_lock);
+}
+
 void write_all_ranks_to_visit(const int global_nx, const int global_ny,
                               const int local_nx, const int local_ny,
                               const int pad, const int x_off, const int y_off,
@@ -275,27 +360,63 @@ void write_all_ranks_to_visit(const int global_nx, const int global_ny,
   (void)global_nx; (void)global_ny; (void)x_off; (void)y_off; (void)nranks;
   (void)neighbours;
   if (rank != MASTER) return;
-  const size_t n = (size_t)local_nx * local_ny;
-  double* h = (double*)malloc(n * sizeof(double));
-  cuda_or_die(cudaMemcpy(h, arr, n * sizeof(double), cudaMemcpyDeviceToHost), "visit dump");
-  char name[256];
-  snprintf(name, sizeof(name), "%s%d.dat", arr_name, tt);
-  FILE* fp = fopen(name, "wb");
-  if (fp) {
-    for (int ii = pad; ii < local_ny - pad; ++ii) {
-      fwrite(&h[(size_t)ii * local_nx + pad], sizeof(double), (size_t)(local_nx - 2 * pad), fp);
+  const size_t w = (size_t)(local_nx - 2 * pad), h = (size_t)(local_ny - 2 * pad);
+  pthread_mutex_lock(&g_dump_lock);
+  if (!g_dump_started) {
+    cuda_or_die(cudaStreamCreateWithFlags(&g_dump_stream, cudaStreamNonBlocking),
+                "visit dump: stream");
+    if (pthread_create(&g_dump_thread, NULL, dump_writer, NULL) != 0) {
+      TERMINATE("visit dump: could not start the writer thread\n");
     }
-    fclose(fp);
+    pthread_detach(g_dump_thread);
+    atexit(write_all_ranks_flush);
+    g_dump_started = 1;
   }
-  snprintf(name, sizeof(name), "%s%d.bov", arr_name, tt);
-  fp = fopen(name, "w");
-  if (fp) {
-    fprintf(fp, "TIME: %.12e\nDATA_FILE: %s%d.dat\nDATA_SIZE: %d %d 1\n"
-                "DATA_FORMAT: DOUBLE\nVARIABLE: %s\nDATA_ENDIAN: LITTLE\n"
-                "CENTERING: zonal\nBRICK_ORIGIN: 0. 0. 0.\nBRICK_SIZE: %d %d 1\n",
-            elapsed_sim_time, arr_name, tt, local_nx - 2 * pad,
-            local_ny - 2 * pad, arr_name, local_nx - 2 * pad, local_ny - 2 * pad);
-    fclose(fp);
+  /* A free slot (the oldest dump is written first). */
+  struct DumpSlot* d = NULL;
+  while (!d) {
+    for (int k = 0; k < kDumpSlots && !d; ++k) {
+      if (g_dump[k].state == kSlotFree) d = &g_dump[k];
+    }
+    if (!d) pthread_cond_wait(&g_dump_cond, &g_dump_lock);
   }
-  free(h);
+  d->state = kSlotClaimed;
+  pthread_mutex_unlock(&g_dump_lock);
+
+  cuda_or_die(cudaGetDevice(&d->device), "visit dump: cudaGetDevice");
+  if (d->cap < w * h) {
+    if (d->d_stage) cudaFree(d->d_stage);
+    if (d->h_buf) cudaFreeHost(d->h_buf);
+    cuda_or_die(cudaMalloc((void**)&d->d_stage, w * h * sizeof(double)), "visit dump: cudaMalloc");
+    cuda_or_die(cudaMallocHost((void**)&d->h_buf, w * h * sizeof(double)),
+                "visit dump: cudaMallocHost");
+    d->cap = w * h;
+  }
+  if (!d->staged) {
+    cuda_or_die(cudaEventCreateWithFlags(&d->staged, cudaEventDisableTiming), "visit dump: event");
+    cuda_or_die(cudaEventCreateWithFlags(&d->copied, cudaEventDisableTiming), "visit dump: event");
+  }
+  /* The interior rows, packed, on the stream that writes the field. */
+  cudaStream_t s = (cudaStream_t)gb300_get_stream();
+  cuda_or_die(cudaMemcpy2DAsync(d->d_stage, w * sizeof(double),
+                                arr + (size_t)pad * local_nx + pad, (size_t)local_nx * sizeof(double),
+                                w * sizeof(double), h, cudaMemcpyDeviceToDevice, s),
+              "visit dump: staging copy");
+  cuda_or_die(cudaEventRecord(d->staged, s), "visit dump: event");
+  cuda_or_die(cudaStreamWaitEvent(g_dump_stream, d->staged, 0), "visit dump: wait");
+  cuda_or_die(cudaMemcpyAsync(d->h_buf, d->d_stage, w * h * sizeof(double),
+                              cudaMemcpyDeviceToHost, g_dump_stream),
+              "visit dump: host copy");
+  cuda_or_die(cudaEventRecord(d->copied, g_dump_stream), "visit dump: event");
+  d->w = w;
+  d->h = h;
+  d->time = elapsed_sim_time;
+  snprintf(d->dat, sizeof(d->dat), "%s%d.dat", arr_name, tt);
+  snprintf(d->bov, sizeof(d->bov), "%s%d.bov", arr_name, tt);
+  snprintf(d->var, sizeof(d->var), "%s", arr_name);
+  pthread_mutex_lock(&g_dump_lock);
+  d->seq = g_dump_seq++;
+  d->state = kSlotQueued;
+  pthread_cond_broadcast(&g_dump_cond);
+  pthread_mutex_unlock(&g_dump_lock);
 }

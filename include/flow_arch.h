@@ -87,8 +87,14 @@ void finalise_shared_data(SharedData* shared_data);
 int within_tolerance(const double expected, const double actual,
                      const double tolerance);
 
-/* VisIt field dump (main.c:108-114): writes density as a raw brick of
- * doubles plus a .bov header when visit dumps are requested. */
+/* VisIt field dump (main.c:108-114, 129-135): <arr_name><tt>.dat (the
+ * interior as little-endian doubles, row by row) and <arr_name><tt>.bov (its
+ * header), in the working directory.  Asynchronous: the call stages the
+ * interior on the device (on the kernel set's stream, gb300_get_stream, in
+ * order with the writes of arr) and returns; the host copy runs on a side
+ * stream and a writer thread writes the files, so the timestep stream never
+ * waits for the host or the disk.  At most two dumps are in flight (a third
+ * call waits for the oldest to be written). */
 void write_all_ranks_to_visit(const int global_nx, const int global_ny,
                               const int local_nx, const int local_ny,
                               const int pad, const int x_off, const int y_off,
@@ -96,6 +102,8 @@ void write_all_ranks_to_visit(const int global_nx, const int global_ny,
                               int* neighbours, double* arr,
                               const char* arr_name, const int tt,
                               const double elapsed_sim_time);
+/* Waits until every dump requested so far is on disk (also run at exit). */
+void write_all_ranks_flush(void);
 
 #ifdef __cplusplus
 }
