@@ -80,17 +80,76 @@ int check_sizes(int nx, int ny, int pad, const char* where) {
   return GB300_OK;
 }
 
+namespace {
+// Domain decomposition hooks (gb300_set_halo_exchange, gb300_set_reduce_min).
+gb300_halo_fn g_halo_fn = nullptr;
+void* g_halo_ctx = nullptr;
+gb300_reduce_min_fn g_rmin_fn = nullptr;
+void* g_rmin_ctx = nullptr;
+}  // namespace
+
+bool decomposed(const Mesh* m) {
+  for (int k = 0; k < 4; ++k) {
+    if (m->neighbours[k] != FLOW_EDGE) return true;
+  }
+  return false;
+}
+
+// A rank of a decomposed mesh runs the exact mode's stage kernels with its
+// ghost layers exchanged through the registered hooks.
 int check_mesh(const Mesh* m, int nx, int ny, const char* where) {
   if (!m) return record_error(GB300_ERR_ARG, "%s: mesh is NULL", where);
-  for (int k = 0; k < 4; ++k) {
-    if (m->neighbours[k] != FLOW_EDGE) {
-      return record_error(GB300_ERR_ARG,
-                          "%s: multi-rank meshes (halo exchange) are not "
-                          "supported; neighbour %d is rank %d",
-                          where, k, m->neighbours[k]);
-    }
+  if (decomposed(m) && (!g_halo_fn || !g_rmin_fn)) {
+    return record_error(GB300_ERR_ARG,
+                        "%s: a decomposed mesh (a neighbour is a rank) needs "
+                        "gb300_set_halo_exchange and gb300_set_reduce_min",
+                        where);
   }
   return check_sizes(nx, ny, m->pad, where);
+}
+
+int check_single_rank(const Mesh* m, const char* where) {
+  if (m && decomposed(m)) {
+    return record_error(GB300_ERR_ARG,
+                        "%s: the fused and mixed forms run one rank; a decomposed "
+                        "mesh runs in GB300_MODE_EXACT", where);
+  }
+  return GB300_OK;
+}
+
+// Ghost fill of a rank of a decomposed mesh: physical x walls over the
+// interior rows, the halo exchange (the hook: rows and columns from the
+// neighbouring ranks, full width), then physical y walls over whole rows --
+// the order of the single-rank fill, so corners agree.
+int decomposed_boundary(int w, int h, const Mesh* mesh, double* arr, int invert) {
+  cudaStream_t s = current_stream();
+  int sides = 0;
+  if (mesh->neighbours[FLOW_WEST] == FLOW_EDGE) sides |= 1;
+  if (mesh->neighbours[FLOW_EAST] == FLOW_EDGE) sides |= 2;
+  if (mesh->neighbours[FLOW_SOUTH] == FLOW_EDGE) sides |= 4;
+  if (mesh->neighbours[FLOW_NORTH] == FLOW_EDGE) sides |= 8;
+  launch_reflect_x(s, w, h, mesh->pad, arr, invert, sides);
+  const cudaError_t err = cudaStreamSynchronize(s);
+  if (err != cudaSuccess) {
+    return record_error(GB300_ERR_CUDA, "handle_boundary_2d: %s", cudaGetErrorString(err));
+  }
+  const int rc = g_halo_fn(g_halo_ctx, mesh, arr, w, h, invert);
+  if (rc != 0) {
+    return record_error(GB300_ERR_STATE, "handle_boundary_2d: the halo exchange returned %d",
+                        rc);
+  }
+  launch_reflect_y(s, w, h, mesh->pad, arr, invert, sides);
+  return check_launch("handle_boundary_2d");
+}
+
+// The global CFL minimum of a decomposed mesh: the rank's minimum (left in
+// reduce_array by the reduction kernel), reduced over the ranks by the hook.
+int reduce_min_over_ranks(double* g) {
+  const int rc = g_rmin_fn(g_rmin_ctx, g);
+  if (rc != 0) {
+    return record_error(GB300_ERR_STATE, "set_timestep: the minimum reduction returned %d", rc);
+  }
+  return GB300_OK;
 }
 
 MeshView view(const Mesh* m) {
@@ -113,6 +172,7 @@ namespace {
 // Status-returning forms of the stage entry points.
 
 int st_boundary(int w, int h, const Mesh* mesh, double* arr, int invert) {
+  if (decomposed(mesh)) return decomposed_boundary(w, h, mesh, arr, invert);
   launch_boundary(current_stream(), w, h, mesh->pad, arr, invert);
   return GB300_OK;
 }
@@ -183,8 +243,19 @@ int st_set_timestep(int nx, int ny, const double* Qxx, const double* Qyy,
   if (!reduce_array) return record_error(GB300_ERR_ARG, "set_timestep: reduce_array is NULL");
   cudaStream_t s = current_stream();
   MeshView m{mesh->edgedx, mesh->edgedy, celldx, celldy};
+  const bool ranks = decomposed(mesh);
   launch_min_timestep(s, nx, ny, mesh->pad, mesh->max_dt, mesh->dt_h,
-                      first_step, Qxx, Qyy, rho, e, m, reduce_array);
+                      first_step, Qxx, Qyy, rho, e, m, reduce_array, ranks ? 1 : 0);
+  if (ranks) {
+    double g = 0.0;
+    cudaMemcpyAsync(&g, reduce_array + kRaMinBits, sizeof(double), cudaMemcpyDeviceToHost, s);
+    const cudaError_t e1 = cudaStreamSynchronize(s);
+    if (e1 != cudaSuccess) {
+      return record_error(GB300_ERR_CUDA, "set_timestep: %s", cudaGetErrorString(e1));
+    }
+    FLOW_TRY(reduce_min_over_ranks(&g));
+    launch_dt_rule(s, g, mesh->dt_h, first_step, reduce_array);
+  }
   double local[2];
   double* pair = pinned_pair();
   if (!pair) pair = local;
@@ -375,6 +446,7 @@ int gb300_solve_hydro_2d(Mesh* mesh, int tt, double* P, double* rho,
   if (g_verbose && mesh->rank == 0) {
     printf("Timestep:        %.12e\n", mesh->dt);
   }
+  if (t_mode != GB300_MODE_EXACT) FLOW_TRY(check_single_rank(mesh, "solve_hydro_2d"));
   if (t_mode == GB300_MODE_EXACT) {
     return st_solve_exact(mesh, tt, P, rho, rho_old, e, u, v, rho_u, rho_v, Qxx,
                           Qyy, F_x, F_y, uF_x, uF_y, vF_x, vF_y, reduce_array);
@@ -582,6 +654,16 @@ int gb300_set_mode(int mode) {
 }
 int gb300_get_mode(void) { return t_mode; }
 int gb300_set_lagrangian_rows(int rows) { return set_lagrangian_rows(rows); }
+int gb300_set_halo_exchange(gb300_halo_fn fn, void* ctx) {
+  g_halo_fn = fn;
+  g_halo_ctx = ctx;
+  return GB300_OK;
+}
+int gb300_set_reduce_min(gb300_reduce_min_fn fn, void* ctx) {
+  g_rmin_fn = fn;
+  g_rmin_ctx = ctx;
+  return GB300_OK;
+}
 unsigned long long gb300_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
 int gb300_set_verbose(int v) {
   g_verbose = v;
@@ -615,6 +697,7 @@ int gb300_mixed_prepare(Mesh* mesh, double* rho, double* e, void* workspace,
                         size_t bytes, double* reduce_array,
                         int initial_timestep) {
   if (!mesh) return record_error(GB300_ERR_ARG, "gb300_mixed_prepare: mesh is NULL");
+  FLOW_TRY(check_single_rank(mesh, "gb300_mixed_prepare"));
   FLOW_TRY(check_mesh(mesh, mesh->local_nx, mesh->local_ny, "gb300_mixed_prepare"));
   FLOW_TRY(mixed_prepare(mesh, rho, e, workspace, bytes));
   if (!initial_timestep) return GB300_OK;
@@ -632,6 +715,7 @@ int gb300_mixed_solve(Mesh* mesh, int tt, double* rho, double* e, float* rho_u,
                       float* rho_v, void* workspace, size_t bytes,
                       double* reduce_array) {
   if (!mesh) return record_error(GB300_ERR_ARG, "gb300_mixed_solve: mesh is NULL");
+  FLOW_TRY(check_single_rank(mesh, "gb300_mixed_solve"));
   FLOW_TRY(check_mesh(mesh, mesh->local_nx, mesh->local_ny, "gb300_mixed_solve"));
   if (g_verbose && mesh->rank == 0) {
     printf("Timestep:        %.12e\n", mesh->dt);

@@ -143,11 +143,22 @@ __device__ __forceinline__ double warp_sum(double x) {
 
 constexpr int kRedThreads = 256;
 
+// Leapfrog update of omp3/flow.c:103-105 from the global CFL minimum g.
+__device__ __forceinline__ void apply_dt_rule(double g, double dt_h_in, int first_step,
+                                              double* ra) {
+  const double limited = dmin(g, FLOW_C_M * dt_h_in);
+  const double dt = 0.5 * (kCT * limited + dt_h_in);
+  ra[kRaDt] = dt;
+  ra[kRaDtH] = first_step ? dt : kCT * limited;
+}
+
+// local_only: a rank of a decomposed mesh keeps its minimum in ra[kRaMinBits]
+// (the caller reduces it over the ranks and applies the rule, k_dt_rule).
 __global__ void __launch_bounds__(kRedThreads)
     k_min_timestep(int nx, int ny, int pad, double max_dt, double dt_h_in,
                    int first_step, const double* Qxx, const double* Qyy,
                    const double* rho, const double* e, const double* celldx,
-                   const double* celldy, double* ra) {
+                   const double* celldy, double* ra, int local_only) {
   const int w = nx - 2 * pad;
   const long long n = (long long)w * (ny - 2 * pad);
   double m = max_dt;
@@ -191,13 +202,17 @@ __global__ void __launch_bounds__(kRedThreads)
   if (threadIdx.x == 0) {
     double g = s_part[0];
     for (int k = 1; k < kRedThreads / 32; ++k) g = dmin(g, s_part[k]);
-    // Leapfrog update of omp3/flow.c:103-105.
-    const double limited = dmin(g, FLOW_C_M * dt_h_in);
-    const double dt = 0.5 * (kCT * limited + dt_h_in);
-    ra[kRaDt] = dt;
-    ra[kRaDtH] = first_step ? dt : kCT * limited;
+    if (local_only) {
+      ra[kRaMinBits] = g;
+    } else {
+      apply_dt_rule(g, dt_h_in, first_step, ra);
+    }
     *reinterpret_cast<unsigned long long*>(ra + kRaTicket) = 0ull;
   }
+}
+
+__global__ void k_dt_rule(double g, double dt_h_in, int first_step, double* ra) {
+  if (threadIdx.x == 0) apply_dt_rule(g, dt_h_in, first_step, ra);
 }
 
 // Partial sums of one thread: two (mass, energy) pairs.
@@ -605,6 +620,46 @@ __global__ void k_boundary(int w, int h, int pad, double* arr, int flip_x,
   arr[(size_t)ii * w + jj] = neg ? -val : val;
 }
 
+// The x-wall part of the reflective fill (ghost columns of the interior rows)
+// on the sides whose bit is set in sides (1 west, 2 east), and the y-wall part
+// (whole ghost rows, x ghosts included) on sides 4 south (low rows), 8 north.
+// With all four bits, the x part followed by the y part fills exactly what
+// k_boundary fills.
+__global__ void k_reflect_x(int w, int h, int pad, double* arr, int flip_x, int sides) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= 2LL * pad * (h - 2 * pad)) return;
+  const int r = (int)(t / (2 * pad));
+  const int k = (int)(t % (2 * pad));
+  const int ii = pad + r;
+  if (k < pad) {
+    if (!(sides & 1)) return;
+    const int jj = k;
+    const double val = arr[(size_t)ii * w + (2 * pad - 1 - jj)];
+    arr[(size_t)ii * w + jj] = flip_x ? -val : val;
+  } else {
+    if (!(sides & 2)) return;
+    const int jj = w - 2 * pad + k;
+    const double val = arr[(size_t)ii * w + (2 * (w - pad) - 1 - jj)];
+    arr[(size_t)ii * w + jj] = flip_x ? -val : val;
+  }
+}
+__global__ void k_reflect_y(int w, int h, int pad, double* arr, int flip_y, int sides) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= 2LL * pad * w) return;
+  const int r = (int)(t / w);
+  const int jj = (int)(t % w);
+  if (r < pad) {
+    if (!(sides & 4)) return;
+    const double val = arr[(size_t)(2 * pad - 1 - r) * w + jj];
+    arr[(size_t)r * w + jj] = flip_y ? -val : val;
+  } else {
+    if (!(sides & 8)) return;
+    const int ii = h - 2 * pad + r;
+    const double val = arr[(size_t)(2 * (h - pad) - 1 - ii) * w + jj];
+    arr[(size_t)ii * w + jj] = flip_y ? -val : val;
+  }
+}
+
 __global__ void k_copy(size_t n, double* dst, const double* src) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
        i += (size_t)gridDim.x * blockDim.x) {
@@ -698,11 +753,31 @@ int conservation_blocks(int nx, int ny, int pad) {
 void launch_min_timestep(cudaStream_t s, int nx, int ny, int pad, double max_dt,
                          double dt_h, int first_step, const double* Qxx,
                          const double* Qyy, const double* rho, const double* e,
-                         const MeshView& m, double* reduce_array) {
+                         const MeshView& m, double* reduce_array, int local_only) {
   cudaMemsetAsync(reduce_array + kRaTicket, 0, sizeof(double), s);
   k_min_timestep<<<reduce_blocks(nx, ny, pad, 1), kRedThreads, 0, s>>>(
       nx, ny, pad, max_dt, dt_h, first_step, Qxx, Qyy, rho, e, m.celldx,
-      m.celldy, reduce_array);
+      m.celldy, reduce_array, local_only);
+}
+
+void launch_dt_rule(cudaStream_t s, double g, double dt_h, int first_step, double* ra) {
+  k_dt_rule<<<1, 32, 0, s>>>(g, dt_h, first_step, ra);
+}
+
+void launch_reflect_x(cudaStream_t s, int w, int h, int pad, double* arr, int invert,
+                      int sides) {
+  const long long n = 2LL * pad * (h - 2 * pad);
+  if (n <= 0 || !(sides & 3)) return;
+  k_reflect_x<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(w, h, pad, arr, invert == kInvertX,
+                                                         sides);
+}
+
+void launch_reflect_y(cudaStream_t s, int w, int h, int pad, double* arr, int invert,
+                      int sides) {
+  const long long n = 2LL * pad * w;
+  if (n <= 0 || !(sides & 12)) return;
+  k_reflect_y<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(w, h, pad, arr, invert == kInvertY,
+                                                         sides);
 }
 
 void launch_conservation(cudaStream_t s, int nx, int ny, int pad,

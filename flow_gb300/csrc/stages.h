@@ -33,10 +33,20 @@ void launch_shock_heating(cudaStream_t s, int nx, int ny, int pad, double dt_h,
 void launch_min_timestep(cudaStream_t s, int nx, int ny, int pad, double max_dt,
                          double dt_h, int first_step, const double* Qxx,
                          const double* Qyy, const double* rho, const double* e,
-                         const MeshView& m, double* reduce_array);
+                         const MeshView& m, double* reduce_array, int local_only = 0);
 // Writes interior sum(rho), sum(rho e) to reduce_array[3..4].
 // Counts kernel launches for gb300_launch_count (interface.cu).
 void count_launches(unsigned n);
+
+// Ghost fill of a rank of a decomposed mesh: x walls over the interior rows,
+// y walls over whole rows, on the sides set (1 west, 2 east, 4 south, 8 north).
+void launch_reflect_x(cudaStream_t s, int w, int h, int pad, double* arr, int invert,
+                      int sides);
+void launch_reflect_y(cudaStream_t s, int w, int h, int pad, double* arr, int invert,
+                      int sides);
+// The dt rule (omp3/flow.c:103-105) applied on the device to a CFL minimum g
+// reduced over the ranks of a decomposed mesh.
+void launch_dt_rule(cudaStream_t s, double g, double dt_h, int first_step, double* ra);
 
 void launch_conservation(cudaStream_t s, int nx, int ny, int pad,
                          const double* rho, const double* e,

@@ -171,6 +171,27 @@ int gb300_get_mode(void);
  * the same numbers.  No reference counterpart (the reference has no tiles). */
 int gb300_set_lagrangian_rows(int rows);
 
+/* Domain decomposition (the arch layer's MPI DECOMP, Makefile:47-59: each
+ * rank a band of the mesh, halo layers exchanged in every
+ * handle_boundary_2d(..., PACK), e.g. omp3/flow.c:156-157, and the dt
+ * minimum reduced by reduce_all_min, omp3/flow.c:100).  A rank whose Mesh
+ * has a neighbour that is a rank (neighbours[k] != FLOW_EDGE) runs in
+ * GB300_MODE_EXACT, with its ghost layers filled as the single-rank step
+ * fills them: physical x walls over the interior rows, then the exchange,
+ * then physical y walls over whole rows.  The caller supplies the transport:
+ *   halo(ctx, mesh, arr, w, h, invert) fills the ghost layers of the w x h
+ *     device array arr that face neighbouring ranks (pad rows/columns, full
+ *     width) from those ranks' interior values, synchronously; the library
+ *     has synchronised its stream before the call.  Returns 0 on success.
+ *   reduce_min(ctx, &value) replaces value by its minimum over the ranks.
+ * flow_gb300/decomp.py gives both over torch.distributed and over threads
+ * sharing one GPU.  Results match the single-rank exact step bit for bit. */
+typedef int (*gb300_halo_fn)(void* ctx, const Mesh* mesh, double* arr, int w, int h,
+                             int invert);
+typedef int (*gb300_reduce_min_fn)(void* ctx, double* value);
+int gb300_set_halo_exchange(gb300_halo_fn fn, void* ctx);
+int gb300_set_reduce_min(gb300_reduce_min_fn fn, void* ctx);
+
 /* Kernel launches this library has issued for the fused timestep and the
  * conservation totals since it was loaded (a counter a benchmark reads around
  * its timed region).  No reference counterpart. */

@@ -98,6 +98,14 @@ int strmatch(const char* a, const char* b);
 void initialise_mpi(int argc, char** argv, int* rank, int* nranks);
 void initialise_comms(Mesh* mesh);
 void initialise_devices(int rank);
+/* Transport hooks of a decomposed run (tests only): fill the ghost layers of
+ * arr (nx x ny) facing other ranks; replace *value by its minimum over the
+ * ranks. */
+typedef int (*flow_shim_halo_fn)(void* ctx, const Mesh* mesh, double* arr, int nx, int ny,
+                                 int invert);
+typedef int (*flow_shim_min_fn)(void* ctx, double* value);
+void flow_shim_set_halo(flow_shim_halo_fn fn, void* ctx);
+void flow_shim_set_reduce_min(flow_shim_min_fn fn, void* ctx);
 double reduce_all_min(double value);
 double reduce_all_sum(double value);
 double reduce_to_master(double value);
