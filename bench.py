@@ -221,40 +221,68 @@ def oracle_start(prob):
     return hm, st
 
 
+class quiet_stdout:
+    """Sends file descriptor 1 to /dev/null (the reference's own code prints
+    dt and totals every step; the benchmark prints one JSON line)."""
+
+    def __enter__(self):
+        sys.stdout.flush()
+        self.saved = os.dup(1)
+        self.null = os.open(os.devnull, os.O_WRONLY)
+        os.dup2(self.null, 1)
+        return self
+
+    def __exit__(self, *exc):
+        os.dup2(self.saved, 1)
+        os.close(self.saved)
+        os.close(self.null)
+
+
+def cpu_kind() -> str:
+    """The reference's own omp3 set built with its flags where it was built
+    (oracle/_ref), else the oracle with the same flags."""
+    from oracle import oracle as O
+    ok = os.path.exists(os.path.join(ROOT, "oracle", "_ref", "libflow_ref_default.so"))
+    return "reference_default" if ok else "fast"
+
+
 def cpu_run(n: int, steps: int, warmup: int, budget_s: float, workload: str = "sedov"):
-    """Times the oracle, built with the reference's flags (-O3 -march=native
-    -fopenmp, Makefile:15), on the same workload; returns (cell-steps/s,
-    steps timed, threads).  Times all `steps` steps unless that would take
-    more than about budget_s seconds."""
+    """Times the reference's omp3 set (or, where it was not built, the oracle)
+    built with the reference's flags (-O3 -march=native -fopenmp, Makefile:15)
+    on the same workload, a step being solve_hydro_2d + print_conservation as
+    the reference driver times it (main.c:80-93); returns (cell-steps/s,
+    steps timed, threads, kind).  Times all `steps` steps unless that would
+    take more than about budget_s seconds."""
     threads = _omp_env()
     from flow_gb300 import problems
     from oracle import oracle as O
+    kind = cpu_kind()
     prob = main_problem(problems, workload, n)
     hm = O.HostMesh(n, n, dt=prob.dt_param)
     st = O.HostState(hm)
     O.fill_fields(hm, st, prob.interior(prob.rho), prob.interior(prob.e))
-    O.initial_timestep(hm, st, "fast")
-    L = O.lib("fast")
-    out = (O.ctypes.c_double * 2)()
+    L = O.lib(kind)
+    with quiet_stdout():
+        O.initial_timestep(hm, st, kind)
 
-    def one(tt):
-        O.step(hm, st, tt, "fast")
-        L.flow_oracle_conservation(hm.nx, hm.ny, O.PAD, O.ptr(st["rho"]), O.ptr(st["e"]),
-                                   O.ctypes.cast(out, O.ctypes.POINTER(O.ctypes.c_double)))
+        def one(tt):
+            O.step(hm, st, tt, kind)
+            L.print_conservation(hm.nx, hm.ny, O.ptr(st["rho"]), O.ptr(st["e"]),
+                                 O.ptr(st["reduce"]), O.ctypes.byref(hm.mesh))
 
-    tt = 0
-    for _ in range(max(1, warmup)):
+        tt = 0
+        for _ in range(max(1, warmup)):
+            t0 = time.perf_counter()
+            one(tt)
+            tt += 1
+            t_step = time.perf_counter() - t0
+        timed = max(1, min(steps, int(budget_s / max(t_step, 1e-6))))
         t0 = time.perf_counter()
-        one(tt)
-        tt += 1
-        t_step = time.perf_counter() - t0
-    timed = max(1, min(steps, int(budget_s / max(t_step, 1e-6))))
-    t0 = time.perf_counter()
-    for _ in range(timed):
-        one(tt)
-        tt += 1
-    el = time.perf_counter() - t0
-    return n * n * timed / el, timed, threads
+        for _ in range(timed):
+            one(tt)
+            tt += 1
+        el = time.perf_counter() - t0
+    return n * n * timed / el, timed, threads, kind
 
 
 def oracle_compare(fields: dict, prob, steps: int, dt_pair=None):
@@ -288,16 +316,23 @@ def oracle_compare(fields: dict, prob, steps: int, dt_pair=None):
     return out
 
 
+CPU_WHAT = {
+    "reference_default": "the reference's own omp3/flow.c, main.c's step, built -O3 "
+                         "-march=native -fopenmp as its Makefile:15 on the restated arch layer",
+    "fast": "the oracle, a C restatement of the reference omp3 set that the tests hold "
+            "bit-identical to it, built -O3 -march=native -fopenmp as the reference's Makefile:15",
+}
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    value, timed, threads = cpu_run(args.size, args.steps, args.warmup, budget_s=150.0,
-                                    workload=args.workload)
+    value, timed, threads, kind = cpu_run(args.size, args.steps, args.warmup, budget_s=150.0,
+                                          workload=args.workload)
     sample = (f"{args.workload} {args.size}^2 FP64 timesteps + conservation totals on "
-              f"{threads} host threads (the oracle, -O3 -march=native -fopenmp as the "
-              f"reference's Makefile:15): {timed} of {args.steps} requested steps timed "
-              f"after {args.warmup} warm-up")
+              f"{threads} host threads ({CPU_WHAT[kind]}): {timed} of {args.steps} requested "
+              f"steps timed after {args.warmup} warm-up")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
@@ -305,7 +340,8 @@ def run_reference(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": f"{args.workload}_{args.size}_fp64", "nx": args.size, "ny": args.size,
                    "form": "fp64", "parallelism": "host OpenMP"},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads,
+                         "kind": "reference" if kind == "reference_default" else "port",
                          "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -473,6 +509,48 @@ def run_fp64_smooth(fg, problems, torch, device, n, steps, warmup, figures, fma_
         out["fp64_pipe"] = {"fp64_inst_per_cell_step": per_cell,
                             "fraction_of_measured_fp64_rate": per_cell * value / fma_rate}
     return out
+
+
+def run_reference_cuda(fg, problems, torch, device, n, steps, warmup, workload, fused_value):
+    """A second GPU baseline: the reference's own cuda kernel set (cuda/flow.cu
+    and cuda/flow.k, its flow_interface.h entry points) built for sm_103a on
+    the restated arch CUDA layer, timed on the same workload and GPU -- a step
+    is its solve_hydro_2d (22 kernels and 19 ghost fills, each followed by a
+    device synchronisation, and the dt read back) -- with its errors against
+    the fused step after the same steps."""
+    import ctypes
+    from oracle import oracle as O
+    if not O.have_reference_cuda():
+        return {"unavailable": "the reference's cuda set was not built here (its sources "
+                               "were not staged to this machine)"}
+    Lr = O.lib("reference_cuda")
+    sim = fg.DeviceSim(main_problem(problems, workload, n), device)
+    m = sim.mesh
+    mp = ctypes.cast(ctypes.addressof(m), ctypes.POINTER(O.Mesh))
+    args = sim.args()
+    with quiet_stdout():
+        Lr.set_timestep(sim.nx, sim.ny, args[8], args[9], args[1], args[3], mp, args[16], 0,
+                        m.celldx, m.celldy)
+        for tt in range(warmup):
+            Lr.solve_hydro_2d(mp, tt, *args)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for tt in range(warmup, warmup + steps):
+            Lr.solve_hydro_2d(mp, tt, *args)
+        torch.cuda.synchronize()
+        el = time.perf_counter() - t0
+    value = n * n * steps / el
+    ref = fg.DeviceSim(main_problem(problems, workload, n), device)
+    ref.initial_timestep()
+    ref.run(warmup + steps)
+    errs = field_errors(fg, sim, ref, names=STATE)
+    del sim, ref
+    torch.cuda.empty_cache()
+    return {"workload": f"{workload}_{n}_fp64", "value": value, "unit": UNIT,
+            "ms_per_step": el * 1e3 / steps, "steps": steps, "warmup": warmup,
+            "what": "the reference's cuda set (cuda/flow.cu, cuda/flow.k) for sm_103a, host-timed",
+            "fused_fp64_over_reference_cuda": fused_value / value,
+            "errors_vs_fused_fp64": errs}
 
 
 def mixed_problem(problems, workload, n):
@@ -660,6 +738,9 @@ def run_gpu(args):
     forms = {}
     oracle_checks = []
     if not args.fp64_only:
+        forms["reference_cuda"] = run_reference_cuda(fg, problems, torch, device, n,
+                                                     min(args.steps, 50), 2, args.workload,
+                                                     value / world)
         if args.workload != "smooth":
             forms["fp64_smooth"] = run_fp64_smooth(fg, problems, torch, device, n,
                                                    min(args.steps, 100), args.warmup, figures,
@@ -704,13 +785,13 @@ def run_gpu(args):
 
     cpu = None
     if host_legs:
-        cv, timed, threads = cpu_run(n, args.steps, 1, budget_s=60.0, workload=args.workload)
-        cpu = {"value": cv, "unit": UNIT, "cores": threads, "kind": "port",
+        cv, timed, threads, kind = cpu_run(n, args.steps, 1, budget_s=60.0,
+                                           workload=args.workload)
+        cpu = {"value": cv, "unit": UNIT, "cores": threads,
+               "kind": "reference" if kind == "reference_default" else "port",
                "sample": f"{args.workload} {n}^2 FP64 timesteps + conservation totals, {timed} "
-                         f"of the GPU arm's {args.steps} steps, on {threads} host threads (the "
-                         "oracle, a C restatement of the reference omp3 set that the tests hold "
-                         "bit-identical to it, built -O3 -march=native -fopenmp as the "
-                         "reference's Makefile:15)"}
+                         f"of the GPU arm's {args.steps} steps, on {threads} host threads "
+                         f"({CPU_WHAT[kind]})"}
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,

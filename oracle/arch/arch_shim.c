@@ -301,6 +301,7 @@ void finalise_shared_data(SharedData* shared_data) {
  * filled first over the interior rows; the y walls then copy whole rows, so
  * corner ghosts are double mirrors.  PACK (the MPI halo exchange) has no
  * effect on one rank. */
+#ifndef FLOW_SHIM_DEVICE_BOUNDARY  /* the cuda set's fill is arch_cuda.cu's */
 void handle_boundary_2d(const int nx, const int ny, Mesh* mesh, double* arr,
                         const int invert, const int pack) {
   (void)pack;
@@ -347,6 +348,7 @@ void handle_boundary_2d(const int nx, const int ny, Mesh* mesh, double* arr,
     }
   }
 }
+#endif
 
 int within_tolerance(const double expected, const double actual,
                      const double tolerance) {

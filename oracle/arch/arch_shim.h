@@ -70,6 +70,9 @@ extern struct Profile comms_profile;
 #define STOP_PROFILING(profile, name) ((void)(profile), (void)(name))
 #define PRINT_PROFILING_RESULTS(profile) ((void)(profile))
 
+/* Under nvcc (the reference's cuda set, built with cuda/shared.h) CUDA's own
+ * min overloads and the device minmod of cuda/shared.h take their place. */
+#ifndef __CUDACC__
 /* Ordinary minimum: the first argument when it is strictly smaller. */
 static inline double min(const double a, const double b) {
   return (a < b) ? a : b;
@@ -83,6 +86,7 @@ static inline double minmod(const double a, const double b) {
   }
   return 0.0;
 }
+#endif
 
 /* --- params --------------------------------------------------------------- */
 int get_int_parameter(const char* key, const char* filename);

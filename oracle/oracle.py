@@ -79,13 +79,20 @@ def have_reference() -> bool:
     return os.path.exists(os.path.join(HERE, "_ref", "libflow_ref.so"))
 
 
+def have_reference_cuda() -> bool:
+    return os.path.exists(os.path.join(HERE, "_ref", "libflow_ref_cuda.so"))
+
+
 def lib(kind: str = "port") -> ctypes.CDLL:
     """``port`` (strict restatement), ``fast`` (timed flags), ``reference``
-    (omp3/flow.c, strict IEEE evaluation) or ``reference_default`` (omp3/flow.c
-    with the reference's default -O3 -march=native flags)."""
+    (omp3/flow.c, strict IEEE evaluation), ``reference_default`` (omp3/flow.c
+    with the reference's default -O3 -march=native flags) or
+    ``reference_cuda`` (the reference's cuda set for sm_103a: the same entry
+    points over device arrays)."""
     return _load({"port": "libflow_oracle.so", "fast": "libflow_oracle_fast.so",
                   "reference": os.path.join("_ref", "libflow_ref.so"),
-                  "reference_default": os.path.join("_ref", "libflow_ref_default.so")}[kind])
+                  "reference_default": os.path.join("_ref", "libflow_ref_default.so"),
+                  "reference_cuda": os.path.join("_ref", "libflow_ref_cuda.so")}[kind])
 
 
 def _declare(lib: ctypes.CDLL) -> None:
@@ -109,6 +116,8 @@ def _declare(lib: ctypes.CDLL) -> None:
         "handle_boundary_2d": [I, I, M, P, I, I],
     }
     for name, args in sig.items():
+        if not hasattr(lib, name):  # the cuda set has no host stage functions
+            continue
         fn = getattr(lib, name)
         fn.argtypes = args
         fn.restype = None
