@@ -114,14 +114,19 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
+# The translation unit of the single-problem timestep kernels (fused.cu and
+# everything it includes): the sources the committed ncu figures describe.
+STEP_SOURCES = ("common.cuh", "fused.cu", "fused.h", "fused_math.cuh", "fused_tiles.cuh",
+                "lag_fused.cuh", "precision.cuh", "profile.h", "stages.h")
+
+
 def source_fingerprint() -> str:
-    """sha256 (16 hex digits) of the kernel sources, in name order."""
+    """sha256 (16 hex digits) of the timestep kernels' sources, in name order."""
     h = hashlib.sha256()
     csrc = os.path.join(ROOT, "flow_gb300", "csrc")
-    for name in sorted(os.listdir(csrc)):
-        if name.endswith((".cu", ".cuh", ".h")):
-            with open(os.path.join(csrc, name), "rb") as f:
-                h.update(name.encode() + b"\0" + f.read())
+    for name in STEP_SOURCES:
+        with open(os.path.join(csrc, name), "rb") as f:
+            h.update(name.encode() + b"\0" + f.read())
     return h.hexdigest()[:16]
 
 

@@ -32,7 +32,11 @@ constexpr double kCT = 0.3;
 //                             double: bit order = value order)
 //   [7] mesh power-of-two     1 when every mesh spacing is a power of two
 //                             (formed on the device at the start of a step)
-//   [8 ...]                   per-block partials (2 doubles per block)
+//   [8 ...]                   per-block partials (2 doubles per block, at
+//                             most kMaxReduceBlocks blocks)
+//   [kRaQFlags ...]           viscous-stress flags of the fused step (one
+//                             byte per 32 interior cells of a row), when the
+//                             array is large enough to hold them
 enum : int {
   kRaDt = 0,
   kRaDtH = 1,
@@ -45,6 +49,7 @@ enum : int {
   kRaPartial = 8,
 };
 constexpr int kMaxReduceBlocks = 1024;
+constexpr int kRaQFlags = kRaPartial + 2 * kMaxReduceBlocks;
 
 // Ghost-fill modes of handle_boundary_2d (arch; omp3/flow.c:156).
 enum : int { kNoInvert = 0, kInvertX = 1, kInvertY = 2 };

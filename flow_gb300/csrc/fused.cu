@@ -68,26 +68,29 @@ __global__ void __launch_bounds__(kCols) k_lag_pressure(const StepArgs<R> a) {
   }
   tile_lag_pressure(a, blockIdx.x, blockIdx.y);
 }
-template <typename R>
+// kFlags: the viscous-stress flags (a.qmask) are kept -- the viscosity
+// kernel stores only warp rows with a non-zero stress, and the two kernels
+// after it load only those.
+template <typename R, bool kFlags>
 __global__ void __launch_bounds__(kCols) k_lag_viscosity(const StepArgs<R> a) {
   pdl_wait();
   pdl_trigger();
-  tile_lag_viscosity(a, blockIdx.x, blockIdx.y);
+  tile_lag_viscosity<R, kFlags>(a, blockIdx.x, blockIdx.y);
 }
-template <typename R>
+template <typename R, bool kFlags>
 __global__ void __launch_bounds__(kCols) k_lag_viscous_accel(const StepArgs<R> a) {
   pdl_wait();
   pdl_trigger();
-  tile_lag_viscous_accel(a, blockIdx.x, blockIdx.y);
+  tile_lag_viscous_accel<R, true, kFlags>(a, blockIdx.x, blockIdx.y);
 }
 // Shock heating + CFL minimum; the last block to finish (ticket in
 // reduce_array) applies the dt rule.
-template <typename R>
+template <typename R, bool kFlags>
 __global__ void __launch_bounds__(kCols) k_lag_energy_dt(const StepArgs<R> a) {
   __shared__ bool s_last;
   pdl_wait();
   pdl_trigger();
-  tile_lag_energy_dt(a, blockIdx.x, blockIdx.y);
+  tile_lag_energy_dt<R, true, kFlags>(a, blockIdx.x, blockIdx.y);
   if (threadIdx.x == 0) {
     __threadfence();
     unsigned long long* ticket = reinterpret_cast<unsigned long long*>(a.ra + kRaTicket);
@@ -338,13 +341,16 @@ void launch_step(cudaStream_t s, const StepArgs<R>& a, int tt,
   } else {
     prof.mark("lag_pressure");
     launch_pdl(k_lag_pressure<R>, strip_grid(nx, ny, a.rows), s, a);
+    const bool fl = a.qmask != nullptr;
     prof.mark("lag_viscosity");
-    launch_pdl(k_lag_viscosity<R>, strip_grid(nx - 2 * pad, ny - 2 * pad, a.rows), s, a);
+    launch_pdl(fl ? k_lag_viscosity<R, true> : k_lag_viscosity<R, false>,
+               strip_grid(nx - 2 * pad, ny - 2 * pad, a.rows), s, a);
     prof.mark("lag_viscous_accel");
-    launch_pdl(k_lag_viscous_accel<R>, strip_grid(nx + 1 - 2 * pad, ny + 1 - 2 * pad, a.rows), s,
-               a);
+    launch_pdl(fl ? k_lag_viscous_accel<R, true> : k_lag_viscous_accel<R, false>,
+               strip_grid(nx + 1 - 2 * pad, ny + 1 - 2 * pad, a.rows), s, a);
     prof.mark("lag_energy_dt");
-    launch_pdl(k_lag_energy_dt<R>, strip_grid(nx - 2 * pad, ny - 2 * pad, a.rows), s, a);
+    launch_pdl(fl ? k_lag_energy_dt<R, true> : k_lag_energy_dt<R, false>,
+               strip_grid(nx - 2 * pad, ny - 2 * pad, a.rows), s, a);
   }
 
   const bool x_first = (tt % 2 == 0);
@@ -421,6 +427,18 @@ void fill_mesh_args(StepArgs<R>& a, const Mesh* mesh, int tt, double* ra) {
   a.max_dt = mesh->max_dt;
   a.first_step = (tt == 0);
   a.rows = kDefaultRows;
+  // The viscous-stress flags live in reduce_array after the reduction
+  // partials when it holds them (it has nx*ny doubles, as the arch layer
+  // allocates it); a mesh too small for them stores and reads every stress.
+  a.qmask = nullptr;
+  a.qm_stride = 0;
+  const int stride = (a.nx - 2 * a.pad + kCols - 1) / kCols;
+  const long long rows = a.ny - 2 * a.pad;
+  const size_t need = (size_t)kRaQFlags * sizeof(double) + (size_t)rows * stride * sizeof(unsigned);
+  if (stride > 0 && rows > 0 && need <= (size_t)a.nx * a.ny * sizeof(double)) {
+    a.qmask = reinterpret_cast<unsigned*>(ra + kRaQFlags);
+    a.qm_stride = stride;
+  }
 }
 
 }  // namespace

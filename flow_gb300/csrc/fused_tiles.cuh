@@ -82,6 +82,14 @@ struct StepArgs {
   double dt, dt_h, max_dt;     // Lagrangian-phase pair (host values), max_dt
   int first_step;
   int rows;                    // tile height, 1 .. kMaxRows
+  // Viscous-stress flags, or null.  Byte w of word (ii - pad) * qm_stride + bx
+  // is 1 when a stress (Qxx or Qyy) of the 32 cells of warp w of column tile
+  // bx in interior row ii is not +0: the viscosity kernel stored that warp
+  // row's stresses and their ghost images.  0: every one of them is +0 and
+  // nothing was stored (the arrays hold older values there); the readers
+  // take +0 without loading.  Null: every stress is stored and read.
+  unsigned* qmask;
+  int qm_stride;               // words per interior row: ceil((nx - 2 pad) / kCols)
 };
 
 // Writes the value of interior point (ii, jj) of a w x h array into each of
@@ -194,6 +202,23 @@ __device__ __forceinline__ bool warp_zeros(R a, R b) {
     return warp_all(d_is_zero(a) && d_is_zero(b));
   }
 }
+// x is +0 (all bits zero).
+template <typename R>
+__device__ __forceinline__ bool is_plus_zero(R x) {
+  if constexpr (Prec<R>::kMixed) {
+    return __float_as_uint(x) == 0u;
+  } else {
+    return dbits(x) == 0;
+  }
+}
+// The viscous-stress flag of cell column col (interior) in the flag word of
+// its column tile; word0 / word1 hold the words of tiles bx - 1 and bx.
+__device__ __forceinline__ bool qflag(unsigned word0, unsigned word1, int col, int pad, int bx) {
+  const int g = (col - pad) >> 5;
+  const unsigned w = ((g >> 2) == bx) ? word1 : word0;
+  return ((w >> (8 * (g & 3))) & 0xffu) != 0u;
+}
+
 // The IEEE sum of two zeros: -0 only when both are -0.
 template <typename R>
 __device__ __forceinline__ R sum_zeros(R a, R b) {
@@ -494,15 +519,30 @@ __device__ __forceinline__ R visc_stress(R rho, const R* w, R mid, R hi) {
   return R(-kCQ) * rho * m1 * Pr::half(Pr::abs(m2 - m1) + Pr::abs(m1 - m0));
 }
 
-template <typename R>
+// kFlags: a.qmask is set -- a warp row whose stresses are all +0 stores only
+// its flag (the single-problem kernels; the batched kernels keep no flags).
+template <typename R, bool kFlags = false>
 __device__ __forceinline__ void tile_lag_viscosity(const StepArgs<R>& a, int bx, int by) {
   const int nx = a.nx, ny = a.ny, pad = a.pad;
   const int jj = pad + bx * kCols + threadIdx.x;
   const int i0 = pad + by * a.rows;
   const bool edge = tile_near_edge(nx, ny, pad, pad + bx * kCols, i0, a.rows);
-  if (jj >= nx - pad) return;
   using Pr = Prec<R>;
   const int i1 = min(i0 + a.rows, ny - pad);
+  // This warp's stress-flag byte of row i0, or null without flags.
+  unsigned char* qf =
+      kFlags ? reinterpret_cast<unsigned char*>(a.qmask + (size_t)(i0 - pad) * a.qm_stride + bx) +
+                    (threadIdx.x >> 5)
+              : nullptr;
+  const int qf_step = 4 * a.qm_stride;
+  if (jj >= nx - pad) {
+    // A warp wholly right of the interior clears its flags (none are read,
+    // but the viscous-acceleration tile's early exit looks at whole words).
+    if (kFlags && (threadIdx.x & 31) == 0) {
+      for (int ii = i0; ii < i1; ++ii, qf += qf_step) *qf = 0;
+    }
+    return;
+  }
   // The y stress of row ii uses the limited jumps m0, m1, m2 of v around the
   // cell and |m1 - m0|, |m2 - m1|; the next row reuses three of those, so
   // they are carried down the column (same operands, same values).
@@ -540,10 +580,20 @@ __device__ __forceinline__ void tile_lag_viscosity(const StepArgs<R>& a, int bx,
       g12 = Pr::abs(m2 - m1);
       qy = Pr::zero_skip(m1) ? R(0) : R(-kCQ) * rho * m1 * Pr::half(g12 + g01);
     }
-    a.Qxx[c] = qx;
-    a.Qyy[c] = qy;
-    mirror(edge, a.Qxx, nx, ny, pad, ii, jj, qx, false, false);
-    mirror(edge, a.Qyy, nx, ny, pad, ii, jj, qy, false, false);
+    // With flags, a warp row whose stresses are all +0 (the still regions)
+    // stores none of them, only its flag.
+    bool store = true;
+    if constexpr (kFlags) {
+      store = __any_sync(__activemask(), !(is_plus_zero(qx) && is_plus_zero(qy)));
+      if ((threadIdx.x & 31) == 0) *qf = store ? 1 : 0;
+      qf += qf_step;
+    }
+    if (store) {
+      a.Qxx[c] = qx;
+      a.Qyy[c] = qy;
+      mirror(edge, a.Qxx, nx, ny, pad, ii, jj, qx, false, false);
+      mirror(edge, a.Qyy, nx, ny, pad, ii, jj, qy, false, false);
+    }
     m0 = m1;
     m1 = m2;
     g01 = g12;
@@ -553,13 +603,17 @@ __device__ __forceinline__ void tile_lag_viscosity(const StepArgs<R>& a, int bx,
 
 // Viscous acceleration of the face momenta and velocities,
 // omp3/flow.c:212-244.  The face densities are formed again where needed.
-// kEarly: the first row's loads are issued before the barrier that publishes
-// the row tables (off in the persistent batched kernel, whose register budget
-// is spent across all its phases).
-template <typename R, bool kP2, bool kEarly>
+// kEarly: the stresses stream through a ring of asynchronous copies (off in
+// the persistent batched kernel, whose register budget is spent across all
+// its phases).  With stress flags, a tile none of whose stresses can be
+// non-zero returns at once, and a stress flagged +0 is not loaded.
+template <typename R, bool kP2, bool kEarly, bool kFlags>
 __device__ __forceinline__ void tile_lag_viscous_accel_impl(const StepArgs<R>& a, int bx, int by) {
   using Pr = Prec<R>;
   __shared__ R s_cy[kMaxRows], s_icy[kMaxRows], s_wy0[kMaxRows], s_wy1[kMaxRows];
+  // Stress flags (a.qmask) of rows i0 - 1 .. i1 - 1, each row taken at its
+  // mirror source: the words of column tiles bx - 1 and bx.
+  __shared__ unsigned s_qf[kMaxRows + 1][2];
   const int nx = a.nx, ny = a.ny, pad = a.pad;
   const int jj = pad + bx * kCols + threadIdx.x;
   const int i0 = pad + by * a.rows;
@@ -575,6 +629,38 @@ __device__ __forceinline__ void tile_lag_viscous_accel_impl(const StepArgs<R>& a
   }
   const bool col_ok = jj < nx + 1 - pad;
   const int i1 = min(i0 + a.rows, ny + 1 - pad);
+  // Whether any stress this tile reads may be non-zero (block-uniform).
+  bool any_q = true;
+  // The flag of a stress, taken at the mirror source of its cell.
+  auto src_row = [&](int r) {
+    return r < pad ? 2 * pad - 1 - r : (r >= ny - pad ? 2 * (ny - pad) - 1 - r : r);
+  };
+  auto src_col = [&](int c) {
+    return c < pad ? 2 * pad - 1 - c : (c >= nx - pad ? 2 * (nx - pad) - 1 - c : c);
+  };
+  if constexpr (kFlags) {
+    unsigned w0 = 0u, w1 = 0u;
+    const int k = threadIdx.x;
+    if (k <= i1 - i0) {
+      const unsigned* row = a.qmask + (size_t)(src_row(i0 - 1 + k) - pad) * a.qm_stride;
+      w0 = bx >= 1 ? row[bx - 1] : 0u;
+      w1 = bx < a.qm_stride ? row[bx] : 0u;
+      s_qf[k][0] = w0;
+      s_qf[k][1] = w1;
+    }
+    // Tile bx reads the flags of its own groups and the last group of tile
+    // bx - 1 (the stress left of its first face).  (The barrier also
+    // publishes the row tables.)
+    any_q = __syncthreads_or((w1 | (w0 & 0xff000000u)) != 0u) != 0;
+  } else {
+    __syncthreads();
+  }
+  auto flag_x = [&](int ii, int col) {  // Qxx(ii, col), ii an interior row
+    return !kFlags || qflag(s_qf[ii - i0 + 1][0], s_qf[ii - i0 + 1][1], src_col(col), pad, bx);
+  };
+  auto flag_y = [&](int ii) {  // Qyy(ii, jj), ii in i0 - 1 .. i1 - 1
+    return !kFlags || qflag(s_qf[ii - i0 + 1][0], s_qf[ii - i0 + 1][1], jj, pad, bx);
+  };
   // kEarly (the fused kernel): the stresses stream through a shared-memory
   // ring, below.  Otherwise (the batched kernel) row ii+1's are loaded into
   // registers before row ii is processed.
@@ -582,18 +668,18 @@ __device__ __forceinline__ void tile_lag_viscous_accel_impl(const StepArgs<R>& a
   auto load = [&](int ii) {
     const size_t c = cidx(nx, ii, jj);
     if (ii < ny - pad) {
-      q1_n = a.Qxx[c];
-      q0_n = a.Qxx[c - 1];
+      q1_n = flag_x(ii, jj) ? a.Qxx[c] : R(0);
+      q0_n = flag_x(ii, jj - 1) ? a.Qxx[c - 1] : R(0);
     }
-    if (jj < nx - pad) qy_n = a.Qyy[c];
+    if (jj < nx - pad) qy_n = flag_y(ii) ? a.Qyy[c] : R(0);
   };
   auto prime = [&]() {
-    if (jj < nx - pad) qy_dn = a.Qyy[cidx(nx, i0 - 1, jj)];
+    if (jj < nx - pad && flag_y(i0 - 1)) qy_dn = a.Qyy[cidx(nx, i0 - 1, jj)];
     if (!kEarly && i0 < i1) load(i0);
   };
-  if (kEarly && col_ok) prime();
-  __syncthreads();
-  if (!col_ok) return;
+  // No stress gradient anywhere in the tile: momenta and velocities stand.
+  if (!any_q || !col_ok) return;
+  if (kEarly) prime();
   const R cx = geo_v<R>(a.celldx[jj]);
   const R icx = geo_rcp<R, kP2>(a.celldx[jj]);
   // Face-density weights (the pressure phase's): where a stress gradient
@@ -652,9 +738,11 @@ __device__ __forceinline__ void tile_lag_viscous_accel_impl(const StepArgs<R>& a
       const int sl = (ii - i0) % kSlots;
       const size_t c = cidx(nx, ii, jj);
       const bool xq = ii < ny - pad, yq = jj < nx - pad;
-      cp_async_elem(&s_q[sl][0][t], xq ? a.Qxx + c : a.Qxx, xq);
-      cp_async_elem(&s_q[sl][1][t], xq ? a.Qxx + c - 1 : a.Qxx, xq);
-      cp_async_elem(&s_q[sl][2][t], yq ? a.Qyy + c : a.Qyy, yq);
+      const bool x1 = xq && flag_x(ii, jj), x0 = xq && flag_x(ii, jj - 1);
+      const bool y0 = yq && flag_y(ii);
+      cp_async_elem(&s_q[sl][0][t], x1 ? a.Qxx + c : a.Qxx, x1);
+      cp_async_elem(&s_q[sl][1][t], x0 ? a.Qxx + c - 1 : a.Qxx, x0);
+      cp_async_elem(&s_q[sl][2][t], y0 ? a.Qyy + c : a.Qyy, y0);
     };
 #pragma unroll
     for (int d = 0; d < kAhead; ++d) {
@@ -679,11 +767,11 @@ __device__ __forceinline__ void tile_lag_viscous_accel_impl(const StepArgs<R>& a
   }
 }
 
-template <typename R, bool kEarly = true>
+template <typename R, bool kEarly = true, bool kFlags = false>
 __device__ __forceinline__ void tile_lag_viscous_accel(const StepArgs<R>& a, int bx, int by) {
   FLOW_POW2_DISPATCH(R, a, a.pad + bx * kCols, a.pad + by * a.rows,
-                     (tile_lag_viscous_accel_impl<R, true, kEarly>(a, bx, by)),
-                     (tile_lag_viscous_accel_impl<R, false, kEarly>(a, bx, by)));
+                     (tile_lag_viscous_accel_impl<R, true, kEarly, kFlags>(a, bx, by)),
+                     (tile_lag_viscous_accel_impl<R, false, kEarly, kFlags>(a, bx, by)));
 }
 
 __device__ __forceinline__ unsigned long long warp_min_u64(unsigned long long x) {
@@ -700,12 +788,13 @@ __device__ __forceinline__ unsigned long long warp_min_u64(unsigned long long x)
 // block on the FP64 bit pattern of its smallest candidate; the last block to
 // finish applies the leapfrog dt/dt_h rule (finish_dt).  In the mixed form
 // the FP32 energy change is added to the FP64 energy.
-template <typename R, bool kP2, bool kRing>
+template <typename R, bool kP2, bool kRing, bool kFlags>
 __device__ __forceinline__ void tile_lag_energy_dt_impl(const StepArgs<R>& a, int bx, int by) {
   using Pr = Prec<R>;
   __shared__ R s_icy[kMaxRows], s_cy[kMaxRows];
   __shared__ double s_icy2[kMaxRows];
   __shared__ unsigned long long s_warp[kCols / 32];
+  __shared__ unsigned s_qf[kMaxRows];  // stress-flag words of the tile's rows
   const int nx = a.nx, ny = a.ny, pad = a.pad;
   const int jj = pad + bx * kCols + threadIdx.x;
   const int i0 = pad + by * a.rows;
@@ -717,8 +806,14 @@ __device__ __forceinline__ void tile_lag_energy_dt_impl(const StepArgs<R>& a, in
       s_icy[threadIdx.x] = geo_rcp<R, kP2>(a.celldy[ii]);
       if constexpr (!Pr::kMixed) s_icy2[threadIdx.x] = geo_rcp_sq<kP2>(a.celldy[ii]);
     }
+    if (kFlags && ii < ny - pad) s_qf[threadIdx.x] = a.qmask[(size_t)(ii - pad) * a.qm_stride + bx];
   }
   __syncthreads();
+  // Whether the stresses of this thread's warp in tile row k may be non-zero
+  // (flagged +0: not loaded, taken as +0).
+  auto qflag_row = [&](int k) {
+    return !kFlags || ((s_qf[k] >> (8 * (threadIdx.x >> 5))) & 0xffu) != 0u;
+  };
   unsigned long long best = ~0ull;
   // FP64 form: the thread's largest 1/dt^2 key so far, with its S and spacing.
   long long kbest = -1;
@@ -749,8 +844,9 @@ __device__ __forceinline__ void tile_lag_energy_dt_impl(const StepArgs<R>& a, in
       v1_n = a.v[c + nx];
       r_n = a.rho_r[c];
       er_n = a.e_r[c];
-      qx_n = a.Qxx[c];
-      qy_n = a.Qyy[c];
+      const bool qf = qflag_row(ii - i0);
+      qx_n = qf ? a.Qxx[c] : R(0);
+      qy_n = qf ? a.Qyy[c] : R(0);
       u0_n = a.u[f];
       u1_n = a.u[f + 1];
     };
@@ -761,8 +857,9 @@ __device__ __forceinline__ void tile_lag_energy_dt_impl(const StepArgs<R>& a, in
       cp_async_elem(&s_in[sl][0][t], a.v + c + nx, true);
       cp_async_elem(&s_in[sl][1][t], a.rho_r + c, true);
       cp_async_elem(&s_in[sl][2][t], a.e_r + c, true);
-      cp_async_elem(&s_in[sl][3][t], a.Qxx + c, true);
-      cp_async_elem(&s_in[sl][4][t], a.Qyy + c, true);
+      const bool qf = qflag_row(ii - i0);
+      cp_async_elem(&s_in[sl][3][t], a.Qxx + c, qf);
+      cp_async_elem(&s_in[sl][4][t], a.Qyy + c, qf);
       cp_async_elem(&s_in[sl][5][t], a.u + f, true);
       cp_async_elem(&s_in[sl][6][t], a.u + f + 1, true);
     };
@@ -889,11 +986,11 @@ __device__ __forceinline__ void tile_lag_energy_dt_impl(const StepArgs<R>& a, in
   }
 }
 
-template <typename R, bool kRing = true>
+template <typename R, bool kRing = true, bool kFlags = false>
 __device__ __forceinline__ void tile_lag_energy_dt(const StepArgs<R>& a, int bx, int by) {
   FLOW_POW2_DISPATCH(R, a, a.pad + bx * kCols, a.pad + by * a.rows,
-                     (tile_lag_energy_dt_impl<R, true, kRing>(a, bx, by)),
-                     (tile_lag_energy_dt_impl<R, false, kRing>(a, bx, by)));
+                     (tile_lag_energy_dt_impl<R, true, kRing, kFlags>(a, bx, by)),
+                     (tile_lag_energy_dt_impl<R, false, kRing, kFlags>(a, bx, by)));
 }
 
 // The leapfrog dt/dt_h rule of omp3/flow.c:103-105 applied to the finished
