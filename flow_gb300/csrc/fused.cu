@@ -103,33 +103,36 @@ __global__ void __launch_bounds__(kCols) k_lag_energy_dt(const StepArgs<R> a) {
     *reinterpret_cast<unsigned long long*>(a.ra + kRaTicket) = 0ull;
   }
 }
-template <typename R, bool kFirst>
+// kFl (sweeps and momentum pairs): the mass-flux flags (a.fxflag, a.fyflag)
+// are kept -- the sweeps store only warps with a non-zero mass flux, and the
+// momentum pairs load only those.
+template <typename R, bool kFirst, bool kFl>
 __global__ void __launch_bounds__(kCols, Prec<R>::kMixed ? 8 : 7) k_mass_sweep_x(const StepArgs<R> a,
                                                         const SweepArgs<R> s) {
   pdl_wait();
   pdl_trigger();
-  tile_mass_sweep_x<R, kFirst>(a, s, blockIdx.x, blockIdx.y);
+  tile_mass_sweep_x<R, kFirst, true, kFl>(a, s, blockIdx.x, blockIdx.y);
 }
-template <typename R, bool kFirst>
+template <typename R, bool kFirst, bool kFl>
 __global__ void __launch_bounds__(kCols, Prec<R>::kMixed ? 7 : 6) k_mass_sweep_y(const StepArgs<R> a,
                                                         const SweepArgs<R> s) {
   pdl_wait();
   pdl_trigger();
-  tile_mass_sweep_y<R, kFirst>(a, s, blockIdx.x, blockIdx.y);
+  tile_mass_sweep_y<R, kFirst, true, kFl>(a, s, blockIdx.x, blockIdx.y);
 }
 // Momentum pairs (flux fused with its update): x pairs share a row's fluxes
 // through shared memory (127 faces per CTA), y pairs march down columns.
-template <typename R, bool kV, bool kVel>
+template <typename R, bool kV, bool kVel, bool kFl>
 __global__ void __launch_bounds__(kCols) k_mom_x(const StepArgs<R> a) {
   pdl_wait();
   pdl_trigger();
-  tile_mom_x<R, kV, kVel>(a, blockIdx.x, blockIdx.y);
+  tile_mom_x<R, kV, kVel, true, kFl>(a, blockIdx.x, blockIdx.y);
 }
-template <typename R, bool kV, bool kVel>
+template <typename R, bool kV, bool kVel, bool kFl>
 __global__ void __launch_bounds__(kCols) k_mom_y(const StepArgs<R> a) {
   pdl_wait();
   pdl_trigger();
-  tile_mom_y<R, kV, kVel>(a, blockIdx.x, blockIdx.y);
+  tile_mom_y<R, kV, kVel, true, kFl>(a, blockIdx.x, blockIdx.y);
 }
 
 // The whole Lagrangian phase of the FP64 step in one kernel (lag_fused.cuh):
@@ -279,17 +282,34 @@ inline dim3 strip_grid(int cols, int rows, int tile_rows, int cols_per_cta = kCo
 
 // x pair for rho_u (kV false): x-faces pad .. nx-pad, 127 per CTA; for rho_v:
 // y-faces pad .. nx-pad-1.  Rows: the faces' rows.
+// Tile heights of the momentum pairs (with and without the velocity
+// update) and of the viscous acceleration: the pairs without a velocity
+// update and the viscous update skip the still tiles (flags) and work only
+// where the flow moves, and shorter tiles there shorten the longest tile's
+// chain of rows, which bounds such a kernel.
+constexpr int kRowsMomVel = 16, kRowsMomFlux = 8, kRowsAccel = 8;
+template <typename R>
+StepArgs<R> with_rows(const StepArgs<R>& a, int rows) {
+  StepArgs<R> b = a;
+  b.rows = rows;
+  return b;
+}
+
 template <typename R, bool kV, bool kVel>
-void launch_mom_x(cudaStream_t s, const StepArgs<R>& a) {
+void launch_mom_x(cudaStream_t s, const StepArgs<R>& a0) {
+  const StepArgs<R> a = with_rows(a0, kVel ? kRowsMomVel : kRowsMomFlux);
   const int cols = kV ? (a.nx - 2 * a.pad) : (a.nx + 1 - 2 * a.pad);
   const int rows = kV ? (a.ny + 1 - 2 * a.pad) : (a.ny - 2 * a.pad);
-  launch_pdl(k_mom_x<R, kV, kVel>, strip_grid(cols, rows, a.rows, kCols - 1), s, a);
+  launch_pdl(a.fxflag ? k_mom_x<R, kV, kVel, true> : k_mom_x<R, kV, kVel, false>,
+             strip_grid(cols, rows, a.rows, kCols - 1), s, a);
 }
 template <typename R, bool kV, bool kVel>
-void launch_mom_y(cudaStream_t s, const StepArgs<R>& a) {
+void launch_mom_y(cudaStream_t s, const StepArgs<R>& a0) {
+  const StepArgs<R> a = with_rows(a0, kVel ? kRowsMomVel : kRowsMomFlux);
   const int cols = kV ? (a.nx - 2 * a.pad) : (a.nx + 1 - 2 * a.pad);
   const int rows = kV ? (a.ny + 1 - 2 * a.pad) : (a.ny - 2 * a.pad);
-  launch_pdl(k_mom_y<R, kV, kVel>, strip_grid(cols, rows, a.rows), s, a);
+  launch_pdl(a.fyflag ? k_mom_y<R, kV, kVel, true> : k_mom_y<R, kV, kVel, false>,
+             strip_grid(cols, rows, a.rows), s, a);
 }
 
 template <typename R>
@@ -297,14 +317,24 @@ void launch_mass(cudaStream_t s, const StepArgs<R>& a, bool dir_y, bool first,
                  const SweepArgs<R>& sw) {
   const int pad = a.pad;
   if (dir_y) {
+    const bool fl = a.fyflag != nullptr;
     const dim3 g = strip_grid(a.nx - 2 * pad, a.ny - 2 * pad, a.rows);
-    if (first) launch_pdl(k_mass_sweep_y<R, true>, g, s, a, sw);
-    else launch_pdl(k_mass_sweep_y<R, false>, g, s, a, sw);
+    if (first) {
+      launch_pdl(fl ? k_mass_sweep_y<R, true, true> : k_mass_sweep_y<R, true, false>, g, s, a, sw);
+    } else {
+      launch_pdl(fl ? k_mass_sweep_y<R, false, true> : k_mass_sweep_y<R, false, false>, g, s, a,
+                 sw);
+    }
   } else {
+    const bool fl = a.fxflag != nullptr;
     // Faces pad .. nx-pad; every CTA advances 127 columns.
     const dim3 g = strip_grid(a.nx + 1 - 2 * pad, a.ny - 2 * pad, a.rows, kCols - 1);
-    if (first) launch_pdl(k_mass_sweep_x<R, true>, g, s, a, sw);
-    else launch_pdl(k_mass_sweep_x<R, false>, g, s, a, sw);
+    if (first) {
+      launch_pdl(fl ? k_mass_sweep_x<R, true, true> : k_mass_sweep_x<R, true, false>, g, s, a, sw);
+    } else {
+      launch_pdl(fl ? k_mass_sweep_x<R, false, true> : k_mass_sweep_x<R, false, false>, g, s, a,
+                 sw);
+    }
   }
 }
 
@@ -346,8 +376,9 @@ void launch_step(cudaStream_t s, const StepArgs<R>& a, int tt,
     launch_pdl(fl ? k_lag_viscosity<R, true> : k_lag_viscosity<R, false>,
                strip_grid(nx - 2 * pad, ny - 2 * pad, a.rows), s, a);
     prof.mark("lag_viscous_accel");
+    const StepArgs<R> aa = with_rows(a, kRowsAccel);
     launch_pdl(fl ? k_lag_viscous_accel<R, true> : k_lag_viscous_accel<R, false>,
-               strip_grid(nx + 1 - 2 * pad, ny + 1 - 2 * pad, a.rows), s, a);
+               strip_grid(nx + 1 - 2 * pad, ny + 1 - 2 * pad, aa.rows), s, aa);
     prof.mark("lag_energy_dt");
     launch_pdl(fl ? k_lag_energy_dt<R, true> : k_lag_energy_dt<R, false>,
                strip_grid(nx - 2 * pad, ny - 2 * pad, a.rows), s, a);
@@ -427,17 +458,31 @@ void fill_mesh_args(StepArgs<R>& a, const Mesh* mesh, int tt, double* ra) {
   a.max_dt = mesh->max_dt;
   a.first_step = (tt == 0);
   a.rows = kDefaultRows;
-  // The viscous-stress flags live in reduce_array after the reduction
-  // partials when it holds them (it has nx*ny doubles, as the arch layer
-  // allocates it); a mesh too small for them stores and reads every stress.
+  // The viscous-stress and mass-flux flags live in reduce_array after the
+  // reduction partials when it holds them (it has nx*ny doubles, as the arch
+  // layer allocates it); a mesh too small for them stores and reads every
+  // stress and flux.  Words: stresses (ny - 2 pad) x stride, y fluxes
+  // (ny + 1 - 2 pad) x stride, x fluxes (ny - 2 pad) x 4-byte words of
+  // x-sweep tiles.
   a.qmask = nullptr;
   a.qm_stride = 0;
+  a.fxflag = nullptr;
+  a.fyflag = nullptr;
+  a.fx_stride = 0;
   const int stride = (a.nx - 2 * a.pad + kCols - 1) / kCols;
+  const int xtiles = (a.nx + 1 - 2 * a.pad + kCols - 2) / (kCols - 1);
   const long long rows = a.ny - 2 * a.pad;
-  const size_t need = (size_t)kRaQFlags * sizeof(double) + (size_t)rows * stride * sizeof(unsigned);
+  const size_t q_words = (size_t)rows * stride, fy_words = (size_t)(rows + 1) * stride;
+  const size_t fx_words = (size_t)rows * xtiles;
+  const size_t need =
+      (size_t)kRaQFlags * sizeof(double) + (q_words + fy_words + fx_words) * sizeof(unsigned);
   if (stride > 0 && rows > 0 && need <= (size_t)a.nx * a.ny * sizeof(double)) {
-    a.qmask = reinterpret_cast<unsigned*>(ra + kRaQFlags);
+    unsigned* base = reinterpret_cast<unsigned*>(ra + kRaQFlags);
+    a.qmask = base;
     a.qm_stride = stride;
+    a.fyflag = reinterpret_cast<unsigned char*>(base + q_words);
+    a.fxflag = reinterpret_cast<unsigned char*>(base + q_words + fy_words);
+    a.fx_stride = 4 * xtiles;
   }
 }
 

@@ -90,6 +90,16 @@ struct StepArgs {
   // take +0 without loading.  Null: every stress is stored and read.
   unsigned* qmask;
   int qm_stride;               // words per interior row: ceil((nx - 2 pad) / kCols)
+  // Mass-flux flags, or null (set together with qmask), in the same sense
+  // for the mass fluxes the sweeps store and the momentum pairs read:
+  //   fyflag: byte (ii - pad) * 4 qm_stride + 4 bx + w for y-face row ii
+  //     (pad .. ny - pad) and the 32 columns of warp w of column tile bx;
+  //   fxflag: byte (ii - pad) * fx_stride + 4 bx + w for interior row ii and
+  //     the faces pad + 127 bx + 32 w + lane (lane < 32, 32 w + lane < 127)
+  //     of warp w of x-sweep tile bx.
+  unsigned char* fxflag;
+  unsigned char* fyflag;
+  int fx_stride;               // bytes per row: 4 ceil((nx + 1 - 2 pad) / 127)
 };
 
 // Writes the value of interior point (ii, jj) of a w x h array into each of
@@ -202,6 +212,17 @@ __device__ __forceinline__ bool warp_zeros(R a, R b) {
     return warp_all(d_is_zero(a) && d_is_zero(b));
   }
 }
+// Stores a flag byte (every lane of a warp stores the same byte: one
+// transaction, and no divergent branch in the row loop).  An asm statement
+// without a memory clobber: a char
+// store may alias any object, and through a plain store the compiler would
+// have to assume that it changes the data a tile has loaded (and reload or
+// stop prefetching it).  No reader of a flag runs in the kernel that writes
+// it.
+__device__ __forceinline__ void store_flag(unsigned char* p, bool v) {
+  asm volatile("st.global.u8 [%0], %1;" ::"l"(p), "h"((unsigned short)(v ? 1 : 0)));
+}
+
 // x is +0 (all bits zero).
 template <typename R>
 __device__ __forceinline__ bool is_plus_zero(R x) {
@@ -539,7 +560,7 @@ __device__ __forceinline__ void tile_lag_viscosity(const StepArgs<R>& a, int bx,
     // A warp wholly right of the interior clears its flags (none are read,
     // but the viscous-acceleration tile's early exit looks at whole words).
     if (kFlags && (threadIdx.x & 31) == 0) {
-      for (int ii = i0; ii < i1; ++ii, qf += qf_step) *qf = 0;
+      for (int ii = i0; ii < i1; ++ii, qf += qf_step) store_flag(qf, false);
     }
     return;
   }
@@ -585,7 +606,7 @@ __device__ __forceinline__ void tile_lag_viscosity(const StepArgs<R>& a, int bx,
     bool store = true;
     if constexpr (kFlags) {
       store = __any_sync(__activemask(), !(is_plus_zero(qx) && is_plus_zero(qy)));
-      if ((threadIdx.x & 31) == 0) *qf = store ? 1 : 0;
+      store_flag(qf, store);
       qf += qf_step;
     }
     if (store) {
@@ -1281,7 +1302,7 @@ struct SweepArgs {
 // face is shared with the next CTA and written only by its owner).  In the
 // second sweep of a step the old density of a cell is read from rho just
 // before the same thread overwrites that cell.
-template <typename R, bool kFirst, bool kP2, bool kEarly>
+template <typename R, bool kFirst, bool kP2, bool kEarly, bool kFl>
 __device__ __forceinline__ void tile_mass_sweep_x_impl(const StepArgs<R>& a,
                                                        const SweepArgs<R>& s, int bx, int by) {
   using Pr = Prec<R>;
@@ -1384,20 +1405,25 @@ __device__ __forceinline__ void tile_mass_sweep_x_impl(const StepArgs<R>& a,
       if (ii + 1 < i1) load(ii + 1);
     }
     R F = R(0), eF = R(0);
-    if (face_ok) {
+    // Whether a face of the warp moves (a lane without a face holds +0): a
+    // warp whose faces are all at rest carries +0 fluxes.
+    const bool moves = !warp_all(Pr::is_zero(u0));
+    if (face_ok && moves) {
       const size_t f = fidx(nx, ii, jj);
       const size_t c = cidx(nx, ii, jj);
-      if (!warp_all(Pr::is_zero(u0))) {
-        mass_energy_flux<R, false, kP2>(a.u[f - 1], u0, a.u[f + 1], s.r_in_r[c - 2],
-                                        s.r_in_r[c - 1], s.r_in_r[c], s.r_in_r[c + 1],
-                                        s.e_in_r[c - 2], s.e_in_r[c - 1], s.e_in_r[c],
-                                        s.e_in_r[c + 1], iex, cxm, cx0, icx_r,
-                                        s_ey0r[k], dt_r, dt_h_r, &F, &eF);
-      }
-      if (face_owner) {
-        a.F_x[f] = F;
-        mirror(edge, a.F_x, nx + 1, ny, pad, ii, jj, F, true, false);
-      }
+      mass_energy_flux<R, false, kP2>(a.u[f - 1], u0, a.u[f + 1], s.r_in_r[c - 2],
+                                      s.r_in_r[c - 1], s.r_in_r[c], s.r_in_r[c + 1],
+                                      s.e_in_r[c - 2], s.e_in_r[c - 1], s.e_in_r[c],
+                                      s.e_in_r[c + 1], iex, cxm, cx0, icx_r,
+                                      s_ey0r[k], dt_r, dt_h_r, &F, &eF);
+    }
+    // kFl: a warp at rest stores only its flag (its fluxes are +0).
+    if constexpr (kFl) {
+      store_flag(a.fxflag + (size_t)(ii - pad) * a.fx_stride + 4 * bx + (t >> 5), moves);
+    }
+    if (face_owner && (!kFl || moves)) {
+      a.F_x[fidx(nx, ii, jj)] = F;
+      mirror(edge, a.F_x, nx + 1, ny, pad, ii, jj, F, true, false);
     }
     sF[t] = Pr::to_d(F);
     seF[t] = Pr::to_d(eF);
@@ -1417,17 +1443,17 @@ __device__ __forceinline__ void tile_mass_sweep_x_impl(const StepArgs<R>& a,
   if constexpr (kEarly) cp_async_wait<0>();
 }
 
-template <typename R, bool kFirst, bool kEarly = true>
+template <typename R, bool kFirst, bool kEarly = true, bool kFl = false>
 __device__ __forceinline__ void tile_mass_sweep_x(const StepArgs<R>& a, const SweepArgs<R>& s,
                                                   int bx, int by) {
   FLOW_POW2_DISPATCH_ALL(a, a.pad + bx * (kCols - 1), a.pad + by * a.rows,
-                     (tile_mass_sweep_x_impl<R, kFirst, true, kEarly>(a, s, bx, by)),
-                     (tile_mass_sweep_x_impl<R, kFirst, false, kEarly>(a, s, bx, by)));
+                     (tile_mass_sweep_x_impl<R, kFirst, true, kEarly, kFl>(a, s, bx, by)),
+                     (tile_mass_sweep_x_impl<R, kFirst, false, kEarly, kFl>(a, s, bx, by)));
 }
 
 // y sweep: each thread marches down its column; face row ii+1 is computed
 // in iteration ii and reused by the cell below.
-template <typename R, bool kFirst, bool kP2, bool kEarly>
+template <typename R, bool kFirst, bool kP2, bool kEarly, bool kFl>
 __device__ __forceinline__ void tile_mass_sweep_y_impl(const StepArgs<R>& a,
                                                        const SweepArgs<R>& s, int bx, int by) {
   using Pr = Prec<R>;
@@ -1564,13 +1590,25 @@ __device__ __forceinline__ void tile_mass_sweep_y_impl(const StepArgs<R>& a,
         },
         s_iey[k], s_icy[k], ex0_r, dt_r, dt_h_r, F, eF);
   };
+  // Stores the mass flux of face row f; kFl: only where the face row moves
+  // somewhere in the warp (mv) -- a face row at rest carries +0 (the mixed
+  // form, whose rows all count as moving, votes on the fluxes instead).  The
+  // warp's flags (bit f - i0 of fmask) are written after the row loop.
+  unsigned long long fmask = 0ull;
+  auto store_fy = [&](int f, R F, bool mv) {
+    bool st = true;
+    if constexpr (kFl) {
+      st = Pr::kMixed ? __any_sync(__activemask(), !is_plus_zero(F)) : mv;
+      if (st) fmask |= 1ull << (f - i0);
+    }
+    if (st) {
+      a.F_y[cidx(nx, f, jj)] = F;
+      mirror(edge, a.F_y, nx, ny + 1, pad, f, jj, F, false, true);
+    }
+  };
   R F0 = R(0), eF0 = R(0);
   if (fresh) flux_at(0, &F0, &eF0);
-  {
-    const size_t c = cidx(nx, i0, jj);
-    a.F_y[c] = F0;
-    mirror(edge, a.F_y, nx, ny + 1, pad, i0, jj, F0, false, true);
-  }
+  store_fy(i0, F0, fresh);
   // The fluxes of the face below, widened once and carried to the next row.
   double f0d = Pr::to_d(F0), ef0d = Pr::to_d(eF0);
   if (!kEarly && i0 < i1) load(i0);
@@ -1630,16 +1668,17 @@ __device__ __forceinline__ void tile_mass_sweep_y_impl(const StepArgs<R>& a,
         refresh();
       }
       flux_at(k + 1, &F1, &eF1);
+      // FP64 form with flags: only a moving face row stores its fluxes, here
+      // on the moving path.
+      if (kFl && !Pr::kMixed && (ii + 1 < i1 || ii + 1 == last_face)) store_fy(ii + 1, F1, true);
     } else {
       // A face row at rest carries no mass and no energy (+0, as the flux
       // core returns for a face at rest).
       rw.push(rn);
       ew.push(en);
     }
-    if (ii + 1 < i1 || ii + 1 == last_face) {
-      const size_t c = cidx(nx, ii + 1, jj);
-      a.F_y[c] = F1;
-      mirror(edge, a.F_y, nx, ny + 1, pad, ii + 1, jj, F1, false, true);
+    if (!(kFl && !Pr::kMixed) && (ii + 1 < i1 || ii + 1 == last_face)) {
+      store_fy(ii + 1, F1, fresh);
     }
     double r_new, e_new;
     const double f1d = Pr::to_d(F1), ef1d = Pr::to_d(eF1);
@@ -1652,15 +1691,23 @@ __device__ __forceinline__ void tile_mass_sweep_y_impl(const StepArgs<R>& a,
     f0d = f1d;
     ef0d = ef1d;
   }
+  if constexpr (kFl) {
+    // Face rows i0 .. i1 - 1, and the north boundary row in the last tile.
+    const int f_end = (i1 == last_face) ? last_face : i1 - 1;
+    unsigned char* fp = a.fyflag + (size_t)(i0 - pad) * 4 * a.qm_stride + 4 * bx + (t >> 5);
+    for (int f = i0; f <= f_end; ++f, fp += 4 * a.qm_stride) {
+      store_flag(fp, (fmask >> (f - i0)) & 1ull);
+    }
+  }
   if constexpr (kEarly) cp_async_wait<0>();
 }
 
-template <typename R, bool kFirst, bool kEarly = true>
+template <typename R, bool kFirst, bool kEarly = true, bool kFl = false>
 __device__ __forceinline__ void tile_mass_sweep_y(const StepArgs<R>& a, const SweepArgs<R>& s,
                                                   int bx, int by) {
   FLOW_POW2_DISPATCH_ALL(a, a.pad + bx * kCols, a.pad + by * a.rows,
-                     (tile_mass_sweep_y_impl<R, kFirst, true, kEarly>(a, s, bx, by)),
-                     (tile_mass_sweep_y_impl<R, kFirst, false, kEarly>(a, s, bx, by)));
+                     (tile_mass_sweep_y_impl<R, kFirst, true, kEarly, kFl>(a, s, bx, by)),
+                     (tile_mass_sweep_y_impl<R, kFirst, false, kEarly, kFl>(a, s, bx, by)));
 }
 
 // ===========================================================================
@@ -1772,7 +1819,7 @@ __device__ __forceinline__ void momentum_face_update(const StepArgs<R>& a, bool 
 //   kV = true (rho_v): thread t holds the vF_x of corner c0 + t (c0 = pad +
 //     127 bx) and, for t < 127, updates y-face c0 + t from corners c0 + t and
 //     c0 + t + 1.
-template <typename R, bool kV, bool kVel, bool kP2, bool kRing>
+template <typename R, bool kV, bool kVel, bool kP2, bool kRing, bool kFl>
 __device__ __forceinline__ void tile_mom_x_impl(const StepArgs<R>& a, int bx, int by) {
   using Pr = Prec<R>;
   __shared__ R s_half[kMaxRows], s_h[kMaxRows], s_row[kMaxRows];
@@ -1812,6 +1859,36 @@ __device__ __forceinline__ void tile_mom_x_impl(const StepArgs<R>& a, int bx, in
       }
     }
   }
+  // kFl: the mass-flux flags of rows i0 - 1 .. i1 - 1 (each at its mirror
+  // source row) for x-sweep tiles bx - 1 .. bx + 1, which hold every face
+  // this tile reads; a mass flux flagged +0 is not loaded.  A pair that does
+  // not recompute a velocity has nothing to do where no mass moves.
+  __shared__ unsigned s_fxw[kFl ? kMaxRows + 1 : 1][3];
+  if constexpr (kFl) {
+    unsigned w = 0u;
+    const int k = t / 3, sel = t - 3 * k;
+    if (k <= i1 - i0) {
+      int r = i0 - 1 + k;
+      r = r < pad ? 2 * pad - 1 - r : (r >= ny - pad ? 2 * (ny - pad) - 1 - r : r);
+      const int wi = bx - 1 + sel;
+      if (wi >= 0 && 4 * wi < a.fx_stride) {
+        w = reinterpret_cast<const unsigned*>(a.fxflag + (size_t)(r - pad) * a.fx_stride)[wi];
+      }
+      s_fxw[k][sel] = w;
+    }
+    if (!__syncthreads_or(w != 0u) && !kVel) return;
+  }
+  // The flag of the mass flux of face column jf in row r (i0 - 1 <= r < i1).
+  auto fxf = [&](int r, int jf) -> bool {
+    if constexpr (!kFl) {
+      return true;
+    } else {
+      const int q = jf - pad;
+      const int tile = q / (kCols - 1);
+      const int tt = q - (kCols - 1) * tile;
+      return ((s_fxw[r - i0 + 1][tile - bx + 1] >> (8 * (tt >> 5))) & 0xffu) != 0u;
+    }
+  };
   // The flux point: cells pad-1 .. nx-pad (rho_u), corners pad .. nx-pad (rho_v).
   const bool flux_ok = kV ? (j < nx + 1 - pad) : (j <= nx - pad);
   const int js = kV ? j : (j < pad ? 2 * pad - 1 - j : (j >= nx - pad ? 2 * (nx - pad) - 1 - j : j));
@@ -1845,20 +1922,22 @@ __device__ __forceinline__ void tile_mom_x_impl(const StepArgs<R>& a, int bx, in
   auto load = [&](int ii) {
     if (!flux_ok) return;
     const size_t f = fidx(nx, ii, js);
-    Fa_n = a.F_x[f];
-    Fb_n = kV ? R(0) : a.F_x[f + 1];
+    Fa_n = fxf(ii, js) ? a.F_x[f] : R(0);
+    Fb_n = (kV || !fxf(ii, js + 1)) ? R(0) : a.F_x[f + 1];
     if (kV) u0_n = uu[f];
   };
   auto issue_flux = [&](int ii) {
     const int sl = (ii - i0) % kSlots;
     const size_t f = fidx(nx, ii, js);
-    cp_async_elem(&s_flux[sl][0][t], flux_ok ? a.F_x + f : a.F_x, flux_ok);
-    cp_async_elem(&s_flux[sl][1][t], flux_ok ? (kV ? uu + f : a.F_x + f + 1) : a.F_x, flux_ok);
+    const bool pa = flux_ok && fxf(ii, js);
+    const bool pb = flux_ok && (kV || fxf(ii, js + 1));
+    cp_async_elem(&s_flux[sl][0][t], pa ? a.F_x + f : a.F_x, pa);
+    cp_async_elem(&s_flux[sl][1][t], pb ? (kV ? uu + f : a.F_x + f + 1) : a.F_x, pb);
   };
   if (i0 < i1) {
     if (kV && flux_ok) {
       const size_t f = fidx(nx, i0 - 1, j);
-      F_dn = a.F_x[f];
+      F_dn = fxf(i0 - 1, j) ? a.F_x[f] : R(0);
       u_dn = uu[f];
     }
     if constexpr (kFluxRing) {
@@ -1979,7 +2058,7 @@ __device__ __forceinline__ void tile_mom_x_impl(const StepArgs<R>& a, int bx, in
 //     updates y-faces i0 .. i1-1 from cells ii-1, ii.
 // The windows form their differences only where mass moves in the warp
 // (FP64 form), as the y mass sweep does.
-template <typename R, bool kV, bool kVel, bool kP2, bool kRing>
+template <typename R, bool kV, bool kVel, bool kP2, bool kRing, bool kFl>
 __device__ __forceinline__ void tile_mom_y_impl(const StepArgs<R>& a, int bx, int by) {
   using Pr = Prec<R>;
   // kVel and kRing (the fused kernels): the update inputs of a face stream
@@ -2028,7 +2107,39 @@ __device__ __forceinline__ void tile_mom_y_impl(const StepArgs<R>& a, int bx, in
       }
     }
   }
-  __syncthreads();
+  // kFl: the mass-flux flags of y-face rows i0 - 1 .. i1 for column tiles
+  // bx - 1 and bx, which hold every face this tile reads; a mass flux flagged
+  // +0 is not loaded.  A pair that does not recompute a velocity has nothing
+  // to do where no mass moves.
+  __shared__ unsigned s_fyw[kFl ? kMaxRows + 2 : 1][2];
+  if constexpr (kFl) {
+    unsigned w0 = 0u, w1 = 0u;
+    const int k = threadIdx.x;
+    if (k <= i1 - i0 + 1) {
+      const int f = i0 - 1 + k;
+      if (f >= pad && f <= ny - pad) {
+        const unsigned* row =
+            reinterpret_cast<const unsigned*>(a.fyflag) + (size_t)(f - pad) * a.qm_stride;
+        w0 = bx >= 1 ? row[bx - 1] : 0u;
+        w1 = bx < a.qm_stride ? row[bx] : 0u;
+      }
+      s_fyw[k][0] = w0;
+      s_fyw[k][1] = w1;
+    }
+    if (!__syncthreads_or((w1 | (w0 & 0xff000000u)) != 0u) && !kVel) return;
+  } else {
+    __syncthreads();
+  }
+  // The flag of the mass flux of y-face row f (i0 - 1 <= f <= i1) and column
+  // col (a ghost column at its mirror source, an identical copy).
+  auto fyf = [&](int f, int col) -> bool {
+    if constexpr (!kFl) {
+      return true;
+    } else {
+      col = col < pad ? 2 * pad - 1 - col : (col >= nx - pad ? 2 * (nx - pad) - 1 - col : col);
+      return qflag(s_fyw[f - i0 + 1][0], s_fyw[f - i0 + 1][1], col, pad, bx);
+    }
+  };
   if (jj >= (kV ? nx - pad : nx + 1 - pad) || i0 >= i1) return;
   const R dt_h = Pr::from_d(a.dt_slot[1]);
   const R hcol = geo_half<R>(kV ? a.celldx[jj] : a.edgedx[jj]);  // flux: celldx/2 or edgedx/2
@@ -2080,8 +2191,8 @@ __device__ __forceinline__ void tile_mom_y_impl(const StepArgs<R>& a, int bx, in
   R Fa_n = R(0), Fb_n = R(0), wv_n = R(0);
   auto load = [&](int ci) {
     const size_t c = cidx(nx, ci, jj);
-    Fa_n = a.F_y[c];
-    Fb_n = kV ? a.F_y[c + nx] : a.F_y[c - 1];
+    Fa_n = fyf(ci, jj) ? a.F_y[c] : R(0);
+    Fb_n = (kV ? fyf(ci + 1, jj) : fyf(ci, jj - 1)) ? (kV ? a.F_y[c + nx] : a.F_y[c - 1]) : R(0);
     wv_n = w[widx(ci + wlo + 3)];
   };
   // The flux rows a column consumes are consecutive: from the window's first
@@ -2092,8 +2203,9 @@ __device__ __forceinline__ void tile_mom_y_impl(const StepArgs<R>& a, int bx, in
   auto issue_flux = [&](int ci) {
     const int sl = (ci - w0row) % kSlots;
     const size_t c = cidx(nx, ci, jj);
-    cp_async_elem(&s_flux[sl][0][threadIdx.x], a.F_y + c, true);
-    cp_async_elem(&s_flux[sl][1][threadIdx.x], kV ? a.F_y + c + nx : a.F_y + c - 1, true);
+    cp_async_elem(&s_flux[sl][0][threadIdx.x], a.F_y + c, fyf(ci, jj));
+    cp_async_elem(&s_flux[sl][1][threadIdx.x], kV ? a.F_y + c + nx : a.F_y + c - 1,
+                  kV ? fyf(ci + 1, jj) : fyf(ci, jj - 1));
     cp_async_elem(&s_flux[sl][2][threadIdx.x], w + widx(ci + wlo + 3), true);
   };
   // Row ci's values from the ring (its group waited for), the row kAhead
@@ -2210,17 +2322,17 @@ __device__ __forceinline__ void tile_mom_y_impl(const StepArgs<R>& a, int bx, in
   if constexpr (kUpdRing || kFluxRing) cp_async_wait<0>();
 }
 
-template <typename R, bool kV, bool kVel, bool kRing = true>
+template <typename R, bool kV, bool kVel, bool kRing = true, bool kFl = false>
 __device__ __forceinline__ void tile_mom_x(const StepArgs<R>& a, int bx, int by) {
   FLOW_POW2_DISPATCH(R, a, (kV ? a.pad : a.pad - 1) + bx * (kCols - 1), a.pad + by * a.rows,
-                     (tile_mom_x_impl<R, kV, kVel, true, kRing>(a, bx, by)),
-                     (tile_mom_x_impl<R, kV, kVel, false, kRing>(a, bx, by)));
+                     (tile_mom_x_impl<R, kV, kVel, true, kRing, kFl>(a, bx, by)),
+                     (tile_mom_x_impl<R, kV, kVel, false, kRing, kFl>(a, bx, by)));
 }
-template <typename R, bool kV, bool kVel, bool kRing = true>
+template <typename R, bool kV, bool kVel, bool kRing = true, bool kFl = false>
 __device__ __forceinline__ void tile_mom_y(const StepArgs<R>& a, int bx, int by) {
   FLOW_POW2_DISPATCH(R, a, a.pad + bx * kCols, a.pad + by * a.rows,
-                     (tile_mom_y_impl<R, kV, kVel, true, kRing>(a, bx, by)),
-                     (tile_mom_y_impl<R, kV, kVel, false, kRing>(a, bx, by)));
+                     (tile_mom_y_impl<R, kV, kVel, true, kRing, kFl>(a, bx, by)),
+                     (tile_mom_y_impl<R, kV, kVel, false, kRing, kFl>(a, bx, by)));
 }
 
 }  // namespace tiles
