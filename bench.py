@@ -18,12 +18,15 @@ Prints one JSON line on rank 0.  Besides the timed FP64 line it reports:
   forms         the mixed-precision form (blast, 8192^2 Sod, a field in
                 motion everywhere) and the batched forms at their stated
                 lengths (200 and 1000 steps), with their errors;
-  cpu_baseline  the oracle built with the reference's flags on the host cores.
-With --impl reference the same workload runs on the host cores through the
-oracle, which the tests hold bit-identical to the reference's own omp3 code
-(the reference has no GPU path that builds on this machine).  Under torchrun
-(N > 1) every rank advances its own replica (replicas only; the single-mesh
-step is not decomposed across GPUs here).
+  reference_cuda (in forms) the reference's own cuda kernel set built for
+                sm_103a, timed on the same workload and GPU;
+  cpu_baseline  the reference's own omp3 set built with its flags (where its
+                sources were staged and built), else the oracle with the same
+                flags, on the host cores.
+With --impl reference the same workload runs on the host cores through that
+same CPU build.  Under torchrun (N > 1) every rank advances its own replica
+(the single-mesh decomposition, flow_gb300.decomp, exchanges halos through
+host hooks and is not timed here).
 """
 from __future__ import annotations
 
@@ -46,26 +49,30 @@ CONFIG_STEPS = 500   # the blast workload's stated length
 B_ALG_FP64 = 64      # bytes/cell-step: rho, e, rho_u, rho_v read + written once
 B_ALG_MIXED = 48     # rho, e (FP64) and rho_u, rho_v (FP32), each read + written
 
-# Algorithmic bytes per interior cell of each fused kernel: the arrays it must
-# read and write once (8 bytes each) on every cell.  Arrays that change only
-# where the flow moves (momenta, energy) are counted as read; their writes on
-# moving cells come on top.  Used for the per-kernel HBM roofline.
+# Algorithmic bytes per interior cell of each fused kernel (the per-kernel HBM
+# roofline): the arrays it must read or write at every cell, 8 B each; what the
+# stress and mass-flux flags let it touch only where the flow moves (Q, the
+# mass fluxes, the changed energies and momenta) counts as nothing.
 KERNEL_BYTES_PER_CELL = {
     "lag_pressure": 8 * 7,       # rho, e, rho_u, rho_v in; P, u, v out
-    "lag_viscosity": 8 * 5,      # u, v, rho in; Qxx, Qyy out
-    "lag_viscous_accel": 8 * 2,  # Qxx, Qyy in (momenta, densities, velocities where a stress gradient acts)
-    "lag_energy_dt": 8 * 6,      # rho, e, Qxx, Qyy, u, v in (P in, e out where the cell is compressed)
+    "lag_viscosity": 8 * 3,      # u, v, rho in (Qxx, Qyy out where a stress is not +0)
+    "lag_viscous_accel": 0,      # stresses, momenta, velocities only where a stress gradient acts
+    "lag_energy_dt": 8 * 4,      # rho, e, u, v in (P, Q in and e out where a cell is compressed)
     "lag_fused": 8 * 6,          # one-kernel Lagrangian phase: rho, e, rho_u, rho_v in; u, v out
     "lag_apply": 0,              # changed values only
-    "mass_sweep_x": 8 * 6,       # rho, e, u in; rho, e, F_x out
-    "mass_sweep_y": 8 * 6,
-    # Momentum pairs (flux fused with its update), one launch per step each;
-    # the velocity is recomputed (rho, the momentum in, the velocity out:
-    # 24 B) in every other step's launch, so half of it counts per launch.
-    "mom_uFx": 8 + 12,           # F_x in (u where mass moves)
-    "mom_uFy": 16 + 12,          # F_y, u in
-    "mom_vFx": 16 + 12,          # F_x, u in (v where mass moves)
-    "mom_vFy": 16 + 12,          # F_y, v in
+    # The sweeps: rho, e and the face velocity in, rho, e out (the mass fluxes
+    # where faces move); the second sweep of a step also reads the old
+    # density, and each direction is the second sweep every other step.
+    "mass_sweep_x": 8 * 5 + 4,
+    "mass_sweep_y": 8 * 5 + 4,
+    # Momentum pairs (flux fused with its update), one launch per step each:
+    # every other step's launch recomputes the velocity (momentum, density
+    # in, velocity out: 24 B); the other launch moves bytes only where mass
+    # moves.  Half of 24 B counts per launch.
+    "mom_uFx": 12,
+    "mom_uFy": 12,
+    "mom_vFx": 12,
+    "mom_vFy": 12,
     "mesh_pow2": 0,              # the step's one-block mesh test (spacings only)
 }
 
