@@ -525,9 +525,22 @@ __device__ __forceinline__ void tile_lag_pressure(const StepArgs<R>& a, int bx, 
 }
 
 // Artificial viscous stresses on interior cells, omp3/flow.c:173-207.
+
+// A zero stress as +0.  The mixed form, which takes no zero skip, forms a
+// stress of a cell without compression as (-C_Q rho) (+0) (...) = -0; adding
+// +0 makes it +0 (and changes no other value), so that the stress flags see
+// it as zero.  The sign of a zero stress reaches no non-zero value.
 template <typename R>
+__device__ __forceinline__ R stress_sign0(R q) {
+  if constexpr (Prec<R>::kMixed) {
+    return q + R(0);
+  } else {
+    return q;
+  }
+}
 // mid = w[0], hi = w[1]; lo = w[-1] and hi2 = w[2] are loaded only where
 // the cell is compressed.
+template <typename R>
 __device__ __forceinline__ R visc_stress(R rho, const R* w, R mid, R hi) {
   using Pr = Prec<R>;
   // Equal velocities either side of every cell of the warp: hi - mid = +0,
@@ -537,7 +550,7 @@ __device__ __forceinline__ R visc_stress(R rho, const R* w, R mid, R hi) {
   if (Pr::zero_skip(m1)) return R(0);  // no compression across the cell
   const R m0 = Pr::min0(mid - w[-1]);
   const R m2 = Pr::min0(w[2] - hi);
-  return R(-kCQ) * rho * m1 * Pr::half(Pr::abs(m2 - m1) + Pr::abs(m1 - m0));
+  return stress_sign0(R(-kCQ) * rho * m1 * Pr::half(Pr::abs(m2 - m1) + Pr::abs(m1 - m0)));
 }
 
 // kFlags: a.qmask is set -- a warp row whose stresses are all +0 stores only
@@ -599,7 +612,7 @@ __device__ __forceinline__ void tile_lag_viscosity(const StepArgs<R>& a, int bx,
     } else {
       m2 = Pr::min0(vp2 - vp);
       g12 = Pr::abs(m2 - m1);
-      qy = Pr::zero_skip(m1) ? R(0) : R(-kCQ) * rho * m1 * Pr::half(g12 + g01);
+      qy = Pr::zero_skip(m1) ? R(0) : stress_sign0(R(-kCQ) * rho * m1 * Pr::half(g12 + g01));
     }
     // With flags, a warp row whose stresses are all +0 (the still regions)
     // stores none of them, only its flag.
