@@ -1824,6 +1824,75 @@ __device__ __forceinline__ void momentum_face_update(const StepArgs<R>& a, bool 
   }
 }
 
+// Whether no mass moves through any face of the cells in rows r0 .. r1 and
+// columns c0 .. c1 (the mass-flux flags of the sweeps: x faces of those
+// rows, y faces of rows r0 .. r1 + 1; ghost faces are copies of faces inside
+// these ranges).  Block-uniform (barrier).  Then no cell there changed its
+// density in the sweeps, and no momentum flux of those faces is non-zero.
+template <typename R>
+__device__ __forceinline__ bool tile_mass_still(const StepArgs<R>& a, int r0, int r1, int c0,
+                                                int c1) {
+  const int nx = a.nx, ny = a.ny, pad = a.pad;
+  const int xr0 = max(r0, pad), xr1 = min(r1, ny - pad - 1);
+  const int xc0 = max(c0, pad), xc1 = min(c1, nx - pad);
+  const int yr0 = max(r0, pad), yr1 = min(r1 + 1, ny - pad);
+  const int yc0 = max(c0, pad), yc1 = min(c1, nx - pad - 1);
+  // Flag bytes: x faces by x-sweep tile and warp, y faces by 32 columns.
+  auto xbyte = [&](int c) {
+    const int q = c - pad;
+    return 4 * (q / (kCols - 1)) + ((q % (kCols - 1)) >> 5);
+  };
+  const int xb0 = xbyte(xc0), xnb = xc1 >= xc0 ? xbyte(xc1) - xb0 + 1 : 0;
+  const int yb0 = (yc0 - pad) >> 5, ynb = yc1 >= yc0 ? ((yc1 - pad) >> 5) - yb0 + 1 : 0;
+  const int nxt = max(0, xr1 - xr0 + 1) * xnb;
+  const int total = nxt + max(0, yr1 - yr0 + 1) * ynb;
+  bool any = false;
+  for (int q = threadIdx.x; q < total; q += blockDim.x) {
+    if (q < nxt) {
+      const int r = xr0 + q / xnb, b = xb0 + q % xnb;
+      any |= a.fxflag[(size_t)(r - pad) * a.fx_stride + b] != 0;
+    } else {
+      const int q2 = q - nxt;
+      const int r = yr0 + q2 / ynb, b = yb0 + q2 % ynb;
+      any |= a.fyflag[(size_t)(r - pad) * 4 * a.qm_stride + b] != 0;
+    }
+  }
+  return __syncthreads_or(any) == 0;
+}
+
+// The velocities of a pair that recomputes them, where no mass moves around
+// its faces: the momentum and both densities are what the Lagrangian phase
+// formed the velocity from, so the advected velocity is the Lagrangian one
+// (w), copied with its ghost images (rows i0 .. i1 - 1 of face column j;
+// kU: x faces).  Loads in batches of eight rows, all in flight together.
+template <typename R, bool kU>
+__device__ __forceinline__ void copy_velocities(const StepArgs<R>& a, bool edge, const R* w,
+                                                R* vout, int i0, int i1, int j, bool ok) {
+  const int nx = a.nx, ny = a.ny, pad = a.pad;
+  constexpr int kB = 8;
+  for (int ib = i0; ib < i1; ib += kB) {
+    R v[kB];
+#pragma unroll
+    for (int q = 0; q < kB; ++q) {
+      const int ii = ib + q;
+      v[q] = (ok && ii < i1) ? w[kU ? fidx(nx, ii, j) : cidx(nx, ii, j)] : R(0);
+    }
+#pragma unroll
+    for (int q = 0; q < kB; ++q) {
+      const int ii = ib + q;
+      if (ok && ii < i1) {
+        if (kU) {
+          vout[fidx(nx, ii, j)] = v[q];
+          mirror(edge, vout, nx + 1, ny, pad, ii, j, v[q], true, false);
+        } else {
+          vout[cidx(nx, ii, j)] = v[q];
+          mirror(edge, vout, nx, ny + 1, pad, ii, j, v[q], false, true);
+        }
+      }
+    }
+  }
+}
+
 // x pairs: the flux points of a row are spread over the CTA's threads and
 // shared through shared memory; 127 faces per CTA of 128 threads.
 //   kV = false (rho_u): thread t holds the uF_x of cell c0 + t (c0 = pad-1 +
@@ -1859,6 +1928,14 @@ __device__ __forceinline__ void tile_mom_x_impl(const StepArgs<R>& a, int bx, in
   const int i0 = pad + by * a.rows;
   const bool edge = tile_near_edge(nx, ny, pad, c0, i0, a.rows);
   const int i1 = min(i0 + a.rows, kV ? ny + 1 - pad : ny - pad);
+  if constexpr (kVel && kFl) {
+    // No mass moves around the tile's faces: the Lagrangian velocities stand.
+    if (tile_mass_still(a, i0 - 1, i1, c0 - 1, c0 + kCols)) {
+      const bool upd = kV ? (t < kCols - 1 && j < nx - pad) : (t >= 1 && j < nx + 1 - pad);
+      copy_velocities<R, !kV>(a, edge, kV ? a.v : a.u, kV ? a.v_out : a.u_out, i0, i1, j, upd);
+      return;
+    }
+  }
   if (t < a.rows) {
     const int ii = i0 + t;
     if (ii < ny) {
@@ -2093,6 +2170,15 @@ __device__ __forceinline__ void tile_mom_y_impl(const StepArgs<R>& a, int bx, in
   const int i0 = pad + by * a.rows;
   const bool edge = tile_near_edge(nx, ny, pad, pad + bx * kCols, i0, a.rows);
   const int i1 = min(i0 + a.rows, kV ? ny + 1 - pad : ny - pad);
+  if constexpr (kVel && kFl) {
+    // No mass moves around the tile's faces: the Lagrangian velocities stand.
+    const int cb = pad + bx * kCols;
+    if (tile_mass_still(a, i0 - 1, i1, cb - 1, cb + kCols)) {
+      copy_velocities<R, !kV>(a, edge, kV ? a.v : a.u, kV ? a.v_out : a.u_out, i0, i1, jj,
+                              jj < (kV ? nx - pad : nx + 1 - pad));
+      return;
+    }
+  }
   // Flux rows: corners i0 .. i1 (rho_u); cells i0-1 .. i1-1 (rho_v), a ghost
   // row computed at its mirror source.
   const int fr0 = kV ? i0 - 1 : i0;
