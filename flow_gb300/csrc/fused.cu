@@ -56,7 +56,7 @@ __global__ void __launch_bounds__(kPow2Threads)
   if (threadIdx.x == 0) *flag = ok ? 1ull : 0ull;
 }
 
-template <typename R>
+template <typename R, bool kFl>
 __global__ void __launch_bounds__(kCols) k_lag_pressure(const StepArgs<R> a) {
   pdl_wait();
   pdl_trigger();
@@ -66,7 +66,7 @@ __global__ void __launch_bounds__(kCols) k_lag_pressure(const StepArgs<R> a) {
     *reinterpret_cast<unsigned long long*>(a.ra + kRaTicket) = 0ull;
     *a.min_slot = ~0ull;
   }
-  tile_lag_pressure(a, blockIdx.x, blockIdx.y);
+  tile_lag_pressure<R, kFl>(a, blockIdx.x, blockIdx.y);
 }
 // kFlags: the viscous-stress flags (a.qmask) are kept -- the viscosity
 // kernel stores only warp rows with a non-zero stress, and the two kernels
@@ -370,7 +370,8 @@ void launch_step(cudaStream_t s, const StepArgs<R>& a, int tt,
                      const_cast<double*>(lag->rho_v));
   } else {
     prof.mark("lag_pressure");
-    launch_pdl(k_lag_pressure<R>, strip_grid(nx, ny, a.rows), s, a);
+    launch_pdl(a.vflag ? k_lag_pressure<R, true> : k_lag_pressure<R, false>,
+               strip_grid(nx, ny, a.rows), s, a);
     const bool fl = a.qmask != nullptr;
     prof.mark("lag_viscosity");
     launch_pdl(fl ? k_lag_viscosity<R, true> : k_lag_viscosity<R, false>,
@@ -384,32 +385,36 @@ void launch_step(cudaStream_t s, const StepArgs<R>& a, int tt,
                strip_grid(nx - 2 * pad, ny - 2 * pad, a.rows), s, a);
   }
 
+  // The advection phase reads velocity flags only when this step's
+  // Lagrangian kernels wrote them (not the one-kernel phase).
+  StepArgs<R> ad = a;
+  if (lag) ad.vflag = nullptr;
   const bool x_first = (tt % 2 == 0);
   prof.mark(x_first ? "mass_sweep_x" : "mass_sweep_y");
-  launch_mass(s, a, !x_first, true, first);
+  launch_mass(s, ad, !x_first, true, first);
   prof.mark(x_first ? "mass_sweep_y" : "mass_sweep_x");
-  launch_mass(s, a, x_first, false, second);
+  launch_mass(s, ad, x_first, false, second);
 
   // Momentum: each flux fused with its update, in the reference order; the
   // pair that recomputes a velocity comes first in each chain.
   if (tt % 2) {
     prof.mark("mom_uFx");
-    launch_mom_x<R, false, true>(s, a);
+    launch_mom_x<R, false, true>(s, ad);
     prof.mark("mom_uFy");
-    launch_mom_y<R, false, false>(s, a);
+    launch_mom_y<R, false, false>(s, ad);
     prof.mark("mom_vFx");
-    launch_mom_x<R, true, true>(s, a);
+    launch_mom_x<R, true, true>(s, ad);
     prof.mark("mom_vFy");
-    launch_mom_y<R, true, false>(s, a);
+    launch_mom_y<R, true, false>(s, ad);
   } else {
     prof.mark("mom_uFy");
-    launch_mom_y<R, false, true>(s, a);
+    launch_mom_y<R, false, true>(s, ad);
     prof.mark("mom_uFx");
-    launch_mom_x<R, false, false>(s, a);
+    launch_mom_x<R, false, false>(s, ad);
     prof.mark("mom_vFy");
-    launch_mom_y<R, true, true>(s, a);
+    launch_mom_y<R, true, true>(s, ad);
     prof.mark("mom_vFx");
-    launch_mom_x<R, true, false>(s, a);
+    launch_mom_x<R, true, false>(s, ad);
   }
 }
 
@@ -469,13 +474,17 @@ void fill_mesh_args(StepArgs<R>& a, const Mesh* mesh, int tt, double* ra) {
   a.fxflag = nullptr;
   a.fyflag = nullptr;
   a.fx_stride = 0;
+  a.vflag = nullptr;
+  a.vf_stride = 0;
   const int stride = (a.nx - 2 * a.pad + kCols - 1) / kCols;
   const int xtiles = (a.nx + 1 - 2 * a.pad + kCols - 2) / (kCols - 1);
   const long long rows = a.ny - 2 * a.pad;
   const size_t q_words = (size_t)rows * stride, fy_words = (size_t)(rows + 1) * stride;
   const size_t fx_words = (size_t)rows * xtiles;
-  const size_t need =
-      (size_t)kRaQFlags * sizeof(double) + (q_words + fy_words + fx_words) * sizeof(unsigned);
+  const int vtiles = (a.nx + kCols - 1) / kCols;
+  const size_t v_words = (size_t)a.ny * vtiles;
+  const size_t need = (size_t)kRaQFlags * sizeof(double) +
+                      (q_words + fy_words + fx_words + v_words) * sizeof(unsigned);
   if (stride > 0 && rows > 0 && need <= (size_t)a.nx * a.ny * sizeof(double)) {
     unsigned* base = reinterpret_cast<unsigned*>(ra + kRaQFlags);
     a.qmask = base;
@@ -483,6 +492,8 @@ void fill_mesh_args(StepArgs<R>& a, const Mesh* mesh, int tt, double* ra) {
     a.fyflag = reinterpret_cast<unsigned char*>(base + q_words);
     a.fxflag = reinterpret_cast<unsigned char*>(base + q_words + fy_words);
     a.fx_stride = 4 * xtiles;
+    a.vflag = reinterpret_cast<unsigned char*>(base + q_words + fy_words + fx_words);
+    a.vf_stride = 4 * vtiles;
   }
 }
 

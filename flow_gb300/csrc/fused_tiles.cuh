@@ -100,6 +100,14 @@ struct StepArgs {
   unsigned char* fxflag;
   unsigned char* fyflag;
   int fx_stride;               // bytes per row: 4 ceil((nx + 1 - 2 pad) / 127)
+  // Velocity flags, or null (set with the others): byte r * vf_stride +
+  // (jj >> 5) is 1 when the pressure phase or the viscous update stored a
+  // face velocity (x face (r, jj) or y face (r, jj)) that is not +0 in the
+  // 32 columns jj & ~31 .. (jj | 31) of row r (rows 0 .. ny - 1 of the
+  // padded mesh, columns counted from 0).  Where every byte around a tile is
+  // 0, the velocities it would read are +0 and it does not load them.
+  unsigned char* vflag;
+  int vf_stride;               // bytes per row: 4 ceil(nx / 128)
 };
 
 // Writes the value of interior point (ii, jj) of a w x h array into each of
@@ -221,6 +229,26 @@ __device__ __forceinline__ bool warp_zeros(R a, R b) {
 // it.
 __device__ __forceinline__ void store_flag(unsigned char* p, bool v) {
   asm volatile("st.global.u8 [%0], %1;" ::"l"(p), "h"((unsigned short)(v ? 1 : 0)));
+}
+
+// Whether every face velocity in rows r0 .. r1 and columns c0 .. c1 (of
+// the padded mesh, clamped to it) is +0 by the velocity flags.  The ranges
+// the tiles pass reach two rows and columns past what they read, so that
+// they hold the mirror source of every ghost face they read.  Block-uniform
+// (barrier); called by every thread of the block.  False without flags.
+template <typename A>
+__device__ __forceinline__ bool tile_vel_still(const A& a, int r0, int r1, int c0, int c1) {
+  if (!a.vflag) return false;  // no velocity flags this step (uniform)
+  r0 = max(r0, 0);
+  r1 = min(r1, a.ny - 1);
+  const int g0 = max(c0, 0) >> 5, g1 = min(c1, a.nx) >> 5;
+  const int ng = g1 - g0 + 1, total = max(0, r1 - r0 + 1) * ng;
+  bool any = false;
+  for (int q = threadIdx.x; q < total; q += blockDim.x) {
+    const int r = r0 + q / ng, g = g0 + q % ng;
+    any |= a.vflag[(size_t)r * a.vf_stride + g] != 0;
+  }
+  return __syncthreads_or(any) == 0;
 }
 
 // x is +0 (all bits zero).
@@ -389,7 +417,7 @@ __device__ __forceinline__ R face_average(R a, R wa, R b, R wb) {
 // shock-heating kernel reads it where a cell is compressed) and every interior
 // x/y face.  The reference's rho_old copy is not made: the first mass sweep
 // reads the density itself.  omp3/flow.c:55-70, 110-158.
-template <typename R, bool kP2>
+template <typename R, bool kP2, bool kFl>
 __device__ __forceinline__ void tile_lag_pressure_impl(const StepArgs<R>& a, int bx, int by) {
   using Pr = Prec<R>;
   __shared__ R sP[kCols + 1], sR[kCols + 1];
@@ -452,6 +480,7 @@ __device__ __forceinline__ void tile_lag_pressure_impl(const StepArgs<R>& a, int
     const R rc_l = rc_n, ec_l = ec_n, rl_l = rl_n, el_l = el_n, mu_l = mu_n, mv_l = mv_n;
     if (k + 1 < a.rows && ii + 1 < ny) load(ii + 1);
     R Pc = R(0), rc = R(0);
+    bool vnz = false;  // kFl: this lane stored a face velocity that is not +0
     if (jj < nx) {
       rc = rc_l;
       Pc = g1 * rc * ec_l;
@@ -492,6 +521,7 @@ __device__ __forceinline__ void tile_lag_pressure_impl(const StepArgs<R>& a, int
       const R vel = face_velocity(mom, rbar);
       a.u[f] = vel;
       mirror(edge, a.u, nx + 1, ny, pad, ii, jj, vel, true, false);
+      vnz = !is_plus_zero(vel);
     }
     if (ii >= pad && ii < ny + 1 - pad && jj >= pad && jj < nx - pad) {
       const size_t c = cidx(nx, ii, jj);
@@ -511,6 +541,11 @@ __device__ __forceinline__ void tile_lag_pressure_impl(const StepArgs<R>& a, int
       const R vel = face_velocity(mom, rbar);
       a.v[c] = vel;
       mirror(edge, a.v, nx, ny + 1, pad, ii, jj, vel, false, true);
+      vnz = vnz || !is_plus_zero(vel);
+    }
+    if constexpr (kFl) {
+      store_flag(a.vflag + (size_t)ii * a.vf_stride + (jj >> 5),
+                 __any_sync(0xffffffffu, vnz) != 0);
     }
     P_dn = Pc;
     r_dn = rc;
@@ -518,10 +553,11 @@ __device__ __forceinline__ void tile_lag_pressure_impl(const StepArgs<R>& a, int
   }
 }
 
-template <typename R>
+template <typename R, bool kFl = false>
 __device__ __forceinline__ void tile_lag_pressure(const StepArgs<R>& a, int bx, int by) {
-  FLOW_POW2_DISPATCH(R, a, bx * kCols, by * a.rows, (tile_lag_pressure_impl<R, true>(a, bx, by)),
-                     (tile_lag_pressure_impl<R, false>(a, bx, by)));
+  FLOW_POW2_DISPATCH(R, a, bx * kCols, by * a.rows,
+                     (tile_lag_pressure_impl<R, true, kFl>(a, bx, by)),
+                     (tile_lag_pressure_impl<R, false, kFl>(a, bx, by)));
 }
 
 // Artificial viscous stresses on interior cells, omp3/flow.c:173-207.
@@ -563,6 +599,13 @@ __device__ __forceinline__ void tile_lag_viscosity(const StepArgs<R>& a, int bx,
   const bool edge = tile_near_edge(nx, ny, pad, pad + bx * kCols, i0, a.rows);
   using Pr = Prec<R>;
   const int i1 = min(i0 + a.rows, ny - pad);
+  // kFlags: a tile whose face velocities (with the stencil's reach) are all
+  // +0 loads none of them; its stresses are +0 and nothing is stored.
+  bool vq = false;
+  if constexpr (kFlags) {
+    const int cb = pad + bx * kCols;
+    vq = tile_vel_still(a, i0 - 3, i1 + 4, cb - 3, cb + kCols + 3);
+  }
   // This warp's stress-flag byte of row i0, or null without flags.
   unsigned char* qf =
       kFlags ? reinterpret_cast<unsigned char*>(a.qmask + (size_t)(i0 - pad) * a.qm_stride + bx) +
@@ -580,15 +623,16 @@ __device__ __forceinline__ void tile_lag_viscosity(const StepArgs<R>& a, int bx,
   // The y stress of row ii uses the limited jumps m0, m1, m2 of v around the
   // cell and |m1 - m0|, |m2 - m1|; the next row reuses three of those, so
   // they are carried down the column (same operands, same values).
-  const R vm = a.v[cidx(nx, i0 - 1, jj)];
-  const R v0 = a.v[cidx(nx, i0, jj)];
-  R vp = a.v[cidx(nx, i0 + 1, jj)];
+  const R vm = vq ? R(0) : a.v[cidx(nx, i0 - 1, jj)];
+  const R v0 = vq ? R(0) : a.v[cidx(nx, i0, jj)];
+  R vp = vq ? R(0) : a.v[cidx(nx, i0 + 1, jj)];
   R m0 = Pr::min0(v0 - vm), m1 = Pr::min0(vp - v0);
   R g01 = Pr::abs(m1 - m0);
   // Row ii+1's v, density and face velocities are loaded before row ii is
   // processed.
   R vp2_n = R(0), rho_n = R(0), um_n = R(0), up_n = R(0);
   auto load = [&](int ii) {
+    if (vq) return;
     const size_t f = fidx(nx, ii, jj);
     vp2_n = a.v[cidx(nx, ii + 2, jj)];
     rho_n = a.rho_r[cidx(nx, ii, jj)];
@@ -601,7 +645,7 @@ __device__ __forceinline__ void tile_lag_viscosity(const StepArgs<R>& a, int bx,
     if (ii + 1 < i1) load(ii + 1);
     const size_t f = fidx(nx, ii, jj);
     const size_t c = cidx(nx, ii, jj);
-    const R qx = visc_stress(rho, a.u + f, um, up);
+    const R qx = vq ? R(0) : visc_stress(rho, a.u + f, um, up);
     R m2, g12, qy;
     if (!Pr::kMixed && warp_all(lane_same(vp2, vp) && Pr::is_zero(m1))) {
       // No jump of v across the cell or above it anywhere in the warp:
@@ -740,6 +784,7 @@ __device__ __forceinline__ void tile_lag_viscous_accel_impl(const StepArgs<R>& a
           a.rho_u[f] = mom;
           a.u[f] = vel;
           mirror(edge, a.u, nx + 1, ny, pad, ii, jj, vel, true, false);
+          if constexpr (kFlags) store_flag(a.vflag + (size_t)ii * a.vf_stride + (jj >> 5), true);
         }
       }
     }
@@ -754,6 +799,7 @@ __device__ __forceinline__ void tile_lag_viscous_accel_impl(const StepArgs<R>& a
           a.rho_v[c] = mom;
           a.v[c] = vel;
           mirror(edge, a.v, nx, ny + 1, pad, ii, jj, vel, false, true);
+          if constexpr (kFlags) store_flag(a.vflag + (size_t)ii * a.vf_stride + (jj >> 5), true);
         }
       }
       qy_dn = qy;
@@ -843,6 +889,13 @@ __device__ __forceinline__ void tile_lag_energy_dt_impl(const StepArgs<R>& a, in
     if (kFlags && ii < ny - pad) s_qf[threadIdx.x] = a.qmask[(size_t)(ii - pad) * a.qm_stride + bx];
   }
   __syncthreads();
+  // kFlags: a tile whose face velocities are all +0 (velocity flags) loads
+  // none of them: its cells are still, and take the still path on +0 values.
+  bool vq = false;
+  if constexpr (kFlags) {
+    const int cb = pad + bx * kCols;
+    vq = tile_vel_still(a, i0 - 2, min(i0 + a.rows, ny - pad) + 2, cb - 2, cb + kCols + 2);
+  }
   // Whether the stresses of this thread's warp in tile row k may be non-zero
   // (flagged +0: not loaded, taken as +0).
   auto qflag_row = [&](int k) {
@@ -858,7 +911,7 @@ __device__ __forceinline__ void tile_lag_energy_dt_impl(const StepArgs<R>& a, in
     const double icx2 = Pr::kMixed ? 0.0 : geo_rcp_sq<kP2>(a.celldx[jj]);
     const R dt_h = Pr::from_d(a.dt_h);
     const int i1 = min(i0 + a.rows, ny - pad);
-    R v0 = a.v[cidx(nx, i0, jj)];
+    R v0 = vq ? R(0) : a.v[cidx(nx, i0, jj)];
     // Mixed form: row ii+1's inputs are loaded before row ii is processed.
     // The FP64 form (at 64 registers without that, which loses more
     // occupancy than it gains) streams them through a per-thread ring of
@@ -875,27 +928,27 @@ __device__ __forceinline__ void tile_lag_energy_dt_impl(const StepArgs<R>& a, in
     auto load = [&](int ii) {
       const size_t c = cidx(nx, ii, jj);
       const size_t f = c + (size_t)ii;  // fidx(nx, ii, jj)
-      v1_n = a.v[c + nx];
+      v1_n = vq ? R(0) : a.v[c + nx];
       r_n = a.rho_r[c];
       er_n = a.e_r[c];
       const bool qf = qflag_row(ii - i0);
       qx_n = qf ? a.Qxx[c] : R(0);
       qy_n = qf ? a.Qyy[c] : R(0);
-      u0_n = a.u[f];
-      u1_n = a.u[f + 1];
+      u0_n = vq ? R(0) : a.u[f];
+      u1_n = vq ? R(0) : a.u[f + 1];
     };
     auto issue = [&](int ii) {
       const int sl = (ii - i0) % kESlots;
       const size_t c = cidx(nx, ii, jj);
       const size_t f = c + (size_t)ii;  // fidx(nx, ii, jj)
-      cp_async_elem(&s_in[sl][0][t], a.v + c + nx, true);
+      cp_async_elem(&s_in[sl][0][t], a.v + c + nx, !vq);
       cp_async_elem(&s_in[sl][1][t], a.rho_r + c, true);
       cp_async_elem(&s_in[sl][2][t], a.e_r + c, true);
       const bool qf = qflag_row(ii - i0);
       cp_async_elem(&s_in[sl][3][t], a.Qxx + c, qf);
       cp_async_elem(&s_in[sl][4][t], a.Qyy + c, qf);
-      cp_async_elem(&s_in[sl][5][t], a.u + f, true);
-      cp_async_elem(&s_in[sl][6][t], a.u + f + 1, true);
+      cp_async_elem(&s_in[sl][5][t], a.u + f, !vq);
+      cp_async_elem(&s_in[sl][6][t], a.u + f + 1, !vq);
     };
     if constexpr (kERing) {
 #pragma unroll
@@ -1378,10 +1431,17 @@ __device__ __forceinline__ void tile_mass_sweep_x_impl(const StepArgs<R>& a,
   constexpr int kAhead = Pr::kMixed ? 2 : 3, kSlots = kAhead + 1;
   auto s_ru = ring_slots<R, kEarly ? kSlots : 1, 1, kEarly ? kCols : 1, 6>();
   auto s_rd = ring_slots<double, kEarly ? kSlots : 1, kFirst ? 2 : 3, kEarly ? kCols : 1, 7>();
+  // kFl: a tile whose face velocities are all +0 (velocity flags) does not
+  // load them (its faces are at rest; the ring holds +0).
+  bool vq = false;
+  if constexpr (kFl) {
+    const int cb = pad + bx * (kCols - 1);
+    vq = tile_vel_still(a, i0 - 2, i1 + 2, cb - 3, cb + kCols + 2);
+  }
   auto issue = [&](int ii) {
     const int sl = (ii - i0) % kSlots;
     const size_t c = cidx(nx, ii, jj);
-    cp_async_elem(&s_ru[sl][0][t], face_ok ? a.u + fidx(nx, ii, jj) : a.u, face_ok);
+    cp_async_elem(&s_ru[sl][0][t], face_ok ? a.u + fidx(nx, ii, jj) : a.u, face_ok && !vq);
     cp_async_elem(&s_rd[sl][0][t], cell_ok ? s.r_in + c : s.r_in, cell_ok);
     cp_async_elem(&s_rd[sl][1][t], cell_ok ? s.e_in + c : s.e_in, cell_ok);
     if constexpr (!kFirst) {
@@ -1497,6 +1557,13 @@ __device__ __forceinline__ void tile_mass_sweep_y_impl(const StepArgs<R>& a,
   const bool col_ok = jj < nx - pad;
   const int i1 = min(i0 + a.rows, ny - pad);
   const int last_face = ny - pad;  // the north boundary face row
+  // kFl: a tile whose face velocities are all +0 (velocity flags) does not
+  // load them (its face rows are at rest).
+  bool vq = false;
+  if constexpr (kFl) {
+    const int cb = pad + bx * kCols;
+    vq = tile_vel_still(a, i0 - 3, i1 + 3, cb - 2, cb + kCols + 2);
+  }
   // Windows at face row f: cells f-2..f+1 (densities and energies with their
   // differences), face velocities f-1..f+1 with theirs; each row shifts them
   // by one and forms only the new differences.  In the FP64 form a face row
@@ -1525,9 +1592,9 @@ __device__ __forceinline__ void tile_mass_sweep_y_impl(const StepArgs<R>& a,
   // The windows' first values and the first row's inputs are loaded before
   // the barrier that publishes the row tables (kEarly), else after it.
   auto prime = [&]() {
-    vm = a.v[cidx(nx, i0 - 1, jj)];
-    v0 = a.v[cidx(nx, i0, jj)];
-    vp = a.v[cidx(nx, i0 + 1, jj)];
+    vm = vq ? R(0) : a.v[cidx(nx, i0 - 1, jj)];
+    v0 = vq ? R(0) : a.v[cidx(nx, i0, jj)];
+    vp = vq ? R(0) : a.v[cidx(nx, i0 + 1, jj)];
     R r[4], e[4];
     for (int q = 0; q < 4; ++q) {
       const size_t c = cidx(nx, i0 - 2 + q, jj);
@@ -1555,7 +1622,7 @@ __device__ __forceinline__ void tile_mass_sweep_y_impl(const StepArgs<R>& a,
     const size_t c = cidx(nx, ii + 2, jj);
     cp_async_elem(&s_w[sl][0][t], s.r_in_r + c, true);
     cp_async_elem(&s_w[sl][1][t], s.e_in_r + c, true);
-    cp_async_elem(&s_w[sl][2][t], a.v + c, true);
+    cp_async_elem(&s_w[sl][2][t], a.v + c, !vq);
     if constexpr (kOldRing) cp_async_elem(&s_w[sl][3][t], a.rho + cidx(nx, ii, jj), true);
   };
   auto load_upd = [&](int ii) {
@@ -1864,10 +1931,12 @@ __device__ __forceinline__ bool tile_mass_still(const StepArgs<R>& a, int r0, in
 // its faces: the momentum and both densities are what the Lagrangian phase
 // formed the velocity from, so the advected velocity is the Lagrangian one
 // (w), copied with its ghost images (rows i0 .. i1 - 1 of face column j;
-// kU: x faces).  Loads in batches of eight rows, all in flight together.
+// kU: x faces).  Loads in batches of eight rows, all in flight together;
+// zero: the velocity flags show them all +0, which is stored without a load.
 template <typename R, bool kU>
 __device__ __forceinline__ void copy_velocities(const StepArgs<R>& a, bool edge, const R* w,
-                                                R* vout, int i0, int i1, int j, bool ok) {
+                                                R* vout, int i0, int i1, int j, bool ok,
+                                                bool zero) {
   const int nx = a.nx, ny = a.ny, pad = a.pad;
   constexpr int kB = 8;
   for (int ib = i0; ib < i1; ib += kB) {
@@ -1875,7 +1944,7 @@ __device__ __forceinline__ void copy_velocities(const StepArgs<R>& a, bool edge,
 #pragma unroll
     for (int q = 0; q < kB; ++q) {
       const int ii = ib + q;
-      v[q] = (ok && ii < i1) ? w[kU ? fidx(nx, ii, j) : cidx(nx, ii, j)] : R(0);
+      v[q] = (ok && ii < i1 && !zero) ? w[kU ? fidx(nx, ii, j) : cidx(nx, ii, j)] : R(0);
     }
 #pragma unroll
     for (int q = 0; q < kB; ++q) {
@@ -1932,7 +2001,9 @@ __device__ __forceinline__ void tile_mom_x_impl(const StepArgs<R>& a, int bx, in
     // No mass moves around the tile's faces: the Lagrangian velocities stand.
     if (tile_mass_still(a, i0 - 1, i1, c0 - 1, c0 + kCols)) {
       const bool upd = kV ? (t < kCols - 1 && j < nx - pad) : (t >= 1 && j < nx + 1 - pad);
-      copy_velocities<R, !kV>(a, edge, kV ? a.v : a.u, kV ? a.v_out : a.u_out, i0, i1, j, upd);
+      const bool zero = tile_vel_still(a, i0 - 2, i1 + 2, c0 - 2, c0 + kCols + 2);
+      copy_velocities<R, !kV>(a, edge, kV ? a.v : a.u, kV ? a.v_out : a.u_out, i0, i1, j, upd,
+                              zero);
       return;
     }
   }
@@ -2174,8 +2245,9 @@ __device__ __forceinline__ void tile_mom_y_impl(const StepArgs<R>& a, int bx, in
     // No mass moves around the tile's faces: the Lagrangian velocities stand.
     const int cb = pad + bx * kCols;
     if (tile_mass_still(a, i0 - 1, i1, cb - 1, cb + kCols)) {
+      const bool zero = tile_vel_still(a, i0 - 2, i1 + 2, cb - 2, cb + kCols + 2);
       copy_velocities<R, !kV>(a, edge, kV ? a.v : a.u, kV ? a.v_out : a.u_out, i0, i1, jj,
-                              jj < (kV ? nx - pad : nx + 1 - pad));
+                              jj < (kV ? nx - pad : nx + 1 - pad), zero);
       return;
     }
   }
