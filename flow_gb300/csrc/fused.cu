@@ -390,10 +390,21 @@ void launch_step(cudaStream_t s, const StepArgs<R>& a, int tt,
   StepArgs<R> ad = a;
   if (lag) ad.vflag = nullptr;
   const bool x_first = (tt % 2 == 0);
+  // With flags, the first sweep marks the tiles it skips (in its own grid);
+  // the second reads their cells from the first sweep's input.
+  SweepArgs<R> sw1 = first, sw2 = second;
+  if (a.skipf) {
+    sw1.skip = sw2.skip = a.skipf;
+    sw1.skip_tiles_x = sw2.skip_tiles_x = x_first ? a.fx_stride / 4 : a.qm_stride;
+    sw2.r_alt = first.r_in;
+    sw2.e_alt = first.e_in;
+    sw2.r_alt_r = first.r_in_r;
+    sw2.e_alt_r = first.e_in_r;
+  }
   prof.mark(x_first ? "mass_sweep_x" : "mass_sweep_y");
-  launch_mass(s, ad, !x_first, true, first);
+  launch_mass(s, ad, !x_first, true, sw1);
   prof.mark(x_first ? "mass_sweep_y" : "mass_sweep_x");
-  launch_mass(s, ad, x_first, false, second);
+  launch_mass(s, ad, x_first, false, sw2);
 
   // Momentum: each flux fused with its update, in the reference order; the
   // pair that recomputes a velocity comes first in each chain.
@@ -476,6 +487,7 @@ void fill_mesh_args(StepArgs<R>& a, const Mesh* mesh, int tt, double* ra) {
   a.fx_stride = 0;
   a.vflag = nullptr;
   a.vf_stride = 0;
+  a.skipf = nullptr;
   const int stride = (a.nx - 2 * a.pad + kCols - 1) / kCols;
   const int xtiles = (a.nx + 1 - 2 * a.pad + kCols - 2) / (kCols - 1);
   const long long rows = a.ny - 2 * a.pad;
@@ -483,8 +495,10 @@ void fill_mesh_args(StepArgs<R>& a, const Mesh* mesh, int tt, double* ra) {
   const size_t fx_words = (size_t)rows * xtiles;
   const int vtiles = (a.nx + kCols - 1) / kCols;
   const size_t v_words = (size_t)a.ny * vtiles;
+  const long long bands = (rows + a.rows - 1) / a.rows;
+  const size_t sk_words = ((size_t)bands * (xtiles > stride ? xtiles : stride) + 3) / 4;
   const size_t need = (size_t)kRaQFlags * sizeof(double) +
-                      (q_words + fy_words + fx_words + v_words) * sizeof(unsigned);
+                      (q_words + fy_words + fx_words + v_words + sk_words) * sizeof(unsigned);
   if (stride > 0 && rows > 0 && need <= (size_t)a.nx * a.ny * sizeof(double)) {
     unsigned* base = reinterpret_cast<unsigned*>(ra + kRaQFlags);
     a.qmask = base;
@@ -494,6 +508,7 @@ void fill_mesh_args(StepArgs<R>& a, const Mesh* mesh, int tt, double* ra) {
     a.fx_stride = 4 * xtiles;
     a.vflag = reinterpret_cast<unsigned char*>(base + q_words + fy_words + fx_words);
     a.vf_stride = 4 * vtiles;
+    a.skipf = reinterpret_cast<unsigned char*>(base + q_words + fy_words + fx_words + v_words);
   }
 }
 

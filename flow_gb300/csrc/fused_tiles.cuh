@@ -108,6 +108,10 @@ struct StepArgs {
   // 0, the velocities it would read are +0 and it does not load them.
   unsigned char* vflag;
   int vf_stride;               // bytes per row: 4 ceil(nx / 128)
+  // The sweeps' tile-skip marks (SweepArgs::skip), set with the flags: one
+  // byte per sweep tile, ceil((ny - 2 pad) / rows) bands of
+  // max(ceil((nx + 1 - 2 pad) / 127), qm_stride) tiles.
+  unsigned char* skipf;
 };
 
 // Writes the value of interior point (ii, jj) of a w x h array into each of
@@ -618,6 +622,11 @@ __device__ __forceinline__ void tile_lag_viscosity(const StepArgs<R>& a, int bx,
     if (kFlags && (threadIdx.x & 31) == 0) {
       for (int ii = i0; ii < i1; ++ii, qf += qf_step) store_flag(qf, false);
     }
+    return;
+  }
+  if (kFlags && vq) {
+    // A tile at rest: every stress is +0; only the flags are written.
+    for (int ii = i0; ii < i1; ++ii, qf += qf_step) store_flag(qf, false);
     return;
   }
   // The y stress of row ii uses the limited jumps m0, m1, m2 of v around the
@@ -1362,7 +1371,49 @@ struct SweepArgs {
   double* e_out;
   R* r_out_r;
   R* e_out_r;
+  // Tile skips (the kFl kernels; null otherwise).  The first sweep of a step
+  // marks a tile of its grid (one byte per tile, skip_tiles_x per band of
+  // rows) whose cells are at rest -- every face velocity around them is +0,
+  // so neither sweep moves anything through their faces -- and keep their
+  // energy bit for bit through the density round trip; it stores nothing for
+  // them.  The second sweep reads a cell of a marked tile from r_alt/e_alt
+  // (the first sweep's input, which holds its value), does not store it, and
+  // does nothing at all for a tile of its own whose cells all lie in marked
+  // tiles.
+  unsigned char* skip;
+  int skip_tiles_x;
+  const double* r_alt;
+  const double* e_alt;
+  const R* r_alt_r;
+  const R* e_alt_r;
 };
+
+// The mirror source of a column or row index (identity inside the interior).
+__device__ __forceinline__ int mirror_src(int i, int n, int pad) {
+  return i < pad ? 2 * pad - 1 - i : (i >= n - pad ? 2 * (n - pad) - 1 - i : i);
+}
+
+// Whether every cell of rows r0 .. r1 - 1 in column jj (when ok) takes the
+// density round trip exactly (the sweeps' bit-pattern test for a cell no
+// flux crosses): loads in batches of eight rows.  Block-uniform (barrier).
+__device__ __forceinline__ bool block_round_trip_exact(const double* rho, const double* e,
+                                                       int nx, int r0, int r1, int jj,
+                                                       bool ok) {
+  bool exact = true;
+  constexpr int kB = 8;
+  for (int ib = r0; ib < r1; ib += kB) {
+    double rv[kB], ev[kB];
+#pragma unroll
+    for (int q = 0; q < kB; ++q) {
+      const bool in = ok && ib + q < r1;
+      rv[q] = in ? rho[cidx(nx, ib + q, jj)] : 1.0;
+      ev[q] = in ? e[cidx(nx, ib + q, jj)] : 1.0;
+    }
+#pragma unroll
+    for (int q = 0; q < kB; ++q) exact = exact && d_pow2_product_exact(rv[q], ev[q]);
+  }
+  return __syncthreads_and(exact) != 0;
+}
 
 // x sweep: CTAs own 127 cells and compute the 128 faces around them (the last
 // face is shared with the next CTA and written only by its owner).  In the
@@ -1431,21 +1482,65 @@ __device__ __forceinline__ void tile_mass_sweep_x_impl(const StepArgs<R>& a,
   constexpr int kAhead = Pr::kMixed ? 2 : 3, kSlots = kAhead + 1;
   auto s_ru = ring_slots<R, kEarly ? kSlots : 1, 1, kEarly ? kCols : 1, 6>();
   auto s_rd = ring_slots<double, kEarly ? kSlots : 1, kFirst ? 2 : 3, kEarly ? kCols : 1, 7>();
+  const int cb = pad + bx * (kCols - 1);  // the tile's first cell column
   // kFl: a tile whose face velocities are all +0 (velocity flags) does not
   // load them (its faces are at rest; the ring holds +0).
   bool vq = false;
-  if constexpr (kFl) {
-    const int cb = pad + bx * (kCols - 1);
-    vq = tile_vel_still(a, i0 - 2, i1 + 2, cb - 3, cb + kCols + 2);
+  if constexpr (kFl) vq = tile_vel_still(a, i0 - 2, i1 + 2, cb - 3, cb + kCols + 2);
+  // Tile skips (SweepArgs::skip).  First sweep: a tile at rest in both
+  // directions whose cells take the round trip exactly stores nothing but
+  // its flags.  Second sweep (after the y sweep): the skip marks of this
+  // band's y-sweep tiles tlo .. tlo + 2, which hold every cell it reads.
+  constexpr bool kSkip2 = kFl && !kFirst;
+  if constexpr (kFl && kFirst) {
+    bool sk = tile_vel_still(a, i0 - 2, i1 + 2, cb - 2, cb + kCols + 1);
+    if (sk) sk = block_round_trip_exact(s.r_in, s.e_in, nx, i0, i1, jj, cell_ok);
+    if (t == 0) store_flag(s.skip + (size_t)by * s.skip_tiles_x + bx, sk);
+    if (sk) {
+      for (int ii = i0; ii < i1; ++ii) {
+        store_flag(a.fxflag + (size_t)(ii - pad) * a.fx_stride + 4 * bx + (t >> 5), false);
+      }
+      return;
+    }
+  }
+  const int tlo = max(0, (cb - 2 - pad) >> 7);
+  unsigned sk3 = 0u;
+  if constexpr (kSkip2) {
+    for (int k = 0; k < 3; ++k) {
+      const int tx = tlo + k;
+      if (tx < s.skip_tiles_x && s.skip[(size_t)by * s.skip_tiles_x + tx]) sk3 |= 1u << k;
+    }
+  }
+  // The value of cell column col (this tile's rows) lies in r_alt/e_alt: its
+  // tile was skipped by the first sweep.
+  auto in_alt = [&](int col) -> bool {
+    if constexpr (!kSkip2) {
+      return false;
+    } else {
+      const int q = mirror_src(col, nx, pad) - pad;
+      return ((sk3 >> ((q >> 7) - tlo)) & 1u) != 0u;
+    }
+  };
+  if constexpr (kSkip2) {
+    // Every cell of the tile lies in a skipped tile: at rest, unchanged.
+    if (__syncthreads_and(!cell_ok || in_alt(jj))) {
+      for (int ii = i0; ii < i1; ++ii) {
+        store_flag(a.fxflag + (size_t)(ii - pad) * a.fx_stride + 4 * bx + (t >> 5), false);
+      }
+      return;
+    }
   }
   auto issue = [&](int ii) {
     const int sl = (ii - i0) % kSlots;
     const size_t c = cidx(nx, ii, jj);
+    const bool alt = cell_ok && in_alt(jj);
     cp_async_elem(&s_ru[sl][0][t], face_ok ? a.u + fidx(nx, ii, jj) : a.u, face_ok && !vq);
-    cp_async_elem(&s_rd[sl][0][t], cell_ok ? s.r_in + c : s.r_in, cell_ok);
-    cp_async_elem(&s_rd[sl][1][t], cell_ok ? s.e_in + c : s.e_in, cell_ok);
+    cp_async_elem(&s_rd[sl][0][t], alt ? s.r_alt + c : (cell_ok ? s.r_in + c : s.r_in), cell_ok);
+    cp_async_elem(&s_rd[sl][1][t], alt ? s.e_alt + c : (cell_ok ? s.e_in + c : s.e_in), cell_ok);
     if constexpr (!kFirst) {
-      cp_async_elem(&s_rd[sl][kFirst ? 1 : 2][t], cell_ok ? a.rho + c : a.rho, cell_ok);
+      // The old density (in rho); for a cell of a skipped tile, the value
+      // just read.
+      cp_async_elem(&s_rd[sl][kFirst ? 1 : 2][t], cell_ok ? a.rho + c : a.rho, cell_ok && !alt);
     }
   };
   if constexpr (kEarly) {
@@ -1467,7 +1562,7 @@ __device__ __forceinline__ void tile_mass_sweep_x_impl(const StepArgs<R>& a,
       u0 = s_ru[sl][0][t];
       r_in = s_rd[sl][0][t];
       e_in = s_rd[sl][1][t];
-      r_old = kFirst ? r_in : s_rd[sl][kFirst ? 1 : 2][t];
+      r_old = (kFirst || (cell_ok && in_alt(jj))) ? r_in : s_rd[sl][kFirst ? 1 : 2][t];
       if (ii + kAhead < i1) issue(ii + kAhead);
       cp_async_commit();
     } else {
@@ -1484,10 +1579,12 @@ __device__ __forceinline__ void tile_mass_sweep_x_impl(const StepArgs<R>& a,
     if (face_ok && moves) {
       const size_t f = fidx(nx, ii, jj);
       const size_t c = cidx(nx, ii, jj);
-      mass_energy_flux<R, false, kP2>(a.u[f - 1], u0, a.u[f + 1], s.r_in_r[c - 2],
-                                      s.r_in_r[c - 1], s.r_in_r[c], s.r_in_r[c + 1],
-                                      s.e_in_r[c - 2], s.e_in_r[c - 1], s.e_in_r[c],
-                                      s.e_in_r[c + 1], iex, cxm, cx0, icx_r,
+      // A stencil cell's density and energy (from r_alt/e_alt for a cell of a
+      // skipped tile).
+      auto rr = [&](int d) { return in_alt(jj + d) ? s.r_alt_r[c + d] : s.r_in_r[c + d]; };
+      auto er = [&](int d) { return in_alt(jj + d) ? s.e_alt_r[c + d] : s.e_in_r[c + d]; };
+      mass_energy_flux<R, false, kP2>(a.u[f - 1], u0, a.u[f + 1], rr(-2), rr(-1), rr(0), rr(1),
+                                      er(-2), er(-1), er(0), er(1), iex, cxm, cx0, icx_r,
                                       s_ey0r[k], dt_r, dt_h_r, &F, &eF);
     }
     // kFl: a warp at rest stores only its flag (its fluxes are +0).
@@ -1508,8 +1605,12 @@ __device__ __forceinline__ void tile_mass_sweep_x_impl(const StepArgs<R>& a,
                                          Prec<double>::mulp<kP2>(s_coef[k], icx),
                                          s_ey0[k], s_ey1[k], sF[t],
                                          sF[t + 1], seF[t], seF[t + 1], &r_new, &e_new);
-      store_cell(edge, s.r_out, s.r_out_r, nx, ny, pad, ii, jj, r_new);
-      store_cell(edge, s.e_out, s.e_out_r, nx, ny, pad, ii, jj, e_new);
+      // (A cell of a skipped tile is at rest and keeps its value, which rho
+      // and e hold.)
+      if (!in_alt(jj)) {
+        store_cell(edge, s.r_out, s.r_out_r, nx, ny, pad, ii, jj, r_new);
+        store_cell(edge, s.e_out, s.e_out_r, nx, ny, pad, ii, jj, e_new);
+      }
     }
     __syncthreads();
   }
@@ -1557,13 +1658,59 @@ __device__ __forceinline__ void tile_mass_sweep_y_impl(const StepArgs<R>& a,
   const bool col_ok = jj < nx - pad;
   const int i1 = min(i0 + a.rows, ny - pad);
   const int last_face = ny - pad;  // the north boundary face row
+  const int cb = pad + bx * kCols;  // the tile's first column
   // kFl: a tile whose face velocities are all +0 (velocity flags) does not
   // load them (its face rows are at rest).
   bool vq = false;
-  if constexpr (kFl) {
-    const int cb = pad + bx * kCols;
-    vq = tile_vel_still(a, i0 - 3, i1 + 3, cb - 2, cb + kCols + 2);
+  if constexpr (kFl) vq = tile_vel_still(a, i0 - 3, i1 + 3, cb - 2, cb + kCols + 2);
+  // Tile skips (SweepArgs::skip).  First sweep: a tile at rest in both
+  // directions whose cells take the round trip exactly stores nothing but
+  // its flags.  Second sweep (after the x sweep): the skip marks of this
+  // column's x-sweep tile in bands by - 1 .. by + 1, which hold every cell
+  // it reads (tiles of at least two rows).
+  constexpr bool kSkip2 = kFl && !kFirst;
+  auto store_fy_zero_flags = [&]() {
+    const int f_end = (i1 == last_face) ? last_face : i1 - 1;
+    for (int f = i0; f <= f_end; ++f) {
+      store_flag(a.fyflag + (size_t)(f - pad) * 4 * a.qm_stride + 4 * bx + (threadIdx.x >> 5),
+                 false);
+    }
+  };
+  if constexpr (kFl && kFirst) {
+    bool sk = tile_vel_still(a, i0 - 2, i1 + 2, cb - 2, cb + kCols + 2);
+    if (sk) sk = block_round_trip_exact(s.r_in, s.e_in, nx, i0, i1, jj, col_ok);
+    if (threadIdx.x == 0) store_flag(s.skip + (size_t)by * s.skip_tiles_x + bx, sk);
+    if (sk) {
+      store_fy_zero_flags();
+      return;
+    }
   }
+  unsigned sk3 = 0u;
+  if constexpr (kSkip2) {
+    if (col_ok) {
+      const int xt = (jj - pad) / (kCols - 1);
+      const int nb = (ny - 2 * pad + a.rows - 1) / a.rows;
+      for (int k = 0; k < 3; ++k) {
+        const int b = by - 1 + k;
+        if (b >= 0 && b < nb && s.skip[(size_t)b * s.skip_tiles_x + xt]) sk3 |= 1u << k;
+      }
+    }
+    // Every cell of the tile lies in a skipped tile: at rest, unchanged.
+    if (__syncthreads_and(!col_ok || ((sk3 >> 1) & 1u))) {
+      store_fy_zero_flags();
+      return;
+    }
+  }
+  // The value of this column's cell in row r (i0 - 2 <= r <= i1 + 1) lies
+  // in r_alt/e_alt: its tile was skipped by the first sweep.
+  auto in_alt = [&](int r) -> bool {
+    if constexpr (!kSkip2) {
+      return false;
+    } else {
+      const int rs = mirror_src(r, ny, pad);
+      return ((sk3 >> (rs < i0 ? 0 : (rs >= i1 ? 2 : 1))) & 1u) != 0u;
+    }
+  };
   // Windows at face row f: cells f-2..f+1 (densities and energies with their
   // differences), face velocities f-1..f+1 with theirs; each row shifts them
   // by one and forms only the new differences.  In the FP64 form a face row
@@ -1598,8 +1745,9 @@ __device__ __forceinline__ void tile_mass_sweep_y_impl(const StepArgs<R>& a,
     R r[4], e[4];
     for (int q = 0; q < 4; ++q) {
       const size_t c = cidx(nx, i0 - 2 + q, jj);
-      r[q] = s.r_in_r[c];
-      e[q] = s.e_in_r[c];
+      const bool alt = in_alt(i0 - 2 + q);
+      r[q] = alt ? s.r_alt_r[c] : s.r_in_r[c];
+      e[q] = alt ? s.e_alt_r[c] : s.e_in_r[c];
     }
     rw.m2 = r[0]; rw.m1 = r[1]; rw.p0 = r[2]; rw.p1 = r[3];
     ew.m2 = e[0]; ew.m1 = e[1]; ew.p0 = e[2]; ew.p1 = e[3];
@@ -1620,18 +1768,24 @@ __device__ __forceinline__ void tile_mass_sweep_y_impl(const StepArgs<R>& a,
   auto issue = [&](int ii) {
     const int sl = (ii - i0) % kSlots;
     const size_t c = cidx(nx, ii + 2, jj);
-    cp_async_elem(&s_w[sl][0][t], s.r_in_r + c, true);
-    cp_async_elem(&s_w[sl][1][t], s.e_in_r + c, true);
+    const bool alt = in_alt(ii + 2);
+    cp_async_elem(&s_w[sl][0][t], alt ? s.r_alt_r + c : s.r_in_r + c, true);
+    cp_async_elem(&s_w[sl][1][t], alt ? s.e_alt_r + c : s.e_in_r + c, true);
     cp_async_elem(&s_w[sl][2][t], a.v + c, !vq);
-    if constexpr (kOldRing) cp_async_elem(&s_w[sl][3][t], a.rho + cidx(nx, ii, jj), true);
+    // The old density (in rho); for a cell of a skipped tile, the value the
+    // window holds.
+    if constexpr (kOldRing) {
+      cp_async_elem(&s_w[sl][3][t], a.rho + cidx(nx, ii, jj), !in_alt(ii));
+    }
   };
   auto load_upd = [&](int ii) {
     const size_t c = cidx(nx, ii, jj);
+    const bool alt = in_alt(ii);
     if (Pr::kMixed) {
-      rin_n = s.r_in[c];
-      ein_n = s.e_in[c];
+      rin_n = alt ? s.r_alt[c] : s.r_in[c];
+      ein_n = alt ? s.e_alt[c] : s.e_in[c];
     }
-    if (!kFirst && !kOldRing) rold_n = a.rho[c];
+    if (!kFirst && !kOldRing) rold_n = alt ? rin_n : a.rho[c];
   };
   if (kEarly && col_ok) {
     prime();
@@ -1712,7 +1866,7 @@ __device__ __forceinline__ void tile_mass_sweep_y_impl(const StepArgs<R>& a,
         e_in = ew.p0;
       }
       if constexpr (kOldRing) {
-        r_old = s_w[sl][3][t];
+        r_old = in_alt(ii) ? r_in : s_w[sl][3][t];
       } else {
         r_old = kFirst ? r_in : rold_n;
       }
@@ -1766,8 +1920,12 @@ __device__ __forceinline__ void tile_mass_sweep_y_impl(const StepArgs<R>& a,
                                        a.celldx[jj] * s_cyd[k],
                                        Prec<double>::mulp<kP2>(s_coef[k], icx), ex0, ex1,
                                        f0d, f1d, ef0d, ef1d, &r_new, &e_new);
-    store_cell(edge, s.r_out, s.r_out_r, nx, ny, pad, ii, jj, r_new);
-    store_cell(edge, s.e_out, s.e_out_r, nx, ny, pad, ii, jj, e_new);
+    // (A cell of a skipped tile is at rest and keeps its value, which rho and
+    // e hold.)
+    if (!in_alt(ii)) {
+      store_cell(edge, s.r_out, s.r_out_r, nx, ny, pad, ii, jj, r_new);
+      store_cell(edge, s.e_out, s.e_out_r, nx, ny, pad, ii, jj, e_new);
+    }
     f0d = f1d;
     ef0d = ef1d;
   }
