@@ -396,6 +396,7 @@ void launch_step(cudaStream_t s, const StepArgs<R>& a, int tt,
   if (a.skipf) {
     sw1.skip = sw2.skip = a.skipf;
     sw1.skip_tiles_x = sw2.skip_tiles_x = x_first ? a.fx_stride / 4 : a.qm_stride;
+    sw1.skip_bands = sw2.skip_bands = (ny - 2 * pad + a.rows - 1) / a.rows;
     sw2.r_alt = first.r_in;
     sw2.e_alt = first.e_in;
     sw2.r_alt_r = first.r_in_r;

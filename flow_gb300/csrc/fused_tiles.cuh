@@ -1377,11 +1377,12 @@ struct SweepArgs {
   // so neither sweep moves anything through their faces -- and keep their
   // energy bit for bit through the density round trip; it stores nothing for
   // them.  The second sweep reads a cell of a marked tile from r_alt/e_alt
-  // (the first sweep's input, which holds its value), does not store it, and
-  // does nothing at all for a tile of its own whose cells all lie in marked
-  // tiles.
+  // (the first sweep's input, which holds its value; storing it again writes
+  // that value), and does nothing at all for a tile of its own whose cells
+  // all lie in marked tiles.
   unsigned char* skip;
   int skip_tiles_x;
+  int skip_bands;      // bands of rows
   const double* r_alt;
   const double* e_alt;
   const R* r_alt_r;
@@ -1419,9 +1420,13 @@ __device__ __forceinline__ bool block_round_trip_exact(const double* rho, const 
 // face is shared with the next CTA and written only by its owner).  In the
 // second sweep of a step the old density of a cell is read from rho just
 // before the same thread overwrites that cell.
-template <typename R, bool kFirst, bool kP2, bool kEarly, bool kFl>
+// kAlt (second sweep with flags): some tile near this one was skipped by the
+// first sweep (sk3, the skip marks of this band's y-sweep tiles tlo ..
+// tlo + 2); without it the loads need no selection.
+template <typename R, bool kFirst, bool kP2, bool kEarly, bool kFl, bool kAlt>
 __device__ __forceinline__ void tile_mass_sweep_x_impl(const StepArgs<R>& a,
-                                                       const SweepArgs<R>& s, int bx, int by) {
+                                                       const SweepArgs<R>& s, int bx, int by,
+                                                       unsigned sk3) {
   using Pr = Prec<R>;
   __shared__ R s_ey0r[kMaxRows];
   __shared__ double sF[kCols], seF[kCols];  // the row's face fluxes, widened once
@@ -1432,6 +1437,7 @@ __device__ __forceinline__ void tile_mass_sweep_x_impl(const StepArgs<R>& a,
   const int i0 = pad + by * a.rows;
   const bool edge = tile_near_edge(nx, ny, pad, pad + bx * (kCols - 1), i0, a.rows);
   const double dt = a.dt_slot[0], dt_h = a.dt_slot[1];
+  const int tlo = max(0, (bx * (kCols - 1) - 2) >> 7);
   if (t < a.rows) {
     const int ii = i0 + t;
     if (ii < ny - pad) {
@@ -1483,15 +1489,11 @@ __device__ __forceinline__ void tile_mass_sweep_x_impl(const StepArgs<R>& a,
   auto s_ru = ring_slots<R, kEarly ? kSlots : 1, 1, kEarly ? kCols : 1, 6>();
   auto s_rd = ring_slots<double, kEarly ? kSlots : 1, kFirst ? 2 : 3, kEarly ? kCols : 1, 7>();
   const int cb = pad + bx * (kCols - 1);  // the tile's first cell column
-  // kFl: a tile whose face velocities are all +0 (velocity flags) does not
-  // load them (its faces are at rest; the ring holds +0).
-  bool vq = false;
-  if constexpr (kFl) vq = tile_vel_still(a, i0 - 2, i1 + 2, cb - 3, cb + kCols + 2);
   // Tile skips (SweepArgs::skip).  First sweep: a tile at rest in both
   // directions whose cells take the round trip exactly stores nothing but
   // its flags.  Second sweep (after the y sweep): the skip marks of this
   // band's y-sweep tiles tlo .. tlo + 2, which hold every cell it reads.
-  constexpr bool kSkip2 = kFl && !kFirst;
+  constexpr bool kSkip2 = kFl && !kFirst && kAlt;
   if constexpr (kFl && kFirst) {
     bool sk = tile_vel_still(a, i0 - 2, i1 + 2, cb - 2, cb + kCols + 1);
     if (sk) sk = block_round_trip_exact(s.r_in, s.e_in, nx, i0, i1, jj, cell_ok);
@@ -1503,14 +1505,7 @@ __device__ __forceinline__ void tile_mass_sweep_x_impl(const StepArgs<R>& a,
       return;
     }
   }
-  const int tlo = max(0, (cb - 2 - pad) >> 7);
-  unsigned sk3 = 0u;
-  if constexpr (kSkip2) {
-    for (int k = 0; k < 3; ++k) {
-      const int tx = tlo + k;
-      if (tx < s.skip_tiles_x && s.skip[(size_t)by * s.skip_tiles_x + tx]) sk3 |= 1u << k;
-    }
-  }
+
   // The value of cell column col (this tile's rows) lies in r_alt/e_alt: its
   // tile was skipped by the first sweep.
   auto in_alt = [&](int col) -> bool {
@@ -1534,7 +1529,7 @@ __device__ __forceinline__ void tile_mass_sweep_x_impl(const StepArgs<R>& a,
     const int sl = (ii - i0) % kSlots;
     const size_t c = cidx(nx, ii, jj);
     const bool alt = cell_ok && in_alt(jj);
-    cp_async_elem(&s_ru[sl][0][t], face_ok ? a.u + fidx(nx, ii, jj) : a.u, face_ok && !vq);
+    cp_async_elem(&s_ru[sl][0][t], face_ok ? a.u + fidx(nx, ii, jj) : a.u, face_ok);
     cp_async_elem(&s_rd[sl][0][t], alt ? s.r_alt + c : (cell_ok ? s.r_in + c : s.r_in), cell_ok);
     cp_async_elem(&s_rd[sl][1][t], alt ? s.e_alt + c : (cell_ok ? s.e_in + c : s.e_in), cell_ok);
     if constexpr (!kFirst) {
@@ -1606,11 +1601,9 @@ __device__ __forceinline__ void tile_mass_sweep_x_impl(const StepArgs<R>& a,
                                          s_ey0[k], s_ey1[k], sF[t],
                                          sF[t + 1], seF[t], seF[t + 1], &r_new, &e_new);
       // (A cell of a skipped tile is at rest and keeps its value, which rho
-      // and e hold.)
-      if (!in_alt(jj)) {
-        store_cell(edge, s.r_out, s.r_out_r, nx, ny, pad, ii, jj, r_new);
-        store_cell(edge, s.e_out, s.e_out_r, nx, ny, pad, ii, jj, e_new);
-      }
+      // and e hold: storing it again writes the same value.)
+      store_cell(edge, s.r_out, s.r_out_r, nx, ny, pad, ii, jj, r_new);
+      store_cell(edge, s.e_out, s.e_out_r, nx, ny, pad, ii, jj, e_new);
     }
     __syncthreads();
   }
@@ -1620,16 +1613,37 @@ __device__ __forceinline__ void tile_mass_sweep_x_impl(const StepArgs<R>& a,
 template <typename R, bool kFirst, bool kEarly = true, bool kFl = false>
 __device__ __forceinline__ void tile_mass_sweep_x(const StepArgs<R>& a, const SweepArgs<R>& s,
                                                   int bx, int by) {
-  FLOW_POW2_DISPATCH_ALL(a, a.pad + bx * (kCols - 1), a.pad + by * a.rows,
-                     (tile_mass_sweep_x_impl<R, kFirst, true, kEarly, kFl>(a, s, bx, by)),
-                     (tile_mass_sweep_x_impl<R, kFirst, false, kEarly, kFl>(a, s, bx, by)));
+  if constexpr (kFl && !kFirst) {
+    // The skip marks of this band's y-sweep tiles tlo .. tlo + 2.
+    const int tlo = max(0, (bx * (kCols - 1) - 2) >> 7);
+    unsigned sk3 = 0u;
+    for (int k = 0; k < 3; ++k) {
+      const int tx = tlo + k;
+      if (tx < s.skip_tiles_x && s.skip[(size_t)by * s.skip_tiles_x + tx]) sk3 |= 1u << k;
+    }
+    if (__syncthreads_or(sk3 != 0u)) {
+      FLOW_POW2_DISPATCH_ALL(
+          a, a.pad + bx * (kCols - 1), a.pad + by * a.rows,
+          (tile_mass_sweep_x_impl<R, kFirst, true, kEarly, kFl, true>(a, s, bx, by, sk3)),
+          (tile_mass_sweep_x_impl<R, kFirst, false, kEarly, kFl, true>(a, s, bx, by, sk3)));
+      return;  // (the dispatch returns only after its power-of-two branch)
+    }
+  }
+  FLOW_POW2_DISPATCH_ALL(
+      a, a.pad + bx * (kCols - 1), a.pad + by * a.rows,
+      (tile_mass_sweep_x_impl<R, kFirst, true, kEarly, kFl, false>(a, s, bx, by, 0u)),
+      (tile_mass_sweep_x_impl<R, kFirst, false, kEarly, kFl, false>(a, s, bx, by, 0u)));
 }
 
 // y sweep: each thread marches down its column; face row ii+1 is computed
 // in iteration ii and reused by the cell below.
-template <typename R, bool kFirst, bool kP2, bool kEarly, bool kFl>
+// kAlt (second sweep with flags): some tile near this one was skipped by the
+// first sweep (sk3, the skip marks of bands by - 1 .. by + 1 of this
+// column's x-sweep tile); without it the loads need no selection.
+template <typename R, bool kFirst, bool kP2, bool kEarly, bool kFl, bool kAlt>
 __device__ __forceinline__ void tile_mass_sweep_y_impl(const StepArgs<R>& a,
-                                                       const SweepArgs<R>& s, int bx, int by) {
+                                                       const SweepArgs<R>& s, int bx, int by,
+                                                       unsigned sk3) {
   using Pr = Prec<R>;
   __shared__ R s_iey[kMaxRows + 1], s_cy[kMaxRows + 2], s_icy[kMaxRows + 1];
   __shared__ double s_coef[kMaxRows], s_cyd[kMaxRows];
@@ -1638,6 +1652,7 @@ __device__ __forceinline__ void tile_mass_sweep_y_impl(const StepArgs<R>& a,
   const int i0 = pad + by * a.rows;
   const bool edge = tile_near_edge(nx, ny, pad, pad + bx * kCols, i0, a.rows);
   const double dt = a.dt_slot[0], dt_h = a.dt_slot[1];
+  constexpr bool kSkip2 = kFl && !kFirst && kAlt;
   // Face rows i0 .. i0+a.rows, cell rows i0-1 .. i0+a.rows.
   if (threadIdx.x < a.rows + 2) {
     const int ii = i0 - 1 + threadIdx.x;
@@ -1659,16 +1674,11 @@ __device__ __forceinline__ void tile_mass_sweep_y_impl(const StepArgs<R>& a,
   const int i1 = min(i0 + a.rows, ny - pad);
   const int last_face = ny - pad;  // the north boundary face row
   const int cb = pad + bx * kCols;  // the tile's first column
-  // kFl: a tile whose face velocities are all +0 (velocity flags) does not
-  // load them (its face rows are at rest).
-  bool vq = false;
-  if constexpr (kFl) vq = tile_vel_still(a, i0 - 3, i1 + 3, cb - 2, cb + kCols + 2);
   // Tile skips (SweepArgs::skip).  First sweep: a tile at rest in both
   // directions whose cells take the round trip exactly stores nothing but
   // its flags.  Second sweep (after the x sweep): the skip marks of this
   // column's x-sweep tile in bands by - 1 .. by + 1, which hold every cell
   // it reads (tiles of at least two rows).
-  constexpr bool kSkip2 = kFl && !kFirst;
   auto store_fy_zero_flags = [&]() {
     const int f_end = (i1 == last_face) ? last_face : i1 - 1;
     for (int f = i0; f <= f_end; ++f) {
@@ -1685,16 +1695,7 @@ __device__ __forceinline__ void tile_mass_sweep_y_impl(const StepArgs<R>& a,
       return;
     }
   }
-  unsigned sk3 = 0u;
   if constexpr (kSkip2) {
-    if (col_ok) {
-      const int xt = (jj - pad) / (kCols - 1);
-      const int nb = (ny - 2 * pad + a.rows - 1) / a.rows;
-      for (int k = 0; k < 3; ++k) {
-        const int b = by - 1 + k;
-        if (b >= 0 && b < nb && s.skip[(size_t)b * s.skip_tiles_x + xt]) sk3 |= 1u << k;
-      }
-    }
     // Every cell of the tile lies in a skipped tile: at rest, unchanged.
     if (__syncthreads_and(!col_ok || ((sk3 >> 1) & 1u))) {
       store_fy_zero_flags();
@@ -1739,9 +1740,9 @@ __device__ __forceinline__ void tile_mass_sweep_y_impl(const StepArgs<R>& a,
   // The windows' first values and the first row's inputs are loaded before
   // the barrier that publishes the row tables (kEarly), else after it.
   auto prime = [&]() {
-    vm = vq ? R(0) : a.v[cidx(nx, i0 - 1, jj)];
-    v0 = vq ? R(0) : a.v[cidx(nx, i0, jj)];
-    vp = vq ? R(0) : a.v[cidx(nx, i0 + 1, jj)];
+    vm = a.v[cidx(nx, i0 - 1, jj)];
+    v0 = a.v[cidx(nx, i0, jj)];
+    vp = a.v[cidx(nx, i0 + 1, jj)];
     R r[4], e[4];
     for (int q = 0; q < 4; ++q) {
       const size_t c = cidx(nx, i0 - 2 + q, jj);
@@ -1771,7 +1772,7 @@ __device__ __forceinline__ void tile_mass_sweep_y_impl(const StepArgs<R>& a,
     const bool alt = in_alt(ii + 2);
     cp_async_elem(&s_w[sl][0][t], alt ? s.r_alt_r + c : s.r_in_r + c, true);
     cp_async_elem(&s_w[sl][1][t], alt ? s.e_alt_r + c : s.e_in_r + c, true);
-    cp_async_elem(&s_w[sl][2][t], a.v + c, !vq);
+    cp_async_elem(&s_w[sl][2][t], a.v + c, true);
     // The old density (in rho); for a cell of a skipped tile, the value the
     // window holds.
     if constexpr (kOldRing) {
@@ -1921,11 +1922,9 @@ __device__ __forceinline__ void tile_mass_sweep_y_impl(const StepArgs<R>& a,
                                        Prec<double>::mulp<kP2>(s_coef[k], icx), ex0, ex1,
                                        f0d, f1d, ef0d, ef1d, &r_new, &e_new);
     // (A cell of a skipped tile is at rest and keeps its value, which rho and
-    // e hold.)
-    if (!in_alt(ii)) {
-      store_cell(edge, s.r_out, s.r_out_r, nx, ny, pad, ii, jj, r_new);
-      store_cell(edge, s.e_out, s.e_out_r, nx, ny, pad, ii, jj, e_new);
-    }
+    // e hold: storing it again writes the same value.)
+    store_cell(edge, s.r_out, s.r_out_r, nx, ny, pad, ii, jj, r_new);
+    store_cell(edge, s.e_out, s.e_out_r, nx, ny, pad, ii, jj, e_new);
     f0d = f1d;
     ef0d = ef1d;
   }
@@ -1943,9 +1942,31 @@ __device__ __forceinline__ void tile_mass_sweep_y_impl(const StepArgs<R>& a,
 template <typename R, bool kFirst, bool kEarly = true, bool kFl = false>
 __device__ __forceinline__ void tile_mass_sweep_y(const StepArgs<R>& a, const SweepArgs<R>& s,
                                                   int bx, int by) {
-  FLOW_POW2_DISPATCH_ALL(a, a.pad + bx * kCols, a.pad + by * a.rows,
-                     (tile_mass_sweep_y_impl<R, kFirst, true, kEarly, kFl>(a, s, bx, by)),
-                     (tile_mass_sweep_y_impl<R, kFirst, false, kEarly, kFl>(a, s, bx, by)));
+  if constexpr (kFl && !kFirst) {
+    // The skip marks of bands by - 1 .. by + 1 of this column's x-sweep tile.
+    const int jj = a.pad + bx * kCols + threadIdx.x;
+    unsigned sk3 = 0u;
+    if (jj < a.nx - a.pad) {
+      const int xt = (jj - a.pad) / (kCols - 1);
+      for (int k = 0; k < 3; ++k) {
+        const int b = by - 1 + k;
+        if (b >= 0 && b < s.skip_bands && s.skip[(size_t)b * s.skip_tiles_x + xt]) {
+          sk3 |= 1u << k;
+        }
+      }
+    }
+    if (__syncthreads_or(sk3 != 0u)) {
+      FLOW_POW2_DISPATCH_ALL(
+          a, a.pad + bx * kCols, a.pad + by * a.rows,
+          (tile_mass_sweep_y_impl<R, kFirst, true, kEarly, kFl, true>(a, s, bx, by, sk3)),
+          (tile_mass_sweep_y_impl<R, kFirst, false, kEarly, kFl, true>(a, s, bx, by, sk3)));
+      return;  // (the dispatch returns only after its power-of-two branch)
+    }
+  }
+  FLOW_POW2_DISPATCH_ALL(
+      a, a.pad + bx * kCols, a.pad + by * a.rows,
+      (tile_mass_sweep_y_impl<R, kFirst, true, kEarly, kFl, false>(a, s, bx, by, 0u)),
+      (tile_mass_sweep_y_impl<R, kFirst, false, kEarly, kFl, false>(a, s, bx, by, 0u)));
 }
 
 // ===========================================================================
