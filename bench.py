@@ -55,24 +55,24 @@ B_ALG_MIXED = 48     # rho, e (FP64) and rho_u, rho_v (FP32), each read + writte
 # mass fluxes, the changed energies and momenta) counts as nothing.
 KERNEL_BYTES_PER_CELL = {
     "lag_pressure": 8 * 7,       # rho, e, rho_u, rho_v in; P, u, v out
-    "lag_viscosity": 8 * 3,      # u, v, rho in (Qxx, Qyy out where a stress is not +0)
+    "lag_viscosity": 0,          # u, v, rho where a velocity is not +0; Q where a stress is not
     "lag_viscous_accel": 0,      # stresses, momenta, velocities only where a stress gradient acts
-    "lag_energy_dt": 8 * 4,      # rho, e, u, v in (P, Q in and e out where a cell is compressed)
+    "lag_energy_dt": 8 * 2,      # rho, e in for the CFL minimum (u, v, P, Q, e out where moving)
     "lag_fused": 8 * 6,          # one-kernel Lagrangian phase: rho, e, rho_u, rho_v in; u, v out
     "lag_apply": 0,              # changed values only
-    # The sweeps: rho, e and the face velocity in, rho, e out (the mass fluxes
-    # where faces move); the second sweep of a step also reads the old
-    # density, and each direction is the second sweep every other step.
-    "mass_sweep_x": 8 * 5 + 4,
-    "mass_sweep_y": 8 * 5 + 4,
+    # The sweeps: the first sweep of a step reads rho and e to test a still
+    # tile's round trip (16 B); the second moves nothing in tiles the first
+    # skipped.  Each direction is the first sweep every other step.
+    "mass_sweep_x": 8,
+    "mass_sweep_y": 8,
     # Momentum pairs (flux fused with its update), one launch per step each:
-    # every other step's launch recomputes the velocity (momentum, density
-    # in, velocity out: 24 B); the other launch moves bytes only where mass
-    # moves.  Half of 24 B counts per launch.
-    "mom_uFx": 12,
-    "mom_uFy": 12,
-    "mom_vFx": 12,
-    "mom_vFy": 12,
+    # every other step's launch stores the velocity (8 B, +0 where the
+    # velocity flags show it); the other launch moves bytes only where mass
+    # moves.  Half of 8 B counts per launch.
+    "mom_uFx": 4,
+    "mom_uFy": 4,
+    "mom_vFx": 4,
+    "mom_vFy": 4,
     "mesh_pow2": 0,              # the step's one-block mesh test (spacings only)
 }
 
