@@ -959,6 +959,35 @@ __device__ __forceinline__ void tile_lag_energy_dt_impl(const StepArgs<R>& a, in
       cp_async_elem(&s_in[sl][5][t], a.u + f, !vq);
       cp_async_elem(&s_in[sl][6][t], a.u + f + 1, !vq);
     };
+    // The CFL candidates of the cell in tile row k from S = c_s^2 + 2 Q / rho
+    // along x and y (e_neg: its energy is negative).
+    auto cfl_candidates = [&](int k, R sx, R sy, bool e_neg) {
+      if constexpr (Pr::kMixed) {
+        const unsigned long long mx = (unsigned long long)dbits(Pr::to_d(cx * Pr::rsqrt(sx)));
+        const unsigned long long my =
+            (unsigned long long)dbits(Pr::to_d(s_cy[k] * Pr::rsqrt(sy)));
+        const unsigned long long m = (mx < my) ? mx : my;
+        best = (!e_neg && m < best) ? m : best;
+      } else {
+        // Rank the candidates by the key S / h^2 = 1/dt^2 (the largest key
+        // is the smallest dt) and take the square root only for the
+        // thread's winner after the loop.  Keys in [+0, +inf] only: a
+        // negative or NaN S is a NaN candidate in the reference.
+        const long long kx = e_neg ? -1 : dbits(Prec<double>::mulp<kP2>(sx, icx2));
+        const long long ky = e_neg ? -1 : dbits(Prec<double>::mulp<kP2>(sy, s_icy2[k]));
+        if (kx >= 0 && kx <= 0x7ff0000000000000LL && kx > kbest) {
+          kbest = kx;
+          s_best = sx;
+          c_best = cx;
+        }
+        if (ky >= 0 && ky <= 0x7ff0000000000000LL && ky > kbest) {
+          kbest = ky;
+          s_best = sy;
+          c_best = s_cy[k];
+        }
+      }
+    };
+    if (!vq) {
     if constexpr (kERing) {
 #pragma unroll
       for (int d = 0; d < kEAhead; ++d) {
@@ -1043,33 +1072,40 @@ __device__ __forceinline__ void tile_lag_energy_dt_impl(const StepArgs<R>& a, in
         sy = fma(qy, two_inv_r, s2);
       }
       const bool e_neg = Pr::kMixed ? (e_nr < R(0)) : d_lt0(e_new);
-      if constexpr (Pr::kMixed) {
-        const unsigned long long mx = (unsigned long long)dbits(Pr::to_d(cx * Pr::rsqrt(sx)));
-        const unsigned long long my =
-            (unsigned long long)dbits(Pr::to_d(s_cy[k] * Pr::rsqrt(sy)));
-        const unsigned long long m = (mx < my) ? mx : my;
-        best = (!e_neg && m < best) ? m : best;
-      } else {
-        // Rank the candidates by the key S / h^2 = 1/dt^2 (the largest key
-        // is the smallest dt) and take the square root only for the
-        // thread's winner after the loop.  Keys in [+0, +inf] only: a
-        // negative or NaN S is a NaN candidate in the reference.
-        const long long kx = e_neg ? -1 : dbits(Prec<double>::mulp<kP2>(sx, icx2));
-        const long long ky = e_neg ? -1 : dbits(Prec<double>::mulp<kP2>(sy, s_icy2[k]));
-        if (kx >= 0 && kx <= 0x7ff0000000000000LL && kx > kbest) {
-          kbest = kx;
-          s_best = sx;
-          c_best = cx;
-        }
-        if (ky >= 0 && ky <= 0x7ff0000000000000LL && ky > kbest) {
-          kbest = ky;
-          s_best = sy;
-          c_best = s_cy[k];
-        }
-      }
+      cfl_candidates(k, sx, sy, e_neg);
       v0 = v1;
     }
     if constexpr (kERing) cp_async_wait<0>();
+    } else {
+      // A tile at rest (velocity flags): every cell takes the still path
+      // above on +0 velocities, with no viscous stress -- the energy stays
+      // (a cell without mass takes 0) and the CFL candidates come from the
+      // energy alone -- reading only the density and energy, four rows in
+      // flight together, without the copy ring.
+      constexpr int kB = 4;
+      for (int ib = i0; ib < i1; ib += kB) {
+        R rv[kB], ev[kB];
+#pragma unroll
+        for (int q = 0; q < kB; ++q) {
+          const bool in = ib + q < i1;
+          const size_t c = cidx(nx, in ? ib + q : i0, jj);
+          rv[q] = in ? a.rho_r[c] : R(0);
+          ev[q] = in ? a.e_r[c] : R(0);
+        }
+#pragma unroll
+        for (int q = 0; q < kB; ++q) {
+          const int ii = ib + q;
+          if (ii < i1) {
+            const bool rz = Pr::is_zero(rv[q]);
+            if (rz) store_cell(edge, a.e, a.e_r, nx, ny, pad, ii, jj, 0.0);
+            const R e_nr = rz ? Pr::from_d(0.0) : ev[q];
+            const R s2 = R(kGam * (kGam - 1.0)) * e_nr;
+            const bool e_neg = Pr::kMixed ? (e_nr < R(0)) : d_lt0(rz ? 0.0 : double(ev[q]));
+            cfl_candidates(ii - i0, s2, s2, e_neg);
+          }
+        }
+      }
+    }
   }
   if (!Pr::kMixed && kbest >= 0) best = (unsigned long long)dbits(c_best * d_rsqrt(s_best));
   best = warp_min_u64(best);
