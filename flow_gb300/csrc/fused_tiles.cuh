@@ -1524,23 +1524,11 @@ __device__ __forceinline__ void tile_mass_sweep_x_impl(const StepArgs<R>& a,
   constexpr int kAhead = Pr::kMixed ? 2 : 3, kSlots = kAhead + 1;
   auto s_ru = ring_slots<R, kEarly ? kSlots : 1, 1, kEarly ? kCols : 1, 6>();
   auto s_rd = ring_slots<double, kEarly ? kSlots : 1, kFirst ? 2 : 3, kEarly ? kCols : 1, 7>();
-  const int cb = pad + bx * (kCols - 1);  // the tile's first cell column
   // Tile skips (SweepArgs::skip).  First sweep: a tile at rest in both
   // directions whose cells take the round trip exactly stores nothing but
   // its flags.  Second sweep (after the y sweep): the skip marks of this
   // band's y-sweep tiles tlo .. tlo + 2, which hold every cell it reads.
   constexpr bool kSkip2 = kFl && !kFirst && kAlt;
-  if constexpr (kFl && kFirst) {
-    bool sk = tile_vel_still(a, i0 - 2, i1 + 2, cb - 2, cb + kCols + 1);
-    if (sk) sk = block_round_trip_exact(s.r_in, s.e_in, nx, i0, i1, jj, cell_ok);
-    if (t == 0) store_flag(s.skip + (size_t)by * s.skip_tiles_x + bx, sk);
-    if (sk) {
-      for (int ii = i0; ii < i1; ++ii) {
-        store_flag(a.fxflag + (size_t)(ii - pad) * a.fx_stride + 4 * bx + (t >> 5), false);
-      }
-      return;
-    }
-  }
 
   // The value of cell column col (this tile's rows) lies in r_alt/e_alt: its
   // tile was skipped by the first sweep.
@@ -1552,15 +1540,6 @@ __device__ __forceinline__ void tile_mass_sweep_x_impl(const StepArgs<R>& a,
       return ((sk3 >> ((q >> 7) - tlo)) & 1u) != 0u;
     }
   };
-  if constexpr (kSkip2) {
-    // Every cell of the tile lies in a skipped tile: at rest, unchanged.
-    if (__syncthreads_and(!cell_ok || in_alt(jj))) {
-      for (int ii = i0; ii < i1; ++ii) {
-        store_flag(a.fxflag + (size_t)(ii - pad) * a.fx_stride + 4 * bx + (t >> 5), false);
-      }
-      return;
-    }
-  }
   auto issue = [&](int ii) {
     const int sl = (ii - i0) % kSlots;
     const size_t c = cidx(nx, ii, jj);
@@ -1649,20 +1628,47 @@ __device__ __forceinline__ void tile_mass_sweep_x_impl(const StepArgs<R>& a,
 template <typename R, bool kFirst, bool kEarly = true, bool kFl = false>
 __device__ __forceinline__ void tile_mass_sweep_x(const StepArgs<R>& a, const SweepArgs<R>& s,
                                                   int bx, int by) {
-  if constexpr (kFl && !kFirst) {
-    // The skip marks of this band's y-sweep tiles tlo .. tlo + 2.
-    const int tlo = max(0, (bx * (kCols - 1) - 2) >> 7);
-    unsigned sk3 = 0u;
-    for (int k = 0; k < 3; ++k) {
-      const int tx = tlo + k;
-      if (tx < s.skip_tiles_x && s.skip[(size_t)by * s.skip_tiles_x + tx]) sk3 |= 1u << k;
-    }
-    if (__syncthreads_or(sk3 != 0u)) {
-      FLOW_POW2_DISPATCH_ALL(
-          a, a.pad + bx * (kCols - 1), a.pad + by * a.rows,
-          (tile_mass_sweep_x_impl<R, kFirst, true, kEarly, kFl, true>(a, s, bx, by, sk3)),
-          (tile_mass_sweep_x_impl<R, kFirst, false, kEarly, kFl, true>(a, s, bx, by, sk3)));
-      return;  // (the dispatch returns only after its power-of-two branch)
+  if constexpr (kFl) {
+    // Tile skips (SweepArgs::skip), decided before any other work.
+    const int pad = a.pad, t = threadIdx.x;
+    const int cb = pad + bx * (kCols - 1), jj = cb + t;
+    const int i0 = pad + by * a.rows, i1 = min(i0 + a.rows, a.ny - pad);
+    const bool cell_ok = t < kCols - 1 && jj < a.nx - pad;
+    auto zero_flags = [&]() {  // the mass-flux flags of a tile at rest
+      for (int ii = i0; ii < i1; ++ii) {
+        store_flag(a.fxflag + (size_t)(ii - pad) * a.fx_stride + 4 * bx + (t >> 5), false);
+      }
+    };
+    if constexpr (kFirst) {
+      // At rest in both directions, and every cell's round trip exact.
+      bool sk = tile_vel_still(a, i0 - 2, i1 + 2, cb - 2, cb + kCols + 1);
+      if (sk) sk = block_round_trip_exact(s.r_in, s.e_in, a.nx, i0, i1, jj, cell_ok);
+      if (t == 0) store_flag(s.skip + (size_t)by * s.skip_tiles_x + bx, sk);
+      if (sk) {
+        zero_flags();
+        return;
+      }
+    } else {
+      // The skip marks of this band's y-sweep tiles tlo .. tlo + 2.
+      const int tlo = max(0, (bx * (kCols - 1) - 2) >> 7);
+      unsigned sk3 = 0u;
+      for (int k = 0; k < 3; ++k) {
+        const int tx = tlo + k;
+        if (tx < s.skip_tiles_x && s.skip[(size_t)by * s.skip_tiles_x + tx]) sk3 |= 1u << k;
+      }
+      // Every cell of the tile lies in a skipped tile: at rest, unchanged.
+      const int q = jj - pad;
+      if (__syncthreads_and(!cell_ok || ((sk3 >> ((q >> 7) - tlo)) & 1u))) {
+        zero_flags();
+        return;
+      }
+      if (__syncthreads_or(sk3 != 0u)) {
+        FLOW_POW2_DISPATCH_ALL(
+            a, a.pad + bx * (kCols - 1), a.pad + by * a.rows,
+            (tile_mass_sweep_x_impl<R, kFirst, true, kEarly, kFl, true>(a, s, bx, by, sk3)),
+            (tile_mass_sweep_x_impl<R, kFirst, false, kEarly, kFl, true>(a, s, bx, by, sk3)));
+        return;  // (the dispatch returns only after its power-of-two branch)
+      }
     }
   }
   FLOW_POW2_DISPATCH_ALL(
@@ -1709,35 +1715,11 @@ __device__ __forceinline__ void tile_mass_sweep_y_impl(const StepArgs<R>& a,
   const bool col_ok = jj < nx - pad;
   const int i1 = min(i0 + a.rows, ny - pad);
   const int last_face = ny - pad;  // the north boundary face row
-  const int cb = pad + bx * kCols;  // the tile's first column
   // Tile skips (SweepArgs::skip).  First sweep: a tile at rest in both
   // directions whose cells take the round trip exactly stores nothing but
   // its flags.  Second sweep (after the x sweep): the skip marks of this
   // column's x-sweep tile in bands by - 1 .. by + 1, which hold every cell
   // it reads (tiles of at least two rows).
-  auto store_fy_zero_flags = [&]() {
-    const int f_end = (i1 == last_face) ? last_face : i1 - 1;
-    for (int f = i0; f <= f_end; ++f) {
-      store_flag(a.fyflag + (size_t)(f - pad) * 4 * a.qm_stride + 4 * bx + (threadIdx.x >> 5),
-                 false);
-    }
-  };
-  if constexpr (kFl && kFirst) {
-    bool sk = tile_vel_still(a, i0 - 2, i1 + 2, cb - 2, cb + kCols + 2);
-    if (sk) sk = block_round_trip_exact(s.r_in, s.e_in, nx, i0, i1, jj, col_ok);
-    if (threadIdx.x == 0) store_flag(s.skip + (size_t)by * s.skip_tiles_x + bx, sk);
-    if (sk) {
-      store_fy_zero_flags();
-      return;
-    }
-  }
-  if constexpr (kSkip2) {
-    // Every cell of the tile lies in a skipped tile: at rest, unchanged.
-    if (__syncthreads_and(!col_ok || ((sk3 >> 1) & 1u))) {
-      store_fy_zero_flags();
-      return;
-    }
-  }
   // The value of this column's cell in row r (i0 - 2 <= r <= i1 + 1) lies
   // in r_alt/e_alt: its tile was skipped by the first sweep.
   auto in_alt = [&](int r) -> bool {
@@ -1978,25 +1960,53 @@ __device__ __forceinline__ void tile_mass_sweep_y_impl(const StepArgs<R>& a,
 template <typename R, bool kFirst, bool kEarly = true, bool kFl = false>
 __device__ __forceinline__ void tile_mass_sweep_y(const StepArgs<R>& a, const SweepArgs<R>& s,
                                                   int bx, int by) {
-  if constexpr (kFl && !kFirst) {
-    // The skip marks of bands by - 1 .. by + 1 of this column's x-sweep tile.
-    const int jj = a.pad + bx * kCols + threadIdx.x;
-    unsigned sk3 = 0u;
-    if (jj < a.nx - a.pad) {
-      const int xt = (jj - a.pad) / (kCols - 1);
-      for (int k = 0; k < 3; ++k) {
-        const int b = by - 1 + k;
-        if (b >= 0 && b < s.skip_bands && s.skip[(size_t)b * s.skip_tiles_x + xt]) {
-          sk3 |= 1u << k;
+  if constexpr (kFl) {
+    // Tile skips (SweepArgs::skip), decided before any other work.
+    const int pad = a.pad;
+    const int cb = pad + bx * kCols, jj = cb + threadIdx.x;
+    const int i0 = pad + by * a.rows, i1 = min(i0 + a.rows, a.ny - pad);
+    const bool col_ok = jj < a.nx - pad;
+    auto zero_flags = [&]() {  // the mass-flux flags of a tile at rest
+      const int last_face = a.ny - pad;
+      const int f_end = (i1 == last_face) ? last_face : i1 - 1;
+      for (int f = i0; f <= f_end; ++f) {
+        store_flag(a.fyflag + (size_t)(f - pad) * 4 * a.qm_stride + 4 * bx + (threadIdx.x >> 5),
+                   false);
+      }
+    };
+    if constexpr (kFirst) {
+      // At rest in both directions, and every cell's round trip exact.
+      bool sk = tile_vel_still(a, i0 - 2, i1 + 2, cb - 2, cb + kCols + 2);
+      if (sk) sk = block_round_trip_exact(s.r_in, s.e_in, a.nx, i0, i1, jj, col_ok);
+      if (threadIdx.x == 0) store_flag(s.skip + (size_t)by * s.skip_tiles_x + bx, sk);
+      if (sk) {
+        zero_flags();
+        return;
+      }
+    } else {
+      // The skip marks of bands by - 1 .. by + 1 of this column's x-sweep tile.
+      unsigned sk3 = 0u;
+      if (col_ok) {
+        const int xt = (jj - pad) / (kCols - 1);
+        for (int k = 0; k < 3; ++k) {
+          const int b = by - 1 + k;
+          if (b >= 0 && b < s.skip_bands && s.skip[(size_t)b * s.skip_tiles_x + xt]) {
+            sk3 |= 1u << k;
+          }
         }
       }
-    }
-    if (__syncthreads_or(sk3 != 0u)) {
-      FLOW_POW2_DISPATCH_ALL(
-          a, a.pad + bx * kCols, a.pad + by * a.rows,
-          (tile_mass_sweep_y_impl<R, kFirst, true, kEarly, kFl, true>(a, s, bx, by, sk3)),
-          (tile_mass_sweep_y_impl<R, kFirst, false, kEarly, kFl, true>(a, s, bx, by, sk3)));
-      return;  // (the dispatch returns only after its power-of-two branch)
+      // Every cell of the tile lies in a skipped tile: at rest, unchanged.
+      if (__syncthreads_and(!col_ok || ((sk3 >> 1) & 1u))) {
+        zero_flags();
+        return;
+      }
+      if (__syncthreads_or(sk3 != 0u)) {
+        FLOW_POW2_DISPATCH_ALL(
+            a, a.pad + bx * kCols, a.pad + by * a.rows,
+            (tile_mass_sweep_y_impl<R, kFirst, true, kEarly, kFl, true>(a, s, bx, by, sk3)),
+            (tile_mass_sweep_y_impl<R, kFirst, false, kEarly, kFl, true>(a, s, bx, by, sk3)));
+        return;  // (the dispatch returns only after its power-of-two branch)
+      }
     }
   }
   FLOW_POW2_DISPATCH_ALL(
