@@ -107,6 +107,7 @@ def _declare(L: ctypes.CDLL) -> None:
         "gb300_get_mode": [],
         "gb300_set_verbose": [I],
         "gb300_synchronize": [],
+        "gb300_state_changed": [],
         "gb300_solve_hydro_2d": [M, I] + [P] * 17,
         "gb300_conservation": [I, I, I, P, P, P, P, I],
         "gb300_conservation_noalloc": [I, I, I, P, P, P],

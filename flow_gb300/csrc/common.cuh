@@ -34,9 +34,11 @@ constexpr double kCT = 0.3;
 //                             (formed on the device at the start of a step)
 //   [8 ...]                   per-block partials (2 doubles per block, at
 //                             most kMaxReduceBlocks blocks)
-//   [kRaQFlags ...]           viscous-stress flags of the fused step (one
-//                             byte per 32 interior cells of a row), when the
-//                             array is large enough to hold them
+//   [kRaQFlags ...]           the fused step's tile flags, when the array
+//                             is large enough to hold them: per-tile CFL
+//                             minima, then the viscous-stress, mass-flux and
+//                             velocity flags and the two halves of the
+//                             sweeps' skip marks (fused.cu, fill_mesh_args)
 enum : int {
   kRaDt = 0,
   kRaDtH = 1,

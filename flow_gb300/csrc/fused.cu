@@ -1,6 +1,7 @@
 // fused.cu -- the single-problem fused timestep (FP64 form behind
 // solve_hydro_2d, and the mixed form gb300_mixed_solve): one kernel launch per
 // phase, each CTA running one tile function of fused_tiles.cuh.
+#include <array>
 #include <cstddef>
 
 #include "../../include/flow_gb300.h"
@@ -489,6 +490,9 @@ void fill_mesh_args(StepArgs<R>& a, const Mesh* mesh, int tt, double* ra) {
   a.vflag = nullptr;
   a.vf_stride = 0;
   a.skipf = nullptr;
+  a.rest = nullptr;
+  a.rest_w = a.rest_tiles_x = a.rest_rows = 0;
+  a.cfl_tile = nullptr;
   const int stride = (a.nx - 2 * a.pad + kCols - 1) / kCols;
   const int xtiles = (a.nx + 1 - 2 * a.pad + kCols - 2) / (kCols - 1);
   const long long rows = a.ny - 2 * a.pad;
@@ -498,10 +502,17 @@ void fill_mesh_args(StepArgs<R>& a, const Mesh* mesh, int tt, double* ra) {
   const size_t v_words = (size_t)a.ny * vtiles;
   const long long bands = (rows + a.rows - 1) / a.rows;
   const size_t sk_words = ((size_t)bands * (xtiles > stride ? xtiles : stride) + 3) / 4;
+  // Per-tile CFL minima (8 bytes per shock-heating tile) first, then the
+  // 4-byte words: stresses, y fluxes, x fluxes, velocities, and the skip
+  // marks of even and odd steps (a step's first sweep writes its own half;
+  // the next step reads it while its own first sweep writes the other).
+  const size_t cfl_words = 2 * (size_t)bands * stride;
   const size_t need = (size_t)kRaQFlags * sizeof(double) +
-                      (q_words + fy_words + fx_words + v_words + sk_words) * sizeof(unsigned);
+                      (cfl_words + q_words + fy_words + fx_words + v_words + 2 * sk_words) *
+                          sizeof(unsigned);
   if (stride > 0 && rows > 0 && need <= (size_t)a.nx * a.ny * sizeof(double)) {
-    unsigned* base = reinterpret_cast<unsigned*>(ra + kRaQFlags);
+    a.cfl_tile = reinterpret_cast<unsigned long long*>(ra + kRaQFlags);
+    unsigned* base = reinterpret_cast<unsigned*>(ra + kRaQFlags) + cfl_words;
     a.qmask = base;
     a.qm_stride = stride;
     a.fyflag = reinterpret_cast<unsigned char*>(base + q_words);
@@ -509,7 +520,15 @@ void fill_mesh_args(StepArgs<R>& a, const Mesh* mesh, int tt, double* ra) {
     a.fx_stride = 4 * xtiles;
     a.vflag = reinterpret_cast<unsigned char*>(base + q_words + fy_words + fx_words);
     a.vf_stride = 4 * vtiles;
-    a.skipf = reinterpret_cast<unsigned char*>(base + q_words + fy_words + fx_words + v_words);
+    unsigned* marks = base + q_words + fy_words + fx_words + v_words;
+    a.skipf = reinterpret_cast<unsigned char*>(marks + (tt & 1) * sk_words);
+    // The previous step's half, described; used only where rest_valid says
+    // that step was a flagged step on these arrays.
+    a.rest = reinterpret_cast<unsigned char*>(marks + ((tt + 1) & 1) * sk_words);
+    const bool prev_x_first = ((tt - 1) % 2 == 0);
+    a.rest_w = prev_x_first ? kCols - 1 : kCols;
+    a.rest_tiles_x = prev_x_first ? xtiles : stride;
+    a.rest_rows = a.rows;
   }
 }
 
@@ -566,6 +585,41 @@ __global__ void k_make_shadows(size_t n, const double* rho, const double* e,
 namespace {
 // Output rows per CTA of the one-kernel Lagrangian phase.
 int g_lag_rows = lagf::kDefaultRows;
+
+// The last flagged step this thread ran, with what identifies its arrays: the
+// step after it (and only that one) may take its tile marks (StepArgs::rest)
+// and its per-tile CFL minima.
+struct RestRecord {
+  std::array<const void*, 12> arrays{};
+  int nx = 0, ny = 0, pad = 0, form = -1, tt = 0;
+  unsigned long long calls = 0;
+  bool valid = false;
+};
+thread_local RestRecord t_rest;
+
+// Keeps a.rest only when this step directly follows the recorded one on the
+// same arrays (and no other mesh call came between), then records this step
+// as the one the next may follow (when it runs with flags).
+template <typename R>
+void take_rest(StepArgs<R>& a, int tt, int form, const std::array<const void*, 12>& arrays,
+               bool flagged) {
+  const unsigned long long calls = mesh_calls();
+  const RestRecord& p = t_rest;
+  const bool follows = p.valid && flagged && !a.first_step && p.tt + 1 == tt &&
+                       p.calls + 1 == calls && p.form == form && p.nx == a.nx &&
+                       p.ny == a.ny && p.pad == a.pad && p.arrays == arrays;
+  if (!follows) a.rest = nullptr;
+  RestRecord r;
+  r.arrays = arrays;
+  r.nx = a.nx;
+  r.ny = a.ny;
+  r.pad = a.pad;
+  r.form = form;
+  r.tt = tt;
+  r.calls = calls;
+  r.valid = flagged;
+  t_rest = r;
+}
 }  // namespace
 
 int set_lagrangian_rows(int rows) {
@@ -631,10 +685,15 @@ int fused_solve(Mesh* mesh, int tt, double* P, double* rho, double* rho_old,
       lagp = &lag;
     }
   }
+  take_rest(a, tt, 0,
+            {P, rho, e, rho_u, rho_v, uF_y, vF_x, uF_x, vF_y, F_x, F_y, reduce_array},
+            a.skipf != nullptr && lagp == nullptr);
   StepProfiler prof;
   prof.begin(s);
   launch_step(s, a, tt, first, second, prof, lagp);
-  return finish_step(s, mesh, reduce_array, prof, "solve_hydro_2d (fused)");
+  const int st = finish_step(s, mesh, reduce_array, prof, "solve_hydro_2d (fused)");
+  if (st != GB300_OK) t_rest.valid = false;
+  return st;
 }
 
 size_t mixed_workspace_bytes(int nx, int ny) { return mixed_layout(nx, ny).total; }
@@ -696,10 +755,15 @@ int mixed_solve(Mesh* mesh, int tt, double* rho, double* e, float* rho_u,
                                F(L.s_r32), F(L.s_e32)};
   const SweepArgs<float> second{D(L.s_r), D(L.s_e), F(L.s_r32), F(L.s_e32),
                                 rho, e, a.rho_r, a.e_r};
+  take_rest(a, tt, 1, {rho, e, rho_u, rho_v, work, reduce_array, nullptr, nullptr, nullptr,
+                       nullptr, nullptr, nullptr},
+            a.skipf != nullptr);
   StepProfiler prof;
   prof.begin(s);
   launch_step(s, a, tt, first, second, prof);
-  return finish_step(s, mesh, reduce_array, prof, "gb300_mixed_solve");
+  const int st = finish_step(s, mesh, reduce_array, prof, "gb300_mixed_solve");
+  if (st != GB300_OK) t_rest.valid = false;
+  return st;
 }
 
 }  // namespace flow

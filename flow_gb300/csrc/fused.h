@@ -16,6 +16,12 @@ int verbose();
 
 // SMs of the current device (cached per device).
 int num_sms();
+// Calls that may have written the state arrays between two fused steps: every
+// entry point taking a mesh (check_mesh) and the other writers count one
+// (note_state_write).  A fused step reuses the previous step's tile marks only
+// when exactly one such call -- its own -- came between them.
+unsigned long long mesh_calls();
+void note_state_write();
 // Kernel launches issued by this library (the fused step's kernels and the
 // conservation totals), for gb300_launch_count.
 void count_launches(unsigned n);

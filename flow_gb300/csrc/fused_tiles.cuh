@@ -112,6 +112,19 @@ struct StepArgs {
   // byte per sweep tile, ceil((ny - 2 pad) / rows) bands of
   // max(ceil((nx + 1 - 2 pad) / 127), qm_stride) tiles.
   unsigned char* skipf;
+  // The skip marks the previous step's first sweep left (its own half of the
+  // two mark buffers), or null when this step does not directly follow a
+  // flagged step on the same arrays.  Mark x of band b covers the interior
+  // cells of rows pad + b rest_rows .. + rest_rows - 1 and columns
+  // pad + x rest_w .. + rest_w - 1 (127 for an x sweep, 128 for a y sweep).
+  // A marked cell, its energy, its density and the momenta of the faces
+  // between two marked cells did not change in that step after its pressure
+  // phase, which stored +0 velocities there and no momentum change.
+  const unsigned char* rest;
+  int rest_w, rest_tiles_x, rest_rows;
+  // Each shock-heating tile's CFL minimum of the last step it ran (FP64 bit
+  // pattern, word by * qm_stride + bx), set with the flags, or null.
+  unsigned long long* cfl_tile;
 };
 
 // Writes the value of interior point (ii, jj) of a w x h array into each of
@@ -253,6 +266,27 @@ __device__ __forceinline__ bool tile_vel_still(const A& a, int r0, int r1, int c
     any |= a.vflag[(size_t)r * a.vf_stride + g] != 0;
   }
   return __syncthreads_or(any) == 0;
+}
+
+// Whether every cell of rows r0 .. r1 - 1 and columns c0 .. c1 - 1 (interior
+// cells only) was at rest through the previous step by its first sweep's skip
+// marks (StepArgs::rest).  Block-uniform (barrier); called by every thread of
+// the block.  False without marks.
+template <typename A>
+__device__ __forceinline__ bool rest_cells(const A& a, int r0, int r1, int c0, int c1) {
+  if (!a.rest) return false;  // uniform
+  const int pad = a.pad;
+  if (r0 < pad || c0 < pad || r1 > a.ny - pad || c1 > a.nx - pad || r0 >= r1 || c0 >= c1) {
+    return false;
+  }
+  const int b0 = (r0 - pad) / a.rest_rows, b1 = (r1 - 1 - pad) / a.rest_rows;
+  const int x0 = (c0 - pad) / a.rest_w, x1 = (c1 - 1 - pad) / a.rest_w;
+  const int nxb = x1 - x0 + 1, total = (b1 - b0 + 1) * nxb;
+  bool ok = true;
+  for (int q = threadIdx.x; q < total; q += blockDim.x) {
+    ok = ok && a.rest[(size_t)(b0 + q / nxb) * a.rest_tiles_x + x0 + q % nxb] != 0;
+  }
+  return __syncthreads_and(ok) != 0;
 }
 
 // x is +0 (all bits zero).
@@ -507,6 +541,7 @@ __device__ __forceinline__ void tile_lag_pressure_impl(const StepArgs<R>& a, int
       const R Pl = sP[t], rl = sR[t];
       R mom = mu_l;
       R rbar;
+      bool dmom = false;  // the momentum changes (kFl: flagged as moving)
       // FP64 form, power-of-two tile: a warp whose faces all have equal
       // pressures, densities and weights either side keeps its momenta
       // (dp = +0) and has the face density 2 (rc wx0) exactly, without FP64
@@ -520,17 +555,19 @@ __device__ __forceinline__ void tile_lag_pressure_impl(const StepArgs<R>& a, int
           mom = Pr::template dsub<kP2>(mom, dt * dp, exr, iex);
           a.rho_u[f] = mom;
         }
+        dmom = !Pr::is_zero(dp);
         rbar = face_average<R, kP2>(rc, wx0, rl, wx1);
       }
       const R vel = face_velocity(mom, rbar);
       a.u[f] = vel;
       mirror(edge, a.u, nx + 1, ny, pad, ii, jj, vel, true, false);
-      vnz = !is_plus_zero(vel);
+      vnz = dmom || !is_plus_zero(vel);
     }
     if (ii >= pad && ii < ny + 1 - pad && jj >= pad && jj < nx - pad) {
       const size_t c = cidx(nx, ii, jj);
       R mom = mv_l;
       R rbar;
+      bool dmom = false;
       if (kP2 && !Pr::kMixed &&
           warp_all(lane_same(Pc, P_dn) && lane_same(rc, r_dn) && lane_same(s_wy0[k], s_wy1[k]))) {
         rbar = Pr::twice(Pr::template mulp<true>(rc, s_wy0[k]));
@@ -540,12 +577,13 @@ __device__ __forceinline__ void tile_lag_pressure_impl(const StepArgs<R>& a, int
           mom = Pr::template dsub<kP2>(mom, dt * dp, s_ey[k], s_iey[k]);
           a.rho_v[c] = mom;
         }
+        dmom = !Pr::is_zero(dp);
         rbar = face_average<R, kP2>(rc, s_wy0[k], r_dn, s_wy1[k]);
       }
       const R vel = face_velocity(mom, rbar);
       a.v[c] = vel;
       mirror(edge, a.v, nx, ny + 1, pad, ii, jj, vel, false, true);
-      vnz = vnz || !is_plus_zero(vel);
+      vnz = vnz || dmom || !is_plus_zero(vel);
     }
     if constexpr (kFl) {
       store_flag(a.vflag + (size_t)ii * a.vf_stride + (jj >> 5),
@@ -559,6 +597,18 @@ __device__ __forceinline__ void tile_lag_pressure_impl(const StepArgs<R>& a, int
 
 template <typename R, bool kFl = false>
 __device__ __forceinline__ void tile_lag_pressure(const StepArgs<R>& a, int bx, int by) {
+  if constexpr (kFl) {
+    // A tile whose cells (and the row above and column left it reads) were
+    // at rest through the previous step: its pressures, momenta, velocities
+    // and velocity flags are what that step's pressure phase stored, from
+    // the same densities, energies and momenta, and nothing has written them
+    // since -- this phase would store the same numbers.
+    const int c0 = bx * kCols, i0 = by * a.rows;
+    if (a.rest && !tile_near_edge(a.nx, a.ny, a.pad, c0, i0, a.rows) &&
+        rest_cells(a, i0 - 1, i0 + a.rows, c0 - 1, c0 + kCols)) {
+      return;
+    }
+  }
   FLOW_POW2_DISPATCH(R, a, bx * kCols, by * a.rows,
                      (tile_lag_pressure_impl<R, true, kFl>(a, bx, by)),
                      (tile_lag_pressure_impl<R, false, kFl>(a, bx, by)));
@@ -1115,11 +1165,31 @@ __device__ __forceinline__ void tile_lag_energy_dt_impl(const StepArgs<R>& a, in
     unsigned long long b = s_warp[0];
     for (int w = 1; w < kCols / 32; ++w) b = (s_warp[w] < b) ? s_warp[w] : b;
     atomicMin(a.min_slot, b);
+    // (Flags run only in the one-problem kernel, whose tile is its block:
+    // the slot is formed from the block index rather than keeping bx, by.)
+    if (kFlags && a.cfl_tile) a.cfl_tile[(size_t)blockIdx.y * a.qm_stride + blockIdx.x] = b;
   }
 }
 
 template <typename R, bool kRing = true, bool kFlags = false>
 __device__ __forceinline__ void tile_lag_energy_dt(const StepArgs<R>& a, int bx, int by) {
+  if constexpr (kFlags) {
+    // A tile at rest now (velocity flags) whose cells were at rest through
+    // the previous step: it keeps every energy, has no viscous stress, and
+    // its cells' CFL candidates are those of the previous step, from the
+    // same densities and energies -- its minimum then stands.
+    if (a.rest && a.cfl_tile) {
+      const int nx = a.nx, ny = a.ny, pad = a.pad;
+      const int cb = pad + bx * kCols, i0 = pad + by * a.rows;
+      const int i1 = min(i0 + a.rows, ny - pad);
+      if (!tile_near_edge(nx, ny, pad, cb, i0, a.rows) &&
+          tile_vel_still(a, i0 - 2, i1 + 2, cb - 2, cb + kCols + 2) &&
+          rest_cells(a, i0, i1, cb, min(cb + kCols, nx - pad))) {
+        if (threadIdx.x == 0) atomicMin(a.min_slot, a.cfl_tile[(size_t)by * a.qm_stride + bx]);
+        return;
+      }
+    }
+  }
   FLOW_POW2_DISPATCH(R, a, a.pad + bx * kCols, a.pad + by * a.rows,
                      (tile_lag_energy_dt_impl<R, true, kRing, kFlags>(a, bx, by)),
                      (tile_lag_energy_dt_impl<R, false, kRing, kFlags>(a, bx, by)));
@@ -1641,8 +1711,12 @@ __device__ __forceinline__ void tile_mass_sweep_x(const StepArgs<R>& a, const Sw
     };
     if constexpr (kFirst) {
       // At rest in both directions, and every cell's round trip exact.
+      // (Cells at rest through the previous step took the round trip
+      // exactly then, on the same values.)
       bool sk = tile_vel_still(a, i0 - 2, i1 + 2, cb - 2, cb + kCols + 1);
-      if (sk) sk = block_round_trip_exact(s.r_in, s.e_in, a.nx, i0, i1, jj, cell_ok);
+      if (sk && !rest_cells(a, i0, i1, cb, min(cb + kCols - 1, a.nx - pad))) {
+        sk = block_round_trip_exact(s.r_in, s.e_in, a.nx, i0, i1, jj, cell_ok);
+      }
       if (t == 0) store_flag(s.skip + (size_t)by * s.skip_tiles_x + bx, sk);
       if (sk) {
         zero_flags();
@@ -1977,7 +2051,9 @@ __device__ __forceinline__ void tile_mass_sweep_y(const StepArgs<R>& a, const Sw
     if constexpr (kFirst) {
       // At rest in both directions, and every cell's round trip exact.
       bool sk = tile_vel_still(a, i0 - 2, i1 + 2, cb - 2, cb + kCols + 2);
-      if (sk) sk = block_round_trip_exact(s.r_in, s.e_in, a.nx, i0, i1, jj, col_ok);
+      if (sk && !rest_cells(a, i0, i1, cb, min(cb + kCols, a.nx - pad))) {
+        sk = block_round_trip_exact(s.r_in, s.e_in, a.nx, i0, i1, jj, col_ok);
+      }
       if (threadIdx.x == 0) store_flag(s.skip + (size_t)by * s.skip_tiles_x + bx, sk);
       if (sk) {
         zero_flags();

@@ -83,6 +83,7 @@ int launch_uniform_edges(cudaStream_t s, double* edges, int count, int pad, doub
 
 extern "C" int gb300_fill_boxes(int nx, int ny, const double* edgex, const double* edgey,
                                 const double* boxes, int nboxes, double* rho, double* e) {
+  flow::note_state_write();
   return flow::launch_fill_boxes(flow::current_stream(), nx, ny, edgex, edgey, boxes, nboxes,
                                  rho, e);
 }

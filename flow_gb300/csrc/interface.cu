@@ -97,7 +97,15 @@ bool decomposed(const Mesh* m) {
 
 // A rank of a decomposed mesh runs the exact mode's stage kernels with its
 // ghost layers exchanged through the registered hooks.
+namespace {
+std::atomic<unsigned long long> g_mesh_calls{0};
+}  // namespace
+
+unsigned long long mesh_calls() { return g_mesh_calls.load(std::memory_order_relaxed); }
+void note_state_write() { g_mesh_calls.fetch_add(1, std::memory_order_relaxed); }
+
 int check_mesh(const Mesh* m, int nx, int ny, const char* where) {
+  note_state_write();
   if (!m) return record_error(GB300_ERR_ARG, "%s: mesh is NULL", where);
   if (decomposed(m) && (!g_halo_fn || !g_rmin_fn)) {
     return record_error(GB300_ERR_ARG,
@@ -495,6 +503,7 @@ void equation_of_state(const int nx, const int ny, double* P, const double* rho,
     record_error(GB300_ERR_ARG, "equation_of_state: empty mesh");
     return;
   }
+  note_state_write();
   launch_eos(current_stream(), nx, ny, P, rho, e);
   check_launch("equation_of_state");
 }
@@ -653,6 +662,10 @@ int gb300_set_mode(int mode) {
   return GB300_OK;
 }
 int gb300_get_mode(void) { return t_mode; }
+int gb300_state_changed(void) {
+  note_state_write();
+  return GB300_OK;
+}
 int gb300_set_lagrangian_rows(int rows) { return set_lagrangian_rows(rows); }
 int gb300_set_halo_exchange(gb300_halo_fn fn, void* ctx) {
   g_halo_fn = fn;

@@ -203,6 +203,15 @@ int gb300_set_verbose(int verbose);
 
 int gb300_synchronize(void);
 
+/* The fused step (both forms) carries from one timestep to the next which
+ * tiles of the mesh were at rest, and does not recompute them while they stay
+ * so.  It trusts that record only for the step that directly follows (tt one
+ * more, the same arrays and reduce_array, no other call of this library that
+ * takes a mesh in between).  A caller that writes the state arrays by other
+ * means (its own copies or kernels) between two such steps calls this first.
+ * No reference counterpart (the reference recomputes every cell). */
+int gb300_state_changed(void);
+
 /* Status-returning forms of the Part 1 calls. */
 int gb300_solve_hydro_2d(Mesh* mesh, int tt, double* P, double* rho,
                          double* rho_old, double* e, double* u, double* v,

@@ -35,6 +35,15 @@ def problems_with_flags():
              (1.0, 1e3, 124 / 300, 13 / 90, 8 / 300, 7 / 90)]).with_cfl_dt(),
         "sod_257x33": problems.sod(257, 33),
         "smooth_96": problems.smooth_random(96, np.random.default_rng(11)),
+        # Tiles away from every wall, most of them at rest from one step to
+        # the next while the blast grows into them (the previous step's
+        # marks: pressures, velocities, CFL minima and round trips reused).
+        "wide_blast": P(700, 300).boxes(
+            [(1.0, 1e-5, 0.0, 0.0, 1.0, 1.0),
+             (1.0, 1e3, 300 / 700, 140 / 300, 10 / 700, 10 / 300)]).with_cfl_dt(),
+        # A pressure jump at rest: the first step changes momenta where the
+        # velocities it stores may still be +0.
+        "sod_700x64": problems.sod(700, 64),
     }
 
 
@@ -47,7 +56,7 @@ def flags_active(p):
 
 @pytest.mark.parametrize("precision", [0, 1])
 @pytest.mark.parametrize("name", ["corner_blast", "tile_boundary_blast", "sod_257x33",
-                                  "smooth_96"])
+                                  "smooth_96", "wide_blast", "sod_700x64"])
 def test_flagged_step_equals_unflagged_batch(fg, name, precision):
     p = problems_with_flags()[name]
     assert flags_active(p)
@@ -64,3 +73,34 @@ def test_flagged_step_equals_unflagged_batch(fg, name, precision):
                                                           int(np.count_nonzero(rho != sim.interior("rho"))))
         assert np.array_equal(e, sim.interior("e")), (tt, "e")
         assert dt[0] == sim.mesh.dt and dt[1] == sim.mesh.dt_h, tt
+
+
+STATE = ("rho", "e", "rho_u", "rho_v", "u", "v")
+
+
+def test_state_written_between_steps(fg):
+    """A caller that writes the state between two steps announces it
+    (gb300_state_changed): the next step then recomputes every tile, and the
+    run equals a fresh one started from the written state."""
+    import torch
+    p = problems_with_flags()["wide_blast"]
+    a = fg.DeviceSim(p)
+    a.initial_timestep()
+    for _ in range(6):
+        a.step()
+    # A second blast, written by the caller into cells at rest.
+    e2 = a.a["e"][: a.nx * a.ny].view(a.ny, a.nx)
+    e2[150:160, 100:110] = 1e3
+    assert fg.lib().gb300_state_changed() == 0
+    b = fg.DeviceSim(p)
+    for f in STATE:
+        b.a[f].copy_(a.a[f])
+    b.mesh.dt, b.mesh.dt_h, b.tt = a.mesh.dt, a.mesh.dt_h, a.tt
+    torch.cuda.synchronize()
+    for _ in range(8):
+        a.step()
+    for _ in range(8):
+        b.step()
+    for f in STATE:
+        assert torch.equal(a.a[f], b.a[f]), f
+    assert a.mesh.dt == b.mesh.dt and a.mesh.dt_h == b.mesh.dt_h
