@@ -89,10 +89,15 @@ __global__ void __launch_bounds__(kCols) k_lag_viscous_accel(const StepArgs<R> a
 template <typename R, bool kFlags>
 __global__ void __launch_bounds__(kCols) k_lag_energy_dt(const StepArgs<R> a) {
   __shared__ bool s_last;
+  __shared__ unsigned long long s_tile_min;  // the tile's CFL minimum (kFlags)
   pdl_wait();
   pdl_trigger();
-  tile_lag_energy_dt<R, true, kFlags>(a, blockIdx.x, blockIdx.y);
+  tile_lag_energy_dt<R, true, kFlags>(a, blockIdx.x, blockIdx.y, kFlags ? &s_tile_min : nullptr);
   if (threadIdx.x == 0) {
+    // (Thread 0 wrote the minimum it stores here.)
+    if (kFlags && a.cfl_tile) {
+      a.cfl_tile[(size_t)blockIdx.y * a.qm_stride + blockIdx.x] = s_tile_min;
+    }
     __threadfence();
     unsigned long long* ticket = reinterpret_cast<unsigned long long*>(a.ra + kRaTicket);
     s_last = (atomicAdd(ticket, 1ull) == (unsigned long long)gridDim.x * gridDim.y - 1);

@@ -928,7 +928,8 @@ __device__ __forceinline__ unsigned long long warp_min_u64(unsigned long long x)
 // finish applies the leapfrog dt/dt_h rule (finish_dt).  In the mixed form
 // the FP32 energy change is added to the FP64 energy.
 template <typename R, bool kP2, bool kRing, bool kFlags>
-__device__ __forceinline__ void tile_lag_energy_dt_impl(const StepArgs<R>& a, int bx, int by) {
+__device__ __forceinline__ void tile_lag_energy_dt_impl(const StepArgs<R>& a, int bx, int by,
+                                                        unsigned long long* tile_min) {
   using Pr = Prec<R>;
   __shared__ R s_icy[kMaxRows], s_cy[kMaxRows];
   __shared__ double s_icy2[kMaxRows];
@@ -1165,14 +1166,14 @@ __device__ __forceinline__ void tile_lag_energy_dt_impl(const StepArgs<R>& a, in
     unsigned long long b = s_warp[0];
     for (int w = 1; w < kCols / 32; ++w) b = (s_warp[w] < b) ? s_warp[w] : b;
     atomicMin(a.min_slot, b);
-    // (Flags run only in the one-problem kernel, whose tile is its block:
-    // the slot is formed from the block index rather than keeping bx, by.)
-    if (kFlags && a.cfl_tile) a.cfl_tile[(size_t)blockIdx.y * a.qm_stride + blockIdx.x] = b;
+    if (tile_min) *tile_min = b;
   }
 }
 
+// tile_min: where thread 0 also stores the tile's CFL minimum, or null.
 template <typename R, bool kRing = true, bool kFlags = false>
-__device__ __forceinline__ void tile_lag_energy_dt(const StepArgs<R>& a, int bx, int by) {
+__device__ __forceinline__ void tile_lag_energy_dt(const StepArgs<R>& a, int bx, int by,
+                                                   unsigned long long* tile_min = nullptr) {
   if constexpr (kFlags) {
     // A tile at rest now (velocity flags) whose cells were at rest through
     // the previous step: it keeps every energy, has no viscous stress, and
@@ -1185,14 +1186,18 @@ __device__ __forceinline__ void tile_lag_energy_dt(const StepArgs<R>& a, int bx,
       if (!tile_near_edge(nx, ny, pad, cb, i0, a.rows) &&
           tile_vel_still(a, i0 - 2, i1 + 2, cb - 2, cb + kCols + 2) &&
           rest_cells(a, i0, i1, cb, min(cb + kCols, nx - pad))) {
-        if (threadIdx.x == 0) atomicMin(a.min_slot, a.cfl_tile[(size_t)by * a.qm_stride + bx]);
+        if (threadIdx.x == 0) {
+          const unsigned long long b = a.cfl_tile[(size_t)by * a.qm_stride + bx];
+          atomicMin(a.min_slot, b);
+          if (tile_min) *tile_min = b;
+        }
         return;
       }
     }
   }
   FLOW_POW2_DISPATCH(R, a, a.pad + bx * kCols, a.pad + by * a.rows,
-                     (tile_lag_energy_dt_impl<R, true, kRing, kFlags>(a, bx, by)),
-                     (tile_lag_energy_dt_impl<R, false, kRing, kFlags>(a, bx, by)));
+                     (tile_lag_energy_dt_impl<R, true, kRing, kFlags>(a, bx, by, tile_min)),
+                     (tile_lag_energy_dt_impl<R, false, kRing, kFlags>(a, bx, by, tile_min)));
 }
 
 // The leapfrog dt/dt_h rule of omp3/flow.c:103-105 applied to the finished
@@ -2303,6 +2308,9 @@ __device__ __forceinline__ void tile_mom_x_impl(const StepArgs<R>& a, int bx, in
     if (tile_mass_still(a, i0 - 1, i1, c0 - 1, c0 + kCols)) {
       const bool upd = kV ? (t < kCols - 1 && j < nx - pad) : (t >= 1 && j < nx + 1 - pad);
       const bool zero = tile_vel_still(a, i0 - 2, i1 + 2, c0 - 2, c0 + kCols + 2);
+      // Velocities all +0 whose cells were at rest through the previous
+      // step, when this pair stored (or kept) +0 for each of them: they stand.
+      if (zero && !edge && rest_cells(a, i0 - 1, i1, c0 - 1, c0 + kCols)) return;
       copy_velocities<R, !kV>(a, edge, kV ? a.v : a.u, kV ? a.v_out : a.u_out, i0, i1, j, upd,
                               zero);
       return;
@@ -2547,6 +2555,7 @@ __device__ __forceinline__ void tile_mom_y_impl(const StepArgs<R>& a, int bx, in
     const int cb = pad + bx * kCols;
     if (tile_mass_still(a, i0 - 1, i1, cb - 1, cb + kCols)) {
       const bool zero = tile_vel_still(a, i0 - 2, i1 + 2, cb - 2, cb + kCols + 2);
+      if (zero && !edge && rest_cells(a, i0 - 1, i1, cb - 1, cb + kCols)) return;
       copy_velocities<R, !kV>(a, edge, kV ? a.v : a.u, kV ? a.v_out : a.u_out, i0, i1, jj,
                               jj < (kV ? nx - pad : nx + 1 - pad), zero);
       return;
