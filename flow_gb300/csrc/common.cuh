@@ -32,7 +32,9 @@ constexpr double kCT = 0.3;
 //                             double: bit order = value order)
 //   [7] mesh power-of-two     1 when every mesh spacing is a power of two
 //                             (formed on the device at the start of a step)
-//   [8 ...]                   per-block partials (2 doubles per block, at
+//   [8] moving tiles          the fused step's count of first-sweep tiles
+//                             it did not skip (uint64), read with dt
+//   [9 ...]                   per-block partials (2 doubles per block, at
 //                             most kMaxReduceBlocks blocks)
 //   [kRaQFlags ...]           the fused step's tile flags, when the array
 //                             is large enough to hold them: per-tile CFL
@@ -48,7 +50,8 @@ enum : int {
   kRaStatus = 5,
   kRaMinBits = 6,
   kRaMeshPow2 = 7,
-  kRaPartial = 8,
+  kRaMoving = 8,
+  kRaPartial = 9,
 };
 constexpr int kMaxReduceBlocks = 1024;
 constexpr int kRaQFlags = kRaPartial + 2 * kMaxReduceBlocks;

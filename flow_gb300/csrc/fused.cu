@@ -31,7 +31,7 @@ __device__ __forceinline__ void pdl_trigger() {
 // step.  The tiles then skip their own spacing tests (block_mesh_pow2).
 constexpr int kPow2Threads = 1024;
 // It also clears the CFL minimum slot and the block ticket for the step's
-// Lagrangian kernels.
+// Lagrangian kernels, and the count of moving first-sweep tiles.
 __global__ void __launch_bounds__(kPow2Threads)
     k_mesh_pow2(int nx, int ny, const double* celldx, const double* edgedx,
                 const double* celldy, const double* edgedy, unsigned long long* flag,
@@ -41,6 +41,7 @@ __global__ void __launch_bounds__(kPow2Threads)
   if (threadIdx.x == 0) {
     *reinterpret_cast<unsigned long long*>(ra + kRaTicket) = 0ull;
     *reinterpret_cast<unsigned long long*>(ra + kRaMinBits) = ~0ull;
+    *reinterpret_cast<unsigned long long*>(ra + kRaMoving) = 0ull;
   }
   // Every test is made (no short circuit), so that a thread's loads are
   // independent and in flight together.
@@ -294,6 +295,12 @@ inline dim3 strip_grid(int cols, int rows, int tile_rows, int cols_per_cta = kCo
 // where the flow moves, and shorter tiles there shorten the longest tile's
 // chain of rows, which bounds such a kernel.
 constexpr int kRowsMomVel = 16, kRowsMomFlux = 8, kRowsAccel = 8;
+// Tile heights of the pressure, viscosity and shock-heating kernels, and of
+// the two mass sweeps (whose bands are also the skip marks' bands): a step
+// whose previous step's first sweep skipped at least half of its tiles takes
+// the shorter sweep tiles (the moving tiles' chains of rows bound a sweep
+// there), others the taller ones (less halo work on a field in motion).
+constexpr int kRowsLag = 16, kRowsSweepStill = 8, kRowsSweepMoving = 16;
 template <typename R>
 StepArgs<R> with_rows(const StepArgs<R>& a, int rows) {
   StepArgs<R> b = a;
@@ -358,7 +365,7 @@ inline int apply_blocks(const lagf::LagArgs& l) {
 template <typename R>
 void launch_step(cudaStream_t s, const StepArgs<R>& a, int tt,
                  const SweepArgs<R>& first, const SweepArgs<R>& second,
-                 StepProfiler& prof, const lagf::LagArgs* lag = nullptr) {
+                 StepProfiler& prof, int sweep_rows, const lagf::LagArgs* lag = nullptr) {
   const int nx = a.nx, ny = a.ny, pad = a.pad;
   // The whole-mesh spacing test the tiles read (the mesh may change between
   // calls, so it is formed every step; one block, a few microseconds).
@@ -395,6 +402,7 @@ void launch_step(cudaStream_t s, const StepArgs<R>& a, int tt,
   // Lagrangian kernels wrote them (not the one-kernel phase).
   StepArgs<R> ad = a;
   if (lag) ad.vflag = nullptr;
+  const StepArgs<R> as = with_rows(ad, sweep_rows);
   const bool x_first = (tt % 2 == 0);
   // With flags, the first sweep marks the tiles it skips (in its own grid);
   // the second reads their cells from the first sweep's input.
@@ -402,16 +410,16 @@ void launch_step(cudaStream_t s, const StepArgs<R>& a, int tt,
   if (a.skipf) {
     sw1.skip = sw2.skip = a.skipf;
     sw1.skip_tiles_x = sw2.skip_tiles_x = x_first ? a.fx_stride / 4 : a.qm_stride;
-    sw1.skip_bands = sw2.skip_bands = (ny - 2 * pad + a.rows - 1) / a.rows;
+    sw1.skip_bands = sw2.skip_bands = (ny - 2 * pad + sweep_rows - 1) / sweep_rows;
     sw2.r_alt = first.r_in;
     sw2.e_alt = first.e_in;
     sw2.r_alt_r = first.r_in_r;
     sw2.e_alt_r = first.e_in_r;
   }
   prof.mark(x_first ? "mass_sweep_x" : "mass_sweep_y");
-  launch_mass(s, ad, !x_first, true, sw1);
+  launch_mass(s, as, !x_first, true, sw1);
   prof.mark(x_first ? "mass_sweep_y" : "mass_sweep_x");
-  launch_mass(s, ad, x_first, false, sw2);
+  launch_mass(s, as, x_first, false, sw2);
 
   // Momentum: each flux fused with its update, in the reference order; the
   // pair that recomputes a velocity comes first in each chain.
@@ -437,13 +445,14 @@ void launch_step(cudaStream_t s, const StepArgs<R>& a, int tt,
 }
 
 int finish_step(cudaStream_t s, Mesh* mesh, double* ra, StepProfiler& prof,
-                const char* where) {
+                const char* where, unsigned long long* moving = nullptr) {
   {
     const int st = check_launch(where);
     if (st != GB300_OK) return st;
   }
-  // dt, dt_h (slots 0, 1) and the status word (slot 5) in one copy.
-  double head[kRaStatus + 1];
+  // dt, dt_h (slots 0, 1), the status word (slot 5) and the moving-tile
+  // count (slot 8) in one copy.
+  double head[kRaMoving + 1];
   cudaMemcpyAsync(head, ra + kRaDt, sizeof(head), cudaMemcpyDeviceToHost, s);
   const cudaError_t err = cudaStreamSynchronize(s);
   if (err != cudaSuccess) {
@@ -457,6 +466,7 @@ int finish_step(cudaStream_t s, Mesh* mesh, double* ra, StepProfiler& prof,
     return record_error(GB300_ERR_TIMEOUT,
                         "%s: a row copy of the Lagrangian kernel did not arrive", where);
   }
+  if (moving) memcpy(moving, &head[kRaMoving], sizeof(*moving));
   const double pair[2] = {head[kRaDt], head[kRaDtH]};
   mesh->dt = pair[0];
   mesh->dt_h = pair[1];
@@ -480,7 +490,7 @@ void fill_mesh_args(StepArgs<R>& a, const Mesh* mesh, int tt, double* ra) {
   a.dt_h = mesh->dt_h;
   a.max_dt = mesh->max_dt;
   a.first_step = (tt == 0);
-  a.rows = kDefaultRows;
+  a.rows = kRowsLag;
   // The viscous-stress and mass-flux flags live in reduce_array after the
   // reduction partials when it holds them (it has nx*ny doubles, as the arch
   // layer allocates it); a mesh too small for them stores and reads every
@@ -498,6 +508,7 @@ void fill_mesh_args(StepArgs<R>& a, const Mesh* mesh, int tt, double* ra) {
   a.rest = nullptr;
   a.rest_w = a.rest_tiles_x = a.rest_rows = 0;
   a.cfl_tile = nullptr;
+  a.moving = nullptr;
   const int stride = (a.nx - 2 * a.pad + kCols - 1) / kCols;
   const int xtiles = (a.nx + 1 - 2 * a.pad + kCols - 2) / (kCols - 1);
   const long long rows = a.ny - 2 * a.pad;
@@ -505,8 +516,9 @@ void fill_mesh_args(StepArgs<R>& a, const Mesh* mesh, int tt, double* ra) {
   const size_t fx_words = (size_t)rows * xtiles;
   const int vtiles = (a.nx + kCols - 1) / kCols;
   const size_t v_words = (size_t)a.ny * vtiles;
-  const long long bands = (rows + a.rows - 1) / a.rows;
-  const size_t sk_words = ((size_t)bands * (xtiles > stride ? xtiles : stride) + 3) / 4;
+  const long long bands = (rows + a.rows - 1) / a.rows;  // shock-heating tiles
+  const long long sweep_bands = (rows + kRowsSweepStill - 1) / kRowsSweepStill;  // at most
+  const size_t sk_words = ((size_t)sweep_bands * (xtiles > stride ? xtiles : stride) + 3) / 4;
   // Per-tile CFL minima (8 bytes per shock-heating tile) first, then the
   // 4-byte words: stresses, y fluxes, x fluxes, velocities, and the skip
   // marks of even and odd steps (a step's first sweep writes its own half;
@@ -533,7 +545,8 @@ void fill_mesh_args(StepArgs<R>& a, const Mesh* mesh, int tt, double* ra) {
     const bool prev_x_first = ((tt - 1) % 2 == 0);
     a.rest_w = prev_x_first ? kCols - 1 : kCols;
     a.rest_tiles_x = prev_x_first ? xtiles : stride;
-    a.rest_rows = a.rows;
+    a.rest_rows = kRowsSweepMoving;  // (take_rest sets the previous step's)
+    a.moving = reinterpret_cast<unsigned long long*>(ra + kRaMoving);
   }
 }
 
@@ -597,6 +610,9 @@ int g_lag_rows = lagf::kDefaultRows;
 struct RestRecord {
   std::array<const void*, 12> arrays{};
   int nx = 0, ny = 0, pad = 0, form = -1, tt = 0;
+  int sweep_rows = 0;                    // the step's sweep tile height
+  unsigned long long tiles = 0;          // its first sweep's tiles
+  unsigned long long moving = ~0ull;     // of which not skipped (read after the step)
   unsigned long long calls = 0;
   bool valid = false;
 };
@@ -604,16 +620,24 @@ thread_local RestRecord t_rest;
 
 // Keeps a.rest only when this step directly follows the recorded one on the
 // same arrays (and no other mesh call came between), then records this step
-// as the one the next may follow (when it runs with flags).
+// as the one the next may follow (when it runs with flags).  Returns this
+// step's sweep tile height: the shorter where the previous step's first sweep
+// skipped at least half of its tiles.
 template <typename R>
-void take_rest(StepArgs<R>& a, int tt, int form, const std::array<const void*, 12>& arrays,
-               bool flagged) {
+int take_rest(StepArgs<R>& a, int tt, int form, const std::array<const void*, 12>& arrays,
+              bool flagged) {
   const unsigned long long calls = mesh_calls();
   const RestRecord& p = t_rest;
   const bool follows = p.valid && flagged && !a.first_step && p.tt + 1 == tt &&
                        p.calls + 1 == calls && p.form == form && p.nx == a.nx &&
                        p.ny == a.ny && p.pad == a.pad && p.arrays == arrays;
-  if (!follows) a.rest = nullptr;
+  if (follows) {
+    a.rest_rows = p.sweep_rows;
+  } else {
+    a.rest = nullptr;
+  }
+  const bool still = follows && p.moving != ~0ull && 2 * p.moving <= p.tiles;
+  const int rows = still ? kRowsSweepStill : kRowsSweepMoving;
   RestRecord r;
   r.arrays = arrays;
   r.nx = a.nx;
@@ -621,9 +645,15 @@ void take_rest(StepArgs<R>& a, int tt, int form, const std::array<const void*, 1
   r.pad = a.pad;
   r.form = form;
   r.tt = tt;
+  r.sweep_rows = rows;
+  const bool x_first = (tt % 2 == 0);
+  const unsigned long long tiles_x =
+      x_first ? (unsigned long long)(a.fx_stride / 4) : (unsigned long long)a.qm_stride;
+  r.tiles = tiles_x * (unsigned long long)((a.ny - 2 * a.pad + rows - 1) / rows);
   r.calls = calls;
   r.valid = flagged;
   t_rest = r;
+  return rows;
 }
 }  // namespace
 
@@ -690,14 +720,16 @@ int fused_solve(Mesh* mesh, int tt, double* P, double* rho, double* rho_old,
       lagp = &lag;
     }
   }
-  take_rest(a, tt, 0,
-            {P, rho, e, rho_u, rho_v, uF_y, vF_x, uF_x, vF_y, F_x, F_y, reduce_array},
-            a.skipf != nullptr && lagp == nullptr);
+  const int sweep_rows =
+      take_rest(a, tt, 0, {P, rho, e, rho_u, rho_v, uF_y, vF_x, uF_x, vF_y, F_x, F_y, reduce_array},
+                a.skipf != nullptr && lagp == nullptr);
   StepProfiler prof;
   prof.begin(s);
-  launch_step(s, a, tt, first, second, prof, lagp);
-  const int st = finish_step(s, mesh, reduce_array, prof, "solve_hydro_2d (fused)");
+  launch_step(s, a, tt, first, second, prof, sweep_rows, lagp);
+  unsigned long long moving = ~0ull;
+  const int st = finish_step(s, mesh, reduce_array, prof, "solve_hydro_2d (fused)", &moving);
   if (st != GB300_OK) t_rest.valid = false;
+  t_rest.moving = moving;
   return st;
 }
 
@@ -760,14 +792,17 @@ int mixed_solve(Mesh* mesh, int tt, double* rho, double* e, float* rho_u,
                                F(L.s_r32), F(L.s_e32)};
   const SweepArgs<float> second{D(L.s_r), D(L.s_e), F(L.s_r32), F(L.s_e32),
                                 rho, e, a.rho_r, a.e_r};
-  take_rest(a, tt, 1, {rho, e, rho_u, rho_v, work, reduce_array, nullptr, nullptr, nullptr,
-                       nullptr, nullptr, nullptr},
-            a.skipf != nullptr);
+  const int sweep_rows =
+      take_rest(a, tt, 1, {rho, e, rho_u, rho_v, work, reduce_array, nullptr, nullptr, nullptr,
+                           nullptr, nullptr, nullptr},
+                a.skipf != nullptr);
   StepProfiler prof;
   prof.begin(s);
-  launch_step(s, a, tt, first, second, prof);
-  const int st = finish_step(s, mesh, reduce_array, prof, "gb300_mixed_solve");
+  launch_step(s, a, tt, first, second, prof, sweep_rows);
+  unsigned long long moving = ~0ull;
+  const int st = finish_step(s, mesh, reduce_array, prof, "gb300_mixed_solve", &moving);
   if (st != GB300_OK) t_rest.valid = false;
+  t_rest.moving = moving;
   return st;
 }
 

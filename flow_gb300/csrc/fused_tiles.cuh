@@ -125,6 +125,8 @@ struct StepArgs {
   // Each shock-heating tile's CFL minimum of the last step it ran (FP64 bit
   // pattern, word by * qm_stride + bx), set with the flags, or null.
   unsigned long long* cfl_tile;
+  // Count of the first sweep's tiles not skipped this step (flags only).
+  unsigned long long* moving;
 };
 
 // Writes the value of interior point (ii, jj) of a w x h array into each of
@@ -1722,7 +1724,10 @@ __device__ __forceinline__ void tile_mass_sweep_x(const StepArgs<R>& a, const Sw
       if (sk && !rest_cells(a, i0, i1, cb, min(cb + kCols - 1, a.nx - pad))) {
         sk = block_round_trip_exact(s.r_in, s.e_in, a.nx, i0, i1, jj, cell_ok);
       }
-      if (t == 0) store_flag(s.skip + (size_t)by * s.skip_tiles_x + bx, sk);
+      if (t == 0) {
+        store_flag(s.skip + (size_t)by * s.skip_tiles_x + bx, sk);
+        if (!sk && a.moving) atomicAdd(a.moving, 1ull);
+      }
       if (sk) {
         zero_flags();
         return;
@@ -2059,7 +2064,10 @@ __device__ __forceinline__ void tile_mass_sweep_y(const StepArgs<R>& a, const Sw
       if (sk && !rest_cells(a, i0, i1, cb, min(cb + kCols, a.nx - pad))) {
         sk = block_round_trip_exact(s.r_in, s.e_in, a.nx, i0, i1, jj, col_ok);
       }
-      if (threadIdx.x == 0) store_flag(s.skip + (size_t)by * s.skip_tiles_x + bx, sk);
+      if (threadIdx.x == 0) {
+        store_flag(s.skip + (size_t)by * s.skip_tiles_x + bx, sk);
+        if (!sk && a.moving) atomicAdd(a.moving, 1ull);
+      }
       if (sk) {
         zero_flags();
         return;

@@ -48,10 +48,10 @@ def problems_with_flags():
 
 
 def flags_active(p):
-    # The flags fit in reduce_array (nx*ny doubles) after the 2056 header and
+    # The flags fit in reduce_array (nx*ny doubles) after the 2057 header and
     # partial slots: four word arrays of at most (ny + 1) x 4 ceil((nx + 1) / 127).
     words = 4 * (p.ny + 1) * 4 * ((p.nx + 1 + 126) // 127 + (p.nx + 127) // 128)
-    return 8 * p.nx * p.ny >= 8 * 2056 + 4 * words
+    return 8 * p.nx * p.ny >= 8 * 2057 + 4 * words
 
 
 @pytest.mark.parametrize("precision", [0, 1])
