@@ -49,31 +49,20 @@ CONFIG_STEPS = 500   # the blast workload's stated length
 B_ALG_FP64 = 64      # bytes/cell-step: rho, e, rho_u, rho_v read + written once
 B_ALG_MIXED = 48     # rho, e (FP64) and rho_u, rho_v (FP32), each read + written
 
-# Algorithmic bytes per interior cell of each fused kernel (the per-kernel HBM
-# roofline): the arrays it must read or write at every cell, 8 B each; what the
-# stress and mass-flux flags let it touch only where the flow moves (Q, the
-# mass fluxes, the changed energies and momenta) counts as nothing.
+# Bytes per interior cell each fused kernel moves on a tile at rest through
+# the step and the one before it (the blast's ambient mesh): the flags and
+# skip marks only, so 0 -- the pressure phase, the CFL minimum, the first
+# sweep's round-trip test and the velocity store take the previous step's
+# results there.  Where the flow moves a kernel moves its full arrays; its
+# bytes per cell on a whole workload are therefore measured (ncu, the
+# committed figures below) rather than fixed here.
 KERNEL_BYTES_PER_CELL = {
-    "lag_pressure": 8 * 7,       # rho, e, rho_u, rho_v in; P, u, v out
-    "lag_viscosity": 0,          # u, v, rho where a velocity is not +0; Q where a stress is not
-    "lag_viscous_accel": 0,      # stresses, momenta, velocities only where a stress gradient acts
-    "lag_energy_dt": 8 * 2,      # rho, e in for the CFL minimum (u, v, P, Q, e out where moving)
+    "lag_pressure": 0, "lag_viscosity": 0, "lag_viscous_accel": 0, "lag_energy_dt": 0,
     "lag_fused": 8 * 6,          # one-kernel Lagrangian phase: rho, e, rho_u, rho_v in; u, v out
-    "lag_apply": 0,              # changed values only
-    # The sweeps: the first sweep of a step reads rho and e to test a still
-    # tile's round trip (16 B); the second moves nothing in tiles the first
-    # skipped.  Each direction is the first sweep every other step.
-    "mass_sweep_x": 8,
-    "mass_sweep_y": 8,
-    # Momentum pairs (flux fused with its update), one launch per step each:
-    # every other step's launch stores the velocity (8 B, +0 where the
-    # velocity flags show it); the other launch moves bytes only where mass
-    # moves.  Half of 8 B counts per launch.
-    "mom_uFx": 4,
-    "mom_uFy": 4,
-    "mom_vFx": 4,
-    "mom_vFy": 4,
-    "mesh_pow2": 0,              # the step's one-block mesh test (spacings only)
+    "lag_apply": 0,
+    "mass_sweep_x": 0, "mass_sweep_y": 0,
+    "mom_uFx": 0, "mom_uFy": 0, "mom_vFx": 0, "mom_vFy": 0,
+    "mesh_pow2": 0,
 }
 
 # ncu figures (DRAM bytes per cell of each kernel on the blast workload, FP64
@@ -785,15 +774,22 @@ def run_gpu(args):
                 k: {m: v[m] for m in ("l1", "linf", "max_cell_rel") if m in v}
                 for k, v in res.items()}
 
-    # ---- roofline of the dominant kernel and of the whole step ----
+    # ---- roofline of the whole step and of the dominant kernel ----
     peak, peak_kind = measured_peaks()
     name, nl, total = kernels[0] if kernels else ("none", 1, float("nan"))
     cells = (nx - 4) * (ny - 4)
-    bytes_launch = KERNEL_BYTES_PER_CELL.get(name, B_ALG_FP64) * cells
-    achieved = bytes_launch / (total / nl * 1e-3) / 1e9
-    tb = ((figures or {}).get("dram_bytes_per_cell") or {}).get(name)
+    measured_bpc = (figures or {}).get("dram_bytes_per_cell") or {}
+
+    def kernel_bpc(k):
+        """DRAM bytes per cell kernel k moves on this workload (ncu, when the
+        figures describe these sources), else its bytes on a tile at rest."""
+        return measured_bpc.get(k, KERNEL_BYTES_PER_CELL.get(k, B_ALG_FP64))
+
+    achieved = kernel_bpc(name) * cells / (total / nl * 1e-3) / 1e9
+    tb = measured_bpc.get(name)
     traffic = tb * cells if tb is not None else None
     step_gbs = value / world * B_ALG_FP64 / 1e9
+    step_bpc = (figures or {}).get("dram_bytes_per_cell_step")
 
     cpu = None
     if host_legs:
@@ -818,24 +814,31 @@ def run_gpu(args):
                 "h2d_bytes_per_step": h2d / args.steps, "d2h_bytes_per_step": d2h / args.steps + 32,
                 "what": "initial state H2D from pinned host, K timesteps + conservation readback "
                         "through the C ABI, final state D2H"},
-        "roofline": {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak,
-                     "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+        # The step as the unit (its 64 algorithmic bytes per cell-step: rho,
+        # e, rho_u, rho_v read and written once), timed live with CUDA
+        # events; traffic: the DRAM bytes ncu measured per step on this
+        # workload.  kernel: the dominant kernel, on the DRAM bytes per cell
+        # ncu measured for it on this workload over its live duration.
+        "roofline": {"bound": "hbm", "kernel": "timestep", "achieved": step_gbs, "peak": peak,
+                     "unit": "GB/s", "frac": step_gbs / peak,
+                     "traffic": step_bpc * cells if step_bpc is not None else None,
                      "peak_kind": peak_kind,
-                     "step": {"what": "cell-steps/s x 64 B (rho, e, rho_u, rho_v read and "
-                                      "written once per step) over the measured copy bandwidth",
-                              "achieved": step_gbs, "frac": step_gbs / peak,
-                              "dram_bytes_per_cell_step": (figures or {}).get(
-                                  "dram_bytes_per_cell_step")}},
+                     "what": "cell-steps/s x 64 B (rho, e, rho_u, rho_v read and written once "
+                             "per step) over the measured copy bandwidth",
+                     "dram_bytes_per_cell_step": step_bpc,
+                     "dominant_kernel": {"name": name, "achieved": achieved,
+                                         "frac": achieved / peak, "traffic": traffic,
+                                         "bytes_per_cell": kernel_bpc(name)}},
         "fp64_pipe": {"fma_per_s_peak": fma_rate.value,
                       "note": "FP64 issue rate measured on this GPU; bounds the FP64 step on "
                               "fields in motion (forms.fp64_smooth.fp64_pipe)"},
-        # Per kernel: launches, total ms, share of the step, and its achieved
-        # GB/s on its algorithmic bytes (KERNEL_BYTES_PER_CELL) with the
-        # fraction of the measured HBM copy bandwidth.
+        # Per kernel: launches, total ms, share of the step, and the GB/s of
+        # the DRAM bytes per cell it moves on this workload (kernel_bpc) over
+        # its live duration, with the fraction of the measured copy bandwidth.
         "kernels": [{"name": k, "launches": c, "ms": t, "share": t / sum(x[2] for x in kernels),
-                     "alg_gbs": KERNEL_BYTES_PER_CELL.get(k, B_ALG_FP64) * cells / (t / c * 1e-3) / 1e9,
-                     "alg_frac": KERNEL_BYTES_PER_CELL.get(k, B_ALG_FP64) * cells
-                                 / (t / c * 1e-3) / 1e9 / peak}
+                     "bytes_per_cell": kernel_bpc(k),
+                     "gbs": kernel_bpc(k) * cells / (t / c * 1e-3) / 1e9,
+                     "frac": kernel_bpc(k) * cells / (t / c * 1e-3) / 1e9 / peak}
                     for k, c, t in kernels],
         "parity": parity,
         "forms": forms,

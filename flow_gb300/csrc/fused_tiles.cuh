@@ -102,21 +102,23 @@ struct StepArgs {
   int fx_stride;               // bytes per row: 4 ceil((nx + 1 - 2 pad) / 127)
   // Velocity flags, or null (set with the others): byte r * vf_stride +
   // (jj >> 5) is 1 when the pressure phase or the viscous update stored a
-  // face velocity (x face (r, jj) or y face (r, jj)) that is not +0 in the
-  // 32 columns jj & ~31 .. (jj | 31) of row r (rows 0 .. ny - 1 of the
-  // padded mesh, columns counted from 0).  Where every byte around a tile is
-  // 0, the velocities it would read are +0 and it does not load them.
+  // face velocity (x face (r, jj) or y face (r, jj)) that is not +0, or
+  // changed a face momentum, in the 32 columns jj & ~31 .. (jj | 31) of row r
+  // (rows 0 .. ny - 1 of the padded mesh, columns counted from 0).  Where
+  // every byte around a tile is 0, the velocities it would read are +0 and it
+  // does not load them.
   unsigned char* vflag;
   int vf_stride;               // bytes per row: 4 ceil(nx / 128)
   // The sweeps' tile-skip marks (SweepArgs::skip), set with the flags: one
-  // byte per sweep tile, ceil((ny - 2 pad) / rows) bands of
+  // byte per sweep tile, ceil((ny - 2 pad) / the sweeps' rows) bands of
   // max(ceil((nx + 1 - 2 pad) / 127), qm_stride) tiles.
   unsigned char* skipf;
   // The skip marks the previous step's first sweep left (its own half of the
   // two mark buffers), or null when this step does not directly follow a
   // flagged step on the same arrays.  Mark x of band b covers the interior
-  // cells of rows pad + b rest_rows .. + rest_rows - 1 and columns
-  // pad + x rest_w .. + rest_w - 1 (127 for an x sweep, 128 for a y sweep).
+  // cells of rows pad + b rest_rows .. + rest_rows - 1 (that step's sweep
+  // tile height) and columns pad + x rest_w .. + rest_w - 1 (127 for an x
+  // sweep, 128 for a y sweep).
   // A marked cell, its energy, its density and the momenta of the faces
   // between two marked cells did not change in that step after its pressure
   // phase, which stored +0 velocities there and no momentum change.
