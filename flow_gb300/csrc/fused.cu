@@ -473,6 +473,48 @@ int finish_step(cudaStream_t s, Mesh* mesh, double* ra, StepProfiler& prof,
   return GB300_OK;
 }
 
+// Where the fused step's flags sit in reduce_array after the reduction
+// partials (ra + kRaQFlags), when it holds them (it has nx*ny doubles, as the
+// arch layer allocates it); a mesh too small for them stores and reads every
+// stress and flux.  Offsets in 4-byte words: the per-tile CFL minima (two
+// words per shock-heating tile) and the conservation totals' tile partials
+// (four words per kConsTile^2 tile) first, 8-byte aligned; then the stress
+// flags ((ny - 2 pad) x stride words), the y mass-flux flags
+// ((ny + 1 - 2 pad) x stride), the x mass-flux flags ((ny - 2 pad) x xtiles),
+// the velocity flags (ny x vtiles) and the skip marks of even and odd steps
+// (a step's first sweep writes its own half; the next step reads it while its
+// own first sweep writes the other).
+constexpr int kConsTile = 128;  // rows and columns of a conservation tile
+struct FlagLayout {
+  bool fits = false;
+  int stride = 0, xtiles = 0, vtiles = 0, cons_tx = 0, cons_ty = 0;
+  size_t cfl = 0, cons = 0, q = 0, fy = 0, fx = 0, v = 0, marks = 0, sk_words = 0;
+};
+FlagLayout flag_layout(int nx, int ny, int pad) {
+  FlagLayout L;
+  L.stride = (nx - 2 * pad + kCols - 1) / kCols;
+  L.xtiles = (nx + 1 - 2 * pad + kCols - 2) / (kCols - 1);
+  L.vtiles = (nx + kCols - 1) / kCols;
+  const long long rows = ny - 2 * pad;
+  if (L.stride <= 0 || rows <= 0) return L;
+  L.cons_tx = (nx - 2 * pad + kConsTile - 1) / kConsTile;
+  L.cons_ty = (int)((rows + kConsTile - 1) / kConsTile);
+  const long long bands = (rows + kRowsLag - 1) / kRowsLag;  // shock-heating tiles
+  const long long sweep_bands = (rows + kRowsSweepStill - 1) / kRowsSweepStill;  // at most
+  L.sk_words = ((size_t)sweep_bands * (L.xtiles > L.stride ? L.xtiles : L.stride) + 3) / 4;
+  L.cfl = 0;
+  L.cons = L.cfl + 2 * (size_t)bands * L.stride;
+  L.q = L.cons + 4 * (size_t)L.cons_tx * L.cons_ty;
+  L.fy = L.q + (size_t)rows * L.stride;
+  L.fx = L.fy + (size_t)(rows + 1) * L.stride;
+  L.v = L.fx + (size_t)rows * L.xtiles;
+  L.marks = L.v + (size_t)ny * L.vtiles;
+  const size_t words = L.marks + 2 * L.sk_words;
+  L.fits = (size_t)kRaQFlags * sizeof(double) + words * sizeof(unsigned) <=
+           (size_t)nx * ny * sizeof(double);
+  return L;
+}
+
 template <typename R>
 void fill_mesh_args(StepArgs<R>& a, const Mesh* mesh, int tt, double* ra) {
   a.nx = mesh->local_nx;
@@ -491,12 +533,6 @@ void fill_mesh_args(StepArgs<R>& a, const Mesh* mesh, int tt, double* ra) {
   a.max_dt = mesh->max_dt;
   a.first_step = (tt == 0);
   a.rows = kRowsLag;
-  // The viscous-stress and mass-flux flags live in reduce_array after the
-  // reduction partials when it holds them (it has nx*ny doubles, as the arch
-  // layer allocates it); a mesh too small for them stores and reads every
-  // stress and flux.  Words: stresses (ny - 2 pad) x stride, y fluxes
-  // (ny + 1 - 2 pad) x stride, x fluxes (ny - 2 pad) x 4-byte words of
-  // x-sweep tiles.
   a.qmask = nullptr;
   a.qm_stride = 0;
   a.fxflag = nullptr;
@@ -509,43 +545,26 @@ void fill_mesh_args(StepArgs<R>& a, const Mesh* mesh, int tt, double* ra) {
   a.rest_w = a.rest_tiles_x = a.rest_rows = 0;
   a.cfl_tile = nullptr;
   a.moving = nullptr;
-  const int stride = (a.nx - 2 * a.pad + kCols - 1) / kCols;
-  const int xtiles = (a.nx + 1 - 2 * a.pad + kCols - 2) / (kCols - 1);
-  const long long rows = a.ny - 2 * a.pad;
-  const size_t q_words = (size_t)rows * stride, fy_words = (size_t)(rows + 1) * stride;
-  const size_t fx_words = (size_t)rows * xtiles;
-  const int vtiles = (a.nx + kCols - 1) / kCols;
-  const size_t v_words = (size_t)a.ny * vtiles;
-  const long long bands = (rows + a.rows - 1) / a.rows;  // shock-heating tiles
-  const long long sweep_bands = (rows + kRowsSweepStill - 1) / kRowsSweepStill;  // at most
-  const size_t sk_words = ((size_t)sweep_bands * (xtiles > stride ? xtiles : stride) + 3) / 4;
-  // Per-tile CFL minima (8 bytes per shock-heating tile) first, then the
-  // 4-byte words: stresses, y fluxes, x fluxes, velocities, and the skip
-  // marks of even and odd steps (a step's first sweep writes its own half;
-  // the next step reads it while its own first sweep writes the other).
-  const size_t cfl_words = 2 * (size_t)bands * stride;
-  const size_t need = (size_t)kRaQFlags * sizeof(double) +
-                      (cfl_words + q_words + fy_words + fx_words + v_words + 2 * sk_words) *
-                          sizeof(unsigned);
-  if (stride > 0 && rows > 0 && need <= (size_t)a.nx * a.ny * sizeof(double)) {
-    a.cfl_tile = reinterpret_cast<unsigned long long*>(ra + kRaQFlags);
-    unsigned* base = reinterpret_cast<unsigned*>(ra + kRaQFlags) + cfl_words;
-    a.qmask = base;
-    a.qm_stride = stride;
-    a.fyflag = reinterpret_cast<unsigned char*>(base + q_words);
-    a.fxflag = reinterpret_cast<unsigned char*>(base + q_words + fy_words);
-    a.fx_stride = 4 * xtiles;
-    a.vflag = reinterpret_cast<unsigned char*>(base + q_words + fy_words + fx_words);
-    a.vf_stride = 4 * vtiles;
-    unsigned* marks = base + q_words + fy_words + fx_words + v_words;
-    a.skipf = reinterpret_cast<unsigned char*>(marks + (tt & 1) * sk_words);
-    // The previous step's half, described; used only where rest_valid says
-    // that step was a flagged step on these arrays.
-    a.rest = reinterpret_cast<unsigned char*>(marks + ((tt + 1) & 1) * sk_words);
+  const FlagLayout L = flag_layout(a.nx, a.ny, a.pad);
+  if (L.fits) {
+    unsigned* base = reinterpret_cast<unsigned*>(ra + kRaQFlags);
+    a.cfl_tile = reinterpret_cast<unsigned long long*>(base + L.cfl);
+    a.qmask = base + L.q;
+    a.qm_stride = L.stride;
+    a.fyflag = reinterpret_cast<unsigned char*>(base + L.fy);
+    a.fxflag = reinterpret_cast<unsigned char*>(base + L.fx);
+    a.fx_stride = 4 * L.xtiles;
+    a.vflag = reinterpret_cast<unsigned char*>(base + L.v);
+    a.vf_stride = 4 * L.vtiles;
+    unsigned* marks = base + L.marks;
+    a.skipf = reinterpret_cast<unsigned char*>(marks + (tt & 1) * L.sk_words);
+    // The previous step's half, described; take_rest keeps it only when
+    // that step was a flagged step on these arrays, and sets its tile height.
+    a.rest = reinterpret_cast<unsigned char*>(marks + ((tt + 1) & 1) * L.sk_words);
     const bool prev_x_first = ((tt - 1) % 2 == 0);
     a.rest_w = prev_x_first ? kCols - 1 : kCols;
-    a.rest_tiles_x = prev_x_first ? xtiles : stride;
-    a.rest_rows = kRowsSweepMoving;  // (take_rest sets the previous step's)
+    a.rest_tiles_x = prev_x_first ? L.xtiles : L.stride;
+    a.rest_rows = kRowsSweepMoving;
     a.moving = reinterpret_cast<unsigned long long*>(ra + kRaMoving);
   }
 }
@@ -609,12 +628,16 @@ int g_lag_rows = lagf::kDefaultRows;
 // and its per-tile CFL minima.
 struct RestRecord {
   std::array<const void*, 12> arrays{};
+  const void* rho = nullptr;             // the state the step advanced
+  const void* e = nullptr;
+  const void* ra = nullptr;
   int nx = 0, ny = 0, pad = 0, form = -1, tt = 0;
   int sweep_rows = 0;                    // the step's sweep tile height
   unsigned long long tiles = 0;          // its first sweep's tiles
   unsigned long long moving = ~0ull;     // of which not skipped (read after the step)
   unsigned long long calls = 0;
   bool valid = false;
+  bool follows = false;                  // it directly followed a flagged step
 };
 thread_local RestRecord t_rest;
 
@@ -625,7 +648,7 @@ thread_local RestRecord t_rest;
 // skipped at least half of its tiles.
 template <typename R>
 int take_rest(StepArgs<R>& a, int tt, int form, const std::array<const void*, 12>& arrays,
-              bool flagged) {
+              bool flagged, const void* rho, const void* e, const void* ra) {
   const unsigned long long calls = mesh_calls();
   const RestRecord& p = t_rest;
   const bool follows = p.valid && flagged && !a.first_step && p.tt + 1 == tt &&
@@ -640,6 +663,9 @@ int take_rest(StepArgs<R>& a, int tt, int form, const std::array<const void*, 12
   const int rows = still ? kRowsSweepStill : kRowsSweepMoving;
   RestRecord r;
   r.arrays = arrays;
+  r.rho = rho;
+  r.e = e;
+  r.ra = ra;
   r.nx = a.nx;
   r.ny = a.ny;
   r.pad = a.pad;
@@ -652,10 +678,185 @@ int take_rest(StepArgs<R>& a, int tt, int form, const std::array<const void*, 12
   r.tiles = tiles_x * (unsigned long long)((a.ny - 2 * a.pad + rows - 1) / rows);
   r.calls = calls;
   r.valid = flagged;
+  r.follows = follows;
   t_rest = r;
   return rows;
 }
 }  // namespace
+
+// ---------------------------------------------------------------------------
+// Conservation totals by tiles (the reference's print_conservation sums,
+// omp3/flow.c:976-994): each kConsTile x kConsTile tile of interior cells
+// keeps its partial sums (sum rho, sum rho e; each thread down its column, the
+// warps and then the four warps of the block in a fixed order) in
+// reduce_array, and the last block adds the partials of all tiles in a fixed
+// order.  A tile whose cells all lay in tiles the last step's first sweep
+// skipped -- at rest through that step, so unchanged since the previous call
+// summed them -- keeps its partials without reading a cell.  The totals
+// depend only on the cells (the same numbers whichever tiles were kept).
+namespace {
+
+struct ConsArgs {
+  const double* rho;
+  const double* e;
+  double* ra;
+  double* part;                // 2 doubles per tile: sum rho, sum rho e
+  int nx, ny, pad, tiles_x, tiles;
+  const unsigned char* marks;  // the last step's skip marks, or null
+  int mark_w, mark_tiles_x, mark_rows;
+};
+
+__device__ __forceinline__ double block_sum_fixed(double x, double* s_w) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+  if ((threadIdx.x & 31) == 0) s_w[threadIdx.x >> 5] = x;
+  __syncthreads();
+  double t = 0.0;
+  if (threadIdx.x == 0) {
+    for (int w = 0; w < kCols / 32; ++w) t += s_w[w];
+  }
+  __syncthreads();
+  return t;  // (thread 0)
+}
+
+__global__ void __launch_bounds__(kCols) k_conservation_tiles(const ConsArgs c) {
+  __shared__ double s_w[kCols / 32];
+  __shared__ bool s_last;
+  const int bx = blockIdx.x % c.tiles_x, by = blockIdx.x / c.tiles_x;
+  const int pad = c.pad;
+  const int c0 = pad + bx * kConsTile, r0 = pad + by * kConsTile;
+  const int c1 = min(c0 + kConsTile, c.nx - pad), r1 = min(r0 + kConsTile, c.ny - pad);
+  bool kept = false;
+  if (c.marks) {
+    const int b0 = (r0 - pad) / c.mark_rows, b1 = (r1 - 1 - pad) / c.mark_rows;
+    const int x0 = (c0 - pad) / c.mark_w, x1 = (c1 - 1 - pad) / c.mark_w;
+    const int nxb = x1 - x0 + 1, total = (b1 - b0 + 1) * nxb;
+    bool ok = true;
+    for (int q = threadIdx.x; q < total; q += blockDim.x) {
+      ok = ok && c.marks[(size_t)(b0 + q / nxb) * c.mark_tiles_x + x0 + q % nxb] != 0;
+    }
+    kept = __syncthreads_and(ok) != 0;
+  }
+  if (!kept) {
+    const int j = c0 + threadIdx.x;
+    double ms = 0.0, es = 0.0;
+    if (j < c1) {
+      constexpr int kB = 8;
+      for (int ib = r0; ib < r1; ib += kB) {
+        double rv[kB], ev[kB];
+#pragma unroll
+        for (int q = 0; q < kB; ++q) {
+          const bool in = ib + q < r1;
+          const size_t k = (size_t)(in ? ib + q : r0) * c.nx + j;
+          rv[q] = in ? c.rho[k] : 0.0;
+          ev[q] = in ? c.e[k] : 0.0;
+        }
+#pragma unroll
+        for (int q = 0; q < kB; ++q) {
+          if (ib + q < r1) {
+            ms = __dadd_rn(ms, rv[q]);
+            es = __fma_rn(rv[q], ev[q], es);
+          }
+        }
+      }
+    }
+    const double tm = block_sum_fixed(ms, s_w);
+    const double te = block_sum_fixed(es, s_w);
+    if (threadIdx.x == 0) {
+      c.part[2 * (size_t)blockIdx.x] = tm;
+      c.part[2 * (size_t)blockIdx.x + 1] = te;
+    }
+  }
+  if (threadIdx.x == 0) {
+    __threadfence();
+    unsigned long long* ticket = reinterpret_cast<unsigned long long*>(c.ra + kRaTicket);
+    s_last = (atomicAdd(ticket, 1ull) == (unsigned long long)gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  double a = 0.0, b = 0.0;
+  for (int k = threadIdx.x; k < c.tiles; k += blockDim.x) {
+    a = __dadd_rn(a, __ldcg(c.part + 2 * (size_t)k));
+    b = __dadd_rn(b, __ldcg(c.part + 2 * (size_t)k + 1));
+  }
+  const double ta = block_sum_fixed(a, s_w);
+  const double tb = block_sum_fixed(b, s_w);
+  if (threadIdx.x == 0) {
+    c.ra[kRaMass] = ta;
+    c.ra[kRaEnergy] = tb;
+    *reinterpret_cast<unsigned long long*>(c.ra + kRaTicket) = 0ull;
+  }
+}
+
+// The call the tile partials were last written by, and the mesh-call count
+// then: the next call may keep tiles only when exactly one mesh call (the
+// step's own) came between.
+struct ConsRecord {
+  const void* rho = nullptr;
+  const void* e = nullptr;
+  const void* ra = nullptr;
+  int nx = 0, ny = 0, pad = 0;
+  unsigned long long calls = 0;
+  bool valid = false;
+  bool after_step = false;  // right after a flagged step on this state ...
+  int step_tt = 0;          // ... of this index
+};
+thread_local ConsRecord t_cons;
+
+}  // namespace
+
+bool tile_conservation(int nx, int ny, int pad, const double* rho, const double* e,
+                       double* ra, cudaStream_t s) {
+  const FlagLayout L = flag_layout(nx, ny, pad);
+  if (!L.fits) return false;
+  unsigned* base = reinterpret_cast<unsigned*>(ra + kRaQFlags);
+  ConsArgs c{};
+  c.rho = rho;
+  c.e = e;
+  c.ra = ra;
+  c.part = reinterpret_cast<double*>(base + L.cons);
+  c.nx = nx;
+  c.ny = ny;
+  c.pad = pad;
+  c.tiles_x = L.cons_tx;
+  c.tiles = L.cons_tx * L.cons_ty;
+  c.marks = nullptr;
+  const unsigned long long calls = mesh_calls();
+  const RestRecord& p = t_rest;
+  const ConsRecord& q = t_cons;
+  // Right after a flagged step that advanced this state and directly
+  // followed the step after which the partials were last written, on the same
+  // arrays, with only that step's own mesh call in between: the state the
+  // partials describe is the one that step started from.
+  const bool after_step = p.valid && p.calls == calls && p.rho == rho && p.e == e &&
+                          p.ra == ra && p.nx == nx && p.ny == ny && p.pad == pad;
+  if (after_step && p.follows && q.valid && q.after_step && q.step_tt + 1 == p.tt &&
+      q.calls + 1 == calls && q.rho == rho && q.e == e && q.ra == ra && q.nx == nx &&
+      q.ny == ny && q.pad == pad) {
+    const bool x_first = (p.tt % 2 == 0);
+    c.marks = reinterpret_cast<const unsigned char*>(base + L.marks + (p.tt & 1) * L.sk_words);
+    c.mark_w = x_first ? kCols - 1 : kCols;
+    c.mark_tiles_x = x_first ? L.xtiles : L.stride;
+    c.mark_rows = p.sweep_rows;
+  }
+  cudaMemsetAsync(ra + kRaTicket, 0, sizeof(double), s);
+  k_conservation_tiles<<<(unsigned)c.tiles, kCols, 0, s>>>(c);
+  count_launches(1);
+  ConsRecord r;
+  r.rho = rho;
+  r.e = e;
+  r.ra = ra;
+  r.nx = nx;
+  r.ny = ny;
+  r.pad = pad;
+  r.calls = calls;
+  r.valid = cudaPeekAtLastError() == cudaSuccess;
+  r.after_step = after_step;
+  r.step_tt = p.tt;
+  t_cons = r;
+  return true;
+}
 
 int set_lagrangian_rows(int rows) {
   if (rows < 1 || rows > lagf::kMaxRows) {
@@ -722,7 +923,7 @@ int fused_solve(Mesh* mesh, int tt, double* P, double* rho, double* rho_old,
   }
   const int sweep_rows =
       take_rest(a, tt, 0, {P, rho, e, rho_u, rho_v, uF_y, vF_x, uF_x, vF_y, F_x, F_y, reduce_array},
-                a.skipf != nullptr && lagp == nullptr);
+                a.skipf != nullptr && lagp == nullptr, rho, e, reduce_array);
   StepProfiler prof;
   prof.begin(s);
   launch_step(s, a, tt, first, second, prof, sweep_rows, lagp);
@@ -795,7 +996,7 @@ int mixed_solve(Mesh* mesh, int tt, double* rho, double* e, float* rho_u,
   const int sweep_rows =
       take_rest(a, tt, 1, {rho, e, rho_u, rho_v, work, reduce_array, nullptr, nullptr, nullptr,
                            nullptr, nullptr, nullptr},
-                a.skipf != nullptr);
+                a.skipf != nullptr, rho, e, reduce_array);
   StepProfiler prof;
   prof.begin(s);
   launch_step(s, a, tt, first, second, prof, sweep_rows);

@@ -22,6 +22,12 @@ int num_sms();
 // when exactly one such call -- its own -- came between them.
 unsigned long long mesh_calls();
 void note_state_write();
+// Conservation totals of the interior (reduce_array[3..4]) by tiles whose
+// partial sums stay in reduce_array's flag region, kept across calls for tiles
+// at rest through the fused step between them; false (nothing launched) when
+// reduce_array is too small for the region.
+bool tile_conservation(int nx, int ny, int pad, const double* rho, const double* e,
+                       double* ra, cudaStream_t s);
 // Kernel launches issued by this library (the fused step's kernels and the
 // conservation totals), for gb300_launch_count.
 void count_launches(unsigned n);

@@ -392,7 +392,9 @@ int st_conservation(int nx, int ny, int pad, const double* rho, const double* e,
   FLOW_TRY(check_sizes(nx, ny, pad, "conservation"));
   if (!reduce_array) return record_error(GB300_ERR_ARG, "conservation: reduce_array is NULL");
   cudaStream_t s = current_stream();
-  launch_conservation(s, nx, ny, pad, rho, e, reduce_array);
+  if (!tile_conservation(nx, ny, pad, rho, e, reduce_array, s)) {
+    launch_conservation(s, nx, ny, pad, rho, e, reduce_array);
+  }
   FLOW_TRY(check_launch("conservation"));
   if (!sync) return GB300_OK;
   double local[2];

@@ -104,3 +104,26 @@ def test_state_written_between_steps(fg):
     for f in STATE:
         assert torch.equal(a.a[f], b.a[f]), f
     assert a.mesh.dt == b.mesh.dt and a.mesh.dt_h == b.mesh.dt_h
+
+
+def test_conservation_kept_tiles_equal_fresh_sums(fg):
+    """The conservation totals after each step keep the partial sums of tiles
+    at rest through that step; they must equal, bit for bit, the totals summed
+    afresh from the same cells (a copy of the state in other arrays)."""
+    import ctypes
+    import torch
+    p = problems_with_flags()["wide_blast"]
+    a = fg.DeviceSim(p)
+    a.initial_timestep()
+    kept, states = [], []
+    for _ in range(12):
+        a.step()
+        kept.append(a.conservation())
+        states.append((a.a["rho"].clone(), a.a["e"].clone()))
+    L = fg.lib()
+    ra = torch.zeros_like(a.a["reduce"])
+    out = (ctypes.c_double * 2)()
+    for k, (rho, e) in enumerate(states):
+        assert L.gb300_conservation(a.nx, a.ny, 2, fg.dptr(rho), fg.dptr(e), fg.dptr(ra),
+                                    ctypes.cast(out, ctypes.POINTER(ctypes.c_double)), 1) == 0
+        assert (out[0], out[1]) == kept[k], k
