@@ -272,17 +272,33 @@ __device__ __forceinline__ bool tile_vel_still(const A& a, int r0, int r1, int c
   return __syncthreads_or(any) == 0;
 }
 
-// Whether every cell of rows r0 .. r1 - 1 and columns c0 .. c1 - 1 (interior
-// cells only) was at rest through the previous step by its first sweep's skip
-// marks (StepArgs::rest).  Block-uniform (barrier); called by every thread of
-// the block.  False without marks.
+// Whether every cell of rows r0 .. r1 - 1 and columns c0 .. c1 - 1 was at rest
+// through the previous step by its first sweep's skip marks (StepArgs::rest).
+// A ghost cell holds the mirror image of one of the pad interior cells next
+// to its wall, written together with it, so a range reaching into the ghosts
+// is tested on the interior cells up to those.  Block-uniform (barrier);
+// called by every thread of the block.  False without marks.
 template <typename A>
 __device__ __forceinline__ bool rest_cells(const A& a, int r0, int r1, int c0, int c1) {
   if (!a.rest) return false;  // uniform
   const int pad = a.pad;
-  if (r0 < pad || c0 < pad || r1 > a.ny - pad || c1 > a.nx - pad || r0 >= r1 || c0 >= c1) {
-    return false;
+  if (r0 < pad) {
+    r0 = pad;
+    r1 = max(r1, 2 * pad);
   }
+  if (r1 > a.ny - pad) {
+    r1 = a.ny - pad;
+    r0 = min(r0, a.ny - 2 * pad);
+  }
+  if (c0 < pad) {
+    c0 = pad;
+    c1 = max(c1, 2 * pad);
+  }
+  if (c1 > a.nx - pad) {
+    c1 = a.nx - pad;
+    c0 = min(c0, a.nx - 2 * pad);
+  }
+  if (r0 >= r1 || c0 >= c1) return false;
   const int b0 = (r0 - pad) / a.rest_rows, b1 = (r1 - 1 - pad) / a.rest_rows;
   const int x0 = (c0 - pad) / a.rest_w, x1 = (c1 - 1 - pad) / a.rest_w;
   const int nxb = x1 - x0 + 1, total = (b1 - b0 + 1) * nxb;
@@ -604,14 +620,12 @@ __device__ __forceinline__ void tile_lag_pressure(const StepArgs<R>& a, int bx, 
   if constexpr (kFl) {
     // A tile whose cells (and the row above and column left it reads) were
     // at rest through the previous step: its pressures, momenta, velocities
-    // and velocity flags are what that step's pressure phase stored, from
-    // the same densities, energies and momenta, and nothing has written them
-    // since -- this phase would store the same numbers.
+    // (with their ghost images) and velocity flags are what that step's
+    // pressure phase stored, from the same densities, energies and momenta,
+    // and nothing has written them since -- this phase would store the same
+    // numbers.
     const int c0 = bx * kCols, i0 = by * a.rows;
-    if (a.rest && !tile_near_edge(a.nx, a.ny, a.pad, c0, i0, a.rows) &&
-        rest_cells(a, i0 - 1, i0 + a.rows, c0 - 1, c0 + kCols)) {
-      return;
-    }
+    if (a.rest && rest_cells(a, i0 - 1, i0 + a.rows, c0 - 1, c0 + kCols)) return;
   }
   FLOW_POW2_DISPATCH(R, a, bx * kCols, by * a.rows,
                      (tile_lag_pressure_impl<R, true, kFl>(a, bx, by)),
@@ -1187,8 +1201,7 @@ __device__ __forceinline__ void tile_lag_energy_dt(const StepArgs<R>& a, int bx,
       const int nx = a.nx, ny = a.ny, pad = a.pad;
       const int cb = pad + bx * kCols, i0 = pad + by * a.rows;
       const int i1 = min(i0 + a.rows, ny - pad);
-      if (!tile_near_edge(nx, ny, pad, cb, i0, a.rows) &&
-          tile_vel_still(a, i0 - 2, i1 + 2, cb - 2, cb + kCols + 2) &&
+      if (tile_vel_still(a, i0 - 2, i1 + 2, cb - 2, cb + kCols + 2) &&
           rest_cells(a, i0, i1, cb, min(cb + kCols, nx - pad))) {
         if (threadIdx.x == 0) {
           const unsigned long long b = a.cfl_tile[(size_t)by * a.qm_stride + bx];
@@ -2320,7 +2333,7 @@ __device__ __forceinline__ void tile_mom_x_impl(const StepArgs<R>& a, int bx, in
       const bool zero = tile_vel_still(a, i0 - 2, i1 + 2, c0 - 2, c0 + kCols + 2);
       // Velocities all +0 whose cells were at rest through the previous
       // step, when this pair stored (or kept) +0 for each of them: they stand.
-      if (zero && !edge && rest_cells(a, i0 - 1, i1, c0 - 1, c0 + kCols)) return;
+      if (zero && rest_cells(a, i0 - 1, i1, c0 - 1, c0 + kCols)) return;
       copy_velocities<R, !kV>(a, edge, kV ? a.v : a.u, kV ? a.v_out : a.u_out, i0, i1, j, upd,
                               zero);
       return;
@@ -2565,7 +2578,7 @@ __device__ __forceinline__ void tile_mom_y_impl(const StepArgs<R>& a, int bx, in
     const int cb = pad + bx * kCols;
     if (tile_mass_still(a, i0 - 1, i1, cb - 1, cb + kCols)) {
       const bool zero = tile_vel_still(a, i0 - 2, i1 + 2, cb - 2, cb + kCols + 2);
-      if (zero && !edge && rest_cells(a, i0 - 1, i1, cb - 1, cb + kCols)) return;
+      if (zero && rest_cells(a, i0 - 1, i1, cb - 1, cb + kCols)) return;
       copy_velocities<R, !kV>(a, edge, kV ? a.v : a.u, kV ? a.v_out : a.u_out, i0, i1, jj,
                               jj < (kV ? nx - pad : nx + 1 - pad), zero);
       return;
