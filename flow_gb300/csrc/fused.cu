@@ -67,6 +67,7 @@ __global__ void __launch_bounds__(kCols) k_lag_pressure(const StepArgs<R> a) {
   if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) {
     *reinterpret_cast<unsigned long long*>(a.ra + kRaTicket) = 0ull;
     *a.min_slot = ~0ull;
+    if (a.moving) *a.moving = 0ull;
   }
   tile_lag_pressure<R, kFl>(a, blockIdx.x, blockIdx.y);
 }
@@ -362,16 +363,21 @@ inline int apply_blocks(const lagf::LagArgs& l) {
 // One timestep of either form; first/second are the two mass sweeps' buffers.
 // lag: the FP64 form's one-kernel Lagrangian phase (k_lag_fused +
 // k_lag_apply), or null for the four separate Lagrangian kernels.
+// mesh_known: the step directly follows a step on the same mesh arrays (no
+// mesh call between), whose spacing test reduce_array still holds.
 template <typename R>
 void launch_step(cudaStream_t s, const StepArgs<R>& a, int tt,
                  const SweepArgs<R>& first, const SweepArgs<R>& second,
-                 StepProfiler& prof, int sweep_rows, const lagf::LagArgs* lag = nullptr) {
+                 StepProfiler& prof, int sweep_rows, bool mesh_known,
+                 const lagf::LagArgs* lag = nullptr) {
   const int nx = a.nx, ny = a.ny, pad = a.pad;
-  // The whole-mesh spacing test the tiles read (the mesh may change between
-  // calls, so it is formed every step; one block, a few microseconds).
-  prof.mark("mesh_pow2");
-  launch_pdl_block(k_mesh_pow2, dim3(1), dim3(kPow2Threads), s, nx, ny, a.celldx, a.edgedx,
-                   a.celldy, a.edgedy, const_cast<unsigned long long*>(a.mesh_pow2), a.ra);
+  // The whole-mesh spacing test the tiles read (one block, a few
+  // microseconds), formed unless the previous step's still stands.
+  if (!mesh_known) {
+    prof.mark("mesh_pow2");
+    launch_pdl_block(k_mesh_pow2, dim3(1), dim3(kPow2Threads), s, nx, ny, a.celldx, a.edgedx,
+                     a.celldy, a.edgedy, const_cast<unsigned long long*>(a.mesh_pow2), a.ra);
+  }
   if (lag) {
     const int nty = (ny - 2 * pad + lag->rows - 1) / lag->rows;
     prof.mark("lag_fused");
@@ -628,6 +634,7 @@ int g_lag_rows = lagf::kDefaultRows;
 // and its per-tile CFL minima.
 struct RestRecord {
   std::array<const void*, 12> arrays{};
+  std::array<const void*, 4> mesh{};     // its spacing arrays
   const void* rho = nullptr;             // the state the step advanced
   const void* e = nullptr;
   const void* ra = nullptr;
@@ -651,9 +658,10 @@ int take_rest(StepArgs<R>& a, int tt, int form, const std::array<const void*, 12
               bool flagged, const void* rho, const void* e, const void* ra) {
   const unsigned long long calls = mesh_calls();
   const RestRecord& p = t_rest;
+  const std::array<const void*, 4> mesh{a.edgedx, a.edgedy, a.celldx, a.celldy};
   const bool follows = p.valid && flagged && !a.first_step && p.tt + 1 == tt &&
                        p.calls + 1 == calls && p.form == form && p.nx == a.nx &&
-                       p.ny == a.ny && p.pad == a.pad && p.arrays == arrays;
+                       p.ny == a.ny && p.pad == a.pad && p.arrays == arrays && p.mesh == mesh;
   if (follows) {
     a.rest_rows = p.sweep_rows;
   } else {
@@ -663,6 +671,7 @@ int take_rest(StepArgs<R>& a, int tt, int form, const std::array<const void*, 12
   const int rows = still ? kRowsSweepStill : kRowsSweepMoving;
   RestRecord r;
   r.arrays = arrays;
+  r.mesh = mesh;
   r.rho = rho;
   r.e = e;
   r.ra = ra;
@@ -926,7 +935,7 @@ int fused_solve(Mesh* mesh, int tt, double* P, double* rho, double* rho_old,
                 a.skipf != nullptr && lagp == nullptr, rho, e, reduce_array);
   StepProfiler prof;
   prof.begin(s);
-  launch_step(s, a, tt, first, second, prof, sweep_rows, lagp);
+  launch_step(s, a, tt, first, second, prof, sweep_rows, a.rest != nullptr, lagp);
   unsigned long long moving = ~0ull;
   const int st = finish_step(s, mesh, reduce_array, prof, "solve_hydro_2d (fused)", &moving);
   if (st != GB300_OK) t_rest.valid = false;
@@ -999,7 +1008,7 @@ int mixed_solve(Mesh* mesh, int tt, double* rho, double* e, float* rho_u,
                 a.skipf != nullptr, rho, e, reduce_array);
   StepProfiler prof;
   prof.begin(s);
-  launch_step(s, a, tt, first, second, prof, sweep_rows);
+  launch_step(s, a, tt, first, second, prof, sweep_rows, a.rest != nullptr);
   unsigned long long moving = ~0ull;
   const int st = finish_step(s, mesh, reduce_array, prof, "gb300_mixed_solve", &moving);
   if (st != GB300_OK) t_rest.valid = false;
