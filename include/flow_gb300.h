@@ -221,7 +221,11 @@ int gb300_solve_hydro_2d(Mesh* mesh, int tt, double* P, double* rho,
                          double* reduce_array);
 
 /* Interior totals: out[0] = sum rho, out[1] = sum rho*e (host array).  With
- * sync = 0 the totals stay in reduce_array[3..4] and out is not written. */
+ * sync = 0 the totals stay in reduce_array[3..4] and out is not written.
+ * Where reduce_array holds the fused step's flag region the sums are formed by
+ * 128x128 tiles whose partial sums stay there; a call directly after a fused
+ * step keeps the partials of the tiles that step left at rest (see
+ * gb300_state_changed).  The totals depend only on the cells. */
 int gb300_conservation(int nx, int ny, int pad, const double* rho,
                        const double* e, double* reduce_array, double* out,
                        int sync);
