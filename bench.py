@@ -807,7 +807,9 @@ def run_gpu(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic",
         "config": {"workload": f"{args.workload}_{n}_fp64", "nx": n, "ny": n, "form": "fp64",
-                   "iterations_timed": args.steps, "l2": "inputs larger than L2 (2 GB state)",
+                   "iterations_timed": args.steps, "l2": "inputs larger than L2 (2.3 GB state), no flush; a step re-reads only the "
+                         "tiles that move (0.9 DRAM B/cell-step, ncu), whose data and the "
+                         "flags may stay in L2 from one step to the next as in any run",
                    "parallelism": "replicas" if world > 1 else "single GPU",
                    "hbm_fraction_of_step": value / world * B_ALG_FP64 / (peak * 1e9)},
         "e2e": {"value": e2e_value, "unit": UNIT,
